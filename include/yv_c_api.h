@@ -1,0 +1,226 @@
+/*
+ * yv_c_api.h - C ABI of the GB300 sparse-voxel-octree / brick-volume ray caster.
+ *
+ * Plain C types only (pointers, sizes, PODs); no C++ or torch types cross this
+ * boundary.  Every function returns a yv_status (0 = ok); nothing aborts and
+ * no exception escapes.  One renderer object per host thread.
+ *
+ * Device pointers are passed as void* and streams as void* (a cudaStream_t;
+ * NULL = legacy default stream).
+ *
+ * Reference interfaces replaced (paths inside znah/yoxel-voxel):
+ *   ISVORenderer            cell/svorenderer.h:5-31
+ *   RendererBase            cell/renderer_base.h:7-62
+ *   CUDA SVORenderer        demo/SVORenderer.h:8-64, demo/SVORenderer.cpp:39-149
+ *   SVOData / VoxNode       cell/svodata.h:22-55, reaction/report/main.tex:36-56
+ *   ntree RunTrace C ABI    ntree/ntree_trace.cuh:22-28
+ *   Python CudaRenderer     trace_cuda.py:17-120
+ */
+#ifndef YV_C_API_H
+#define YV_C_API_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Status codes                                                             */
+/* ------------------------------------------------------------------------ */
+typedef int32_t yv_status;
+#define YV_OK                 0
+#define YV_ERR_INVALID_ARG    1  /* NULL pointer, bad size, bad enum          */
+#define YV_ERR_NO_SCENE       2  /* render before a scene was set             */
+                                 /* (RenderFrame returns NULL in the reference:
+                                    cell/ppu_renderer.cpp:78-79)              */
+#define YV_ERR_BAD_POOL       3  /* node/brick pool failed validation         */
+#define YV_ERR_ITERATION_CAP  4  /* a ray hit the per-ray iteration cap       */
+#define YV_ERR_TIMEOUT        5  /* a bounded device wait gave up             */
+#define YV_ERR_CUDA           6  /* a CUDA runtime call failed                */
+#define YV_ERR_OUT_OF_MEMORY  7
+#define YV_ERR_IO             8  /* file could not be read / written          */
+#define YV_ERR_UNSUPPORTED    9
+
+/* Human-readable name of a status code (static string). */
+const char* yv_status_string(yv_status s);
+
+/* Detail text of the last failure in this process (CUDA error string or the
+ * validation failure); empty if none.  Valid until the next failing call. */
+const char* yv_last_error(void);
+
+/* ------------------------------------------------------------------------ */
+/* Scene data: the reference SVO node layout                                */
+/* ------------------------------------------------------------------------ */
+
+/* VoxNode, 40 bytes (reaction/report/main.tex:38-52, cell/svodata.h:22-55).
+ *   flags bits 0..7  : child i is a leaf (child[i] holds VoxData)
+ *   flags bits 8..15 : child i is null (EmptyNode / FullNode)
+ *   flags bit  19    : empty flag
+ *   data             : coarse-LOD VoxData of the subtree (not used by tracing)
+ *   child[i]         : node index, VoxData (leaf) or a null id (bit 31 set).
+ * Child order: bit 0 of i = +x half, bit 1 = +y half, bit 2 = +z half.
+ * VoxData of a leaf is an index into the leaf attribute array. */
+typedef struct yv_vox_node {
+  uint32_t flags;
+  uint32_t data;
+  uint32_t child[8];
+} yv_vox_node;
+
+#define YV_EMPTY_NODE 0x80000000u /* main.tex:54 */
+#define YV_FULL_NODE  0x80000001u /* main.tex:55 */
+
+/* Leaf attribute (8 bytes): uint8 RGB colour + int8x3 quantised normal
+ * (127 * unit normal), the colour/normal pair of ore/src/main.cpp:37-51. */
+typedef struct yv_leaf_attr {
+  uint8_t r, g, b, a;
+  int8_t nx, ny, nz, nw;
+} yv_leaf_attr;
+
+/* Host-side SVO container produced by a generator or a loader. */
+typedef struct yv_svo_host yv_svo_host;
+
+/* Seeded sphere-union scene in a 2^depth grid: n spheres, centres uniform in
+ * the grid, radius uniform in [rmin, rmax] voxels, one random RGB per sphere;
+ * surface voxel = inside the union with >= 1 of its 6 neighbours outside;
+ * normal = normalize(voxel centre - centre of the first sphere holding it);
+ * interior subtrees = FullNode.  (Surface rule of scene_gen.py:32-66.) */
+yv_status yv_svo_gen_spheres(yv_svo_host** out, int depth, int n_spheres,
+                             float rmin, float rmax, uint64_t seed);
+
+/* Seeded terrain scene in a 2^depth grid: 6-octave value-noise heightfield
+ * (amplitude 0.3 of the grid height, solid below the surface) plus n_cubes
+ * floating axis-aligned cubes of side [cube_min, cube_max] voxels.  Normals
+ * from heightfield central differences (scene_gen.py:49-53) or from the cube
+ * centre. */
+yv_status yv_svo_gen_terrain(yv_svo_host** out, int depth, int n_cubes,
+                             int cube_min, int cube_max, uint64_t seed);
+
+/* Copy caller arrays into a host container (caller keeps ownership). */
+yv_status yv_svo_from_arrays(yv_svo_host** out, const yv_vox_node* nodes,
+                             uint32_t count, uint32_t root,
+                             const yv_leaf_attr* attrs, uint32_t nattrs);
+
+/* .vox file (SVOData::Load, cell/svodata.h:31-50): little-endian
+ * uint32 root, uint32, uint32, uint32 size, VoxNode[size]; followed by an
+ * optional attribute section "YVAT" uint32 count, yv_leaf_attr[count]. */
+yv_status yv_svo_load_vox(yv_svo_host** out, const char* path);
+yv_status yv_svo_save_vox(const yv_svo_host* svo, const char* path);
+
+void               yv_svo_free(yv_svo_host* svo);
+uint32_t           yv_svo_node_count(const yv_svo_host* svo);
+uint32_t           yv_svo_root(const yv_svo_host* svo);
+const yv_vox_node* yv_svo_nodes(const yv_svo_host* svo);
+uint32_t           yv_svo_attr_count(const yv_svo_host* svo);
+const yv_leaf_attr* yv_svo_attrs(const yv_svo_host* svo);
+/* Tree depth (levels of nodes below the root that carry leaves); 0 if empty. */
+int                yv_svo_depth(const yv_svo_host* svo);
+
+/* Host-side validation: child indices in range, leaf VoxData < nattrs,
+ * depth <= 16, no cycles.  YV_OK or YV_ERR_BAD_POOL. */
+yv_status yv_svo_validate(const yv_vox_node* nodes, uint32_t count,
+                          uint32_t root, uint32_t nattrs);
+
+/* ------------------------------------------------------------------------ */
+/* SVO renderer (ISVORenderer / SVORenderer)                                */
+/* ------------------------------------------------------------------------ */
+typedef struct yv_renderer yv_renderer;
+
+/* Directional light + shading (Lambert: ambient + diffuse * max(0, n.L)).
+ * shadows != 0 casts one hard-shadow ray per primary hit toward dir. */
+typedef struct yv_light {
+  float dir[3];     /* direction toward the light (normalised by the caller) */
+  float ambient;
+  float diffuse;
+  int32_t shadows;
+} yv_light;
+
+/* Output buffers of one frame, all DEVICE pointers, each optional (NULL):
+ *   rgba      : uint32 per pixel, R | G<<8 | B<<16 | A<<24 (Color32)
+ *   hit       : uint32 per pixel, (reference node id << 3) | child, or
+ *               0xFFFFFFFF for a miss (TraceResult, cell/ppu_renderer.cpp:8-13)
+ *   hit_t     : float per pixel, t of the hit (max(t1) of the leaf box)
+ *   fetches   : uint32 per pixel, node dereferences of the primary ray
+ *               (RecTrace calls that reach cell/ppu_renderer.cpp:23)
+ *   shadow_fetches : uint32 per pixel, same for the shadow ray
+ * Row-major, y*width + x. */
+typedef struct yv_frame_outputs {
+  void* rgba;
+  void* hit;
+  void* hit_t;
+  void* fetches;
+  void* shadow_fetches;
+} yv_frame_outputs;
+
+/* Counters of the last frame (read by yv_renderer_frame_stats). */
+typedef struct yv_frame_stats {
+  uint64_t primary_rays;
+  uint64_t hits;
+  uint64_t shadow_rays;
+  uint64_t shadowed;
+  uint32_t status;       /* yv_status of the device side */
+  uint32_t launches;     /* kernels launched for the frame */
+} yv_frame_stats;
+
+/* Launch configuration (the autotuned knobs).  Zero fields = defaults. */
+typedef struct yv_launch_config {
+  int32_t block_threads;   /* threads per block (multiple of 32)          */
+  int32_t blocks_per_sm;   /* resident blocks per SM for the persistent grid */
+  int32_t smem_nodes;      /* top-of-tree nodes staged in shared memory   */
+  int32_t tile_rays;       /* rays a warp takes per queue pop (32|64|128) */
+} yv_launch_config;
+
+yv_status yv_renderer_create(yv_renderer** out);
+void      yv_renderer_destroy(yv_renderer* r);
+
+/* ISVORenderer::SetScene.  Copies the pool to the device in the renderer's
+ * own layout; the caller keeps ownership of its arrays. */
+yv_status yv_set_scene_svo(yv_renderer* r, const yv_vox_node* nodes,
+                           uint32_t count, uint32_t root,
+                           const yv_leaf_attr* attrs, uint32_t nattrs);
+yv_status yv_set_scene_host(yv_renderer* r, const yv_svo_host* svo);
+yv_status yv_load_scene_vox(yv_renderer* r, const char* path);
+
+/* Camera: ISVORenderer::SetViewPos/SetViewDir/SetViewUp/SetResolution/
+ * GetResolution/SetFOV (cell/svorenderer.h:12-21).  Defaults follow
+ * RendererBase (cell/renderer_base.h:25): up (0,0,1), fov 70, 640x480. */
+yv_status yv_set_view_pos(yv_renderer* r, const float pos[3]);
+yv_status yv_set_view_dir(yv_renderer* r, const float dir[3]);
+yv_status yv_set_view_up(yv_renderer* r, const float up[3]);
+yv_status yv_set_resolution(yv_renderer* r, int width, int height);
+yv_status yv_get_resolution(const yv_renderer* r, int* width, int* height);
+yv_status yv_set_fov(yv_renderer* r, float fov_deg);
+yv_status yv_set_light(yv_renderer* r, const yv_light* light);
+yv_status yv_set_launch_config(yv_renderer* r, const yv_launch_config* cfg);
+yv_status yv_get_launch_config(const yv_renderer* r, yv_launch_config* cfg);
+
+/* ISVORenderer::RenderFrame.  Synchronous.  Writes RGBA8 to host_rgba
+ * and/or device_rgba (either may be NULL; width*height uint32 each) on the
+ * given stream, waits for it and returns the device status. */
+yv_status yv_render_frame(yv_renderer* r, uint32_t* host_rgba,
+                          void* device_rgba, void* stream);
+
+/* Asynchronous form of SVORenderer::Render(void* d_dstBuf): enqueues the
+ * frame on `stream` writing the requested device outputs.  No host sync;
+ * the status is read later with yv_renderer_frame_stats. */
+yv_status yv_render_frame_async(yv_renderer* r, const yv_frame_outputs* out,
+                                void* stream);
+
+/* Synchronises the last frame's stream and returns its counters. */
+yv_status yv_renderer_frame_stats(yv_renderer* r, yv_frame_stats* stats);
+
+/* Fills the camera basis the kernels use (RendererBase::InitRayDir,
+ * cell/renderer_base.h:50-61): dir0, du, dv (3 floats each). */
+yv_status yv_get_ray_basis(const yv_renderer* r, float dir0[3], float du[3],
+                           float dv[3]);
+
+/* Number of nodes of the device copy and bytes it occupies. */
+yv_status yv_get_device_scene_info(const yv_renderer* r, uint64_t* nodes,
+                                   uint64_t* device_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* YV_C_API_H */

@@ -1,0 +1,205 @@
+"""ctypes binding of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as
+the checker, and by bench.py's CPU-baseline / reference legs.  The product
+(libyoxel.so and the yoxel package) never imports it.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def load_library(build_if_missing=True):
+    path = os.path.join(HERE, "liboracle.so")
+    if build_if_missing:
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("_oracle_build", os.path.join(HERE, "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        try:
+            mod.build()
+        except Exception:
+            if not os.path.exists(path):
+                raise
+    lib = C.CDLL(path)
+    P = C.c_void_p
+    F = C.c_float
+    D = C.c_double
+    I = C.c_int
+    U = C.c_uint32
+    sig = {
+        "orc_init_ray_dir_f32": (None, [P, P, F, I, I, P, P, P]),
+        "orc_init_ray_dir_f64": (None, [P, P, D, I, I, P, P, P]),
+        "orc_svo_render_f32": (I, [P, U, U, P, U, P, P, P, P, I, I, P, F, F, I, I, I,
+                                   P, P, P, P, P, P]),
+        "orc_svo_render_mt": (I, [I, P, U, U, P, U, P, P, P, P, I, I, P, F, F, I,
+                                  P, P, P, P, P, P]),
+        "orc_svo_hits_f64": (I, [P, U, U, P, P, P, D, I, I, I, I, P, P]),
+        "orc_svo_trace_ray_f32": (I, [P, U, U, P, P, I, P, P, P, P]),
+        "orc_find_first_child_f32": (None, [P, P, P]),
+        "orc_go_next_f32": (I, [P, P, P]),
+        "orc_setup_trace_f32": (I, [P, P, P, P, P]),
+        "orc_brick_render_f64": (I, [P, U, P, P, U, I, P, P, P, P, I, I, D, D, I, I, P, P, P]),
+        "orc_brick_render_f32": (I, [P, U, P, P, U, I, P, P, P, P, I, I, F, F, I, I, P, P, P]),
+        "orc_brick_render_mt_f32": (I, [I, P, U, P, P, U, I, P, P, P, P, I, I, F, F, P, P, P]),
+        "orc_brick_backward_f64": (I, [P, U, P, P, U, I, P, P, P, P, I, I, D, D, P, P, P]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    return lib
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = load_library()
+    return _lib
+
+
+_KEEP = []
+
+
+def _p(a):
+    """Pointer to a numpy array's data.  The array is kept alive until the
+    next _release() so temporaries survive the ctypes call."""
+    if a is None:
+        return None
+    _KEEP.append(a)
+    return C.c_void_p(a.ctypes.data)
+
+
+def _release():
+    del _KEEP[:]
+
+
+def _keeps(fn):
+    def w(*a, **k):
+        mark = len(_KEEP)
+        try:
+            return fn(*a, **k)
+        finally:
+            del _KEEP[mark:]
+    w.__name__ = fn.__name__
+    w.__doc__ = fn.__doc__
+    return w
+
+
+def f32(v):
+    return np.ascontiguousarray(np.asarray(v, dtype=np.float32).reshape(-1))
+
+
+def f64(v):
+    return np.ascontiguousarray(np.asarray(v, dtype=np.float64).reshape(-1))
+
+
+@_keeps
+def init_ray_dir_f32(dir_, up, fov, width, height):
+    d0, du, dv = (np.zeros(3, np.float32) for _ in range(3))
+    lib().orc_init_ray_dir_f32(_p(f32(dir_)), _p(f32(up)), float(fov), width, height,
+                               _p(d0), _p(du), _p(dv))
+    return d0, du, dv
+
+
+@_keeps
+def init_ray_dir_f64(dir_, up, fov, width, height):
+    d0, du, dv = (np.zeros(3, np.float64) for _ in range(3))
+    lib().orc_init_ray_dir_f64(_p(f64(dir_)), _p(f64(up)), float(fov), width, height,
+                               _p(d0), _p(du), _p(dv))
+    return d0, du, dv
+
+
+@_keeps
+def svo_render(nodes_u32, root, attrs_u8, pos, dir_, up, fov, width, height, light,
+               ambient=0.15, diffuse=0.85, shadows=False, threads=1, rows=None):
+    """FP32 oracle render.  Returns dict of numpy arrays (rgba u32, hit u32,
+    hit_t f32, fetches u32, shadow_fetches u32, shadowed u8)."""
+    nodes_u32 = np.ascontiguousarray(nodes_u32, dtype=np.uint32)
+    attrs_u8 = np.ascontiguousarray(attrs_u8, dtype=np.uint8)
+    count = len(nodes_u32) // 10
+    nattrs = len(attrs_u8) // 8
+    d0, du, dv = init_ray_dir_f32(dir_, up, fov, width, height)
+    n = width * height
+    out = dict(rgba=np.zeros(n, np.uint32), hit=np.full(n, 0xFFFFFFFF, np.uint32),
+               hit_t=np.zeros(n, np.float32), fetches=np.zeros(n, np.uint32),
+               shadow_fetches=np.zeros(n, np.uint32), shadowed=np.zeros(n, np.uint8))
+    ps, lt = f32(pos), f32(light)
+    if threads <= 1 or rows is not None:
+        y0, y1 = (0, height) if rows is None else rows
+        st = lib().orc_svo_render_f32(_p(nodes_u32), count, root, _p(attrs_u8), nattrs,
+                                      _p(ps), _p(d0), _p(du), _p(dv), width, height, _p(lt),
+                                      ambient, diffuse, 1 if shadows else 0, y0, y1,
+                                      _p(out["rgba"]), _p(out["hit"]), _p(out["hit_t"]),
+                                      _p(out["fetches"]), _p(out["shadow_fetches"]),
+                                      _p(out["shadowed"]))
+    else:
+        st = lib().orc_svo_render_mt(threads, _p(nodes_u32), count, root, _p(attrs_u8),
+                                     nattrs, _p(ps), _p(d0), _p(du), _p(dv), width, height,
+                                     _p(lt), ambient, diffuse, 1 if shadows else 0,
+                                     _p(out["rgba"]), _p(out["hit"]), _p(out["hit_t"]),
+                                     _p(out["fetches"]), _p(out["shadow_fetches"]),
+                                     _p(out["shadowed"]))
+    if st != 0:
+        raise RuntimeError(f"oracle svo render failed: {st}")
+    return {k: v.reshape(height, width) for k, v in out.items()}
+
+
+@_keeps
+def svo_hits_f64(nodes_u32, root, pos, dir_, up, fov, width, height, rows=None):
+    nodes_u32 = np.ascontiguousarray(nodes_u32, dtype=np.uint32)
+    n = width * height
+    hit = np.full(n, 0xFFFFFFFF, np.uint32)
+    t = np.zeros(n, np.float64)
+    y0, y1 = (0, height) if rows is None else rows
+    st = lib().orc_svo_hits_f64(_p(nodes_u32), len(nodes_u32) // 10, root, _p(f64(pos)),
+                                _p(f64(dir_)), _p(f64(up)), float(fov), width, height, y0, y1,
+                                _p(hit), _p(t))
+    if st != 0:
+        raise RuntimeError(f"oracle f64 hits failed: {st}")
+    return hit.reshape(height, width), t.reshape(height, width)
+
+
+@_keeps
+def trace_ray_f32(nodes_u32, root, pos, dir_, cull_behind=False):
+    nodes_u32 = np.ascontiguousarray(nodes_u32, dtype=np.uint32)
+    hit = np.zeros(1, np.uint32)
+    t = np.zeros(1, np.float32)
+    f = np.zeros(1, np.uint32)
+    lv = np.zeros(1, np.int32)
+    ok = lib().orc_svo_trace_ray_f32(_p(nodes_u32), len(nodes_u32) // 10, root, _p(f32(pos)),
+                                     _p(f32(dir_)), 1 if cull_behind else 0, _p(hit), _p(t),
+                                     _p(f), _p(lv))
+    if ok < 0:
+        raise RuntimeError(f"oracle trace failed: {-ok}")
+    return bool(ok), int(hit[0]), float(t[0]), int(f[0]), int(lv[0])
+
+
+@_keeps
+def find_first_child(t1, t2):
+    a, b = f32(t1).copy(), f32(t2).copy()
+    ch = np.zeros(1, np.int32)
+    lib().orc_find_first_child_f32(_p(a), _p(b), _p(ch))
+    return int(ch[0]), a, b
+
+
+@_keeps
+def go_next(ch, t1, t2):
+    a, b = f32(t1).copy(), f32(t2).copy()
+    c = np.array([ch], np.int32)
+    ok = lib().orc_go_next_f32(_p(c), _p(a), _p(b))
+    return bool(ok), int(c[0]), a, b
+
+
+@_keeps
+def setup_trace(pos, dir_):
+    t1, t2 = np.zeros(3, np.float32), np.zeros(3, np.float32)
+    fl = np.zeros(1, np.uint32)
+    ok = lib().orc_setup_trace_f32(_p(f32(pos)), _p(f32(dir_)), _p(t1), _p(t2), _p(fl))
+    return bool(ok), t1, t2, int(fl[0])

@@ -1,0 +1,131 @@
+/*
+ * yv_oracle.h - CPU oracle for the SVO ray cast and the brick ray-march.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the checker the CUDA path is compared
+ * against (and the timed CPU baseline); the product library never links,
+ * loads or calls it.
+ *
+ * It restates, in plain C, the reference CPU renderer of znah/yoxel-voxel:
+ *   RendererBase::InitRayDir       cell/renderer_base.h:50-61
+ *   PPURendererBase::RenderRect    cell/ppu_renderer.cpp:43-70
+ *   PPURendererBase::RecTrace      cell/ppu_renderer.cpp:18-41
+ *   FindFirstChild / GoNext        cell/spu/trace_spu.cpp:48-93
+ *   AdjustDir / SetupTrace         cell/spu/trace_spu.c_:66-105,
+ *                                  reaction/report/voxel.tex:309-326
+ *   brick march castRay/walkBrick  reaction/trace/trace.cu:42-139
+ * The reference cannot be compiled here (its cpp/ headers, Boost and
+ * libspe2 are missing), so parity with it is pinned by this restatement and
+ * by the hand-made known-answer cases in tests/ ("parity unpinned" by the
+ * reference's own tests, which cover no tracing code).
+ */
+#ifndef YV_ORACLE_H
+#define YV_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Camera basis, RendererBase::InitRayDir (cell/renderer_base.h:50-61). */
+void orc_init_ray_dir_f32(const float dir[3], const float up[3], float fov_deg,
+                          int width, int height, float dir0[3], float du[3],
+                          float dv[3]);
+void orc_init_ray_dir_f64(const double dir[3], const double up[3],
+                          double fov_deg, int width, int height, double dir0[3],
+                          double du[3], double dv[3]);
+
+/*
+ * SVO render of rows [y0, y1) (RenderRect).  nodes = count*10 uint32 (the
+ * 40-byte VoxNode), attrs = nattrs*8 bytes.  Outputs are full-frame arrays
+ * (width*height), any may be NULL.  light = direction toward the light.
+ * Returns 0, or 3 if the pool is malformed (index out of range / too deep).
+ */
+int orc_svo_render_f32(const uint32_t* nodes, uint32_t count, uint32_t root,
+                       const uint8_t* attrs, uint32_t nattrs,
+                       const float pos[3], const float dir0[3],
+                       const float du[3], const float dv[3], int width,
+                       int height, const float light[3], float ambient,
+                       float diffuse, int shadows, int y0, int y1,
+                       uint32_t* rgba, uint32_t* hit, float* hit_t,
+                       uint32_t* fetches, uint32_t* shadow_fetches,
+                       uint8_t* shadowed);
+
+/* Same over all rows on nthreads POSIX threads in row bands
+ * (TreadedRenderer, cell/ppu_renderer.cpp:121-144). */
+int orc_svo_render_mt(int nthreads, const uint32_t* nodes, uint32_t count,
+                      uint32_t root, const uint8_t* attrs, uint32_t nattrs,
+                      const float pos[3], const float dir0[3],
+                      const float du[3], const float dv[3], int width,
+                      int height, const float light[3], float ambient,
+                      float diffuse, int shadows, uint32_t* rgba,
+                      uint32_t* hit, float* hit_t, uint32_t* fetches,
+                      uint32_t* shadow_fetches, uint8_t* shadowed);
+
+/* FP64 evaluation of the primary hits (camera basis recomputed in double);
+ * used to count rays whose hit voxel is decided by a float rounding tie. */
+int orc_svo_hits_f64(const uint32_t* nodes, uint32_t count, uint32_t root,
+                     const double pos[3], const double dir[3],
+                     const double up[3], double fov_deg, int width, int height,
+                     int y0, int y1, uint32_t* hit, double* hit_t);
+
+/* Single-ray entry points used by the known-answer tests. */
+int orc_svo_trace_ray_f32(const uint32_t* nodes, uint32_t count, uint32_t root,
+                          const float pos[3], const float dir[3],
+                          int cull_behind, uint32_t* hit, float* hit_t,
+                          uint32_t* fetches, int* level);
+void orc_find_first_child_f32(float t1[3], float t2[3], int* child);
+int orc_go_next_f32(int* child, float t1[3], float t2[3]);
+int orc_setup_trace_f32(const float pos[3], const float dir[3], float t1[3],
+                        float t2[3], uint32_t* dir_flags);
+
+/*
+ * Brick volume ray-march (ntree layout).
+ *   grids   : ngrids*64 uint32 child refs of N=4 grid nodes; ref encoding
+ *             0x80000000 = empty, 0x40000000|b = brick b, else grid index.
+ *   density : nbricks*729 values (9^3 lattice incl. the +1 apron), float
+ *             (f64 oracle reads float input, computes in double)
+ *   albedo  : nbricks*729*3 floats in [0,1]
+ *   levels  : grid levels (scene size = 4^levels * 8 lattice cells)
+ * Output rgba: 4 doubles per pixel.  samples / bricks: per-pixel counters
+ * (optional).  Rows [y0, y1).
+ */
+int orc_brick_render_f64(const uint32_t* grids, uint32_t ngrids,
+                         const float* density, const float* albedo,
+                         uint32_t nbricks, int levels, const double pos[3],
+                         const double dir0[3], const double du[3],
+                         const double dv[3], int width, int height,
+                         double alpha_scale, double step_vox, int y0, int y1,
+                         double* rgba, uint32_t* samples, uint32_t* bricks);
+int orc_brick_render_f32(const uint32_t* grids, uint32_t ngrids,
+                         const float* density, const float* albedo,
+                         uint32_t nbricks, int levels, const float pos[3],
+                         const float dir0[3], const float du[3],
+                         const float dv[3], int width, int height,
+                         float alpha_scale, float step_vox, int y0, int y1,
+                         float* rgba, uint32_t* samples, uint32_t* bricks);
+int orc_brick_render_mt_f32(int nthreads, const uint32_t* grids,
+                            uint32_t ngrids, const float* density,
+                            const float* albedo, uint32_t nbricks, int levels,
+                            const float pos[3], const float dir0[3],
+                            const float du[3], const float dv[3], int width,
+                            int height, float alpha_scale, float step_vox,
+                            float* rgba, uint32_t* samples, uint32_t* bricks);
+
+/* FP64 adjoint of the brick march for an L2-style loss: given dL/drgba per
+ * pixel (4 doubles), accumulates dL/ddensity (nbricks*729) and dL/dalbedo
+ * (nbricks*729*3) in pool layout (apron slots receive their own share). */
+int orc_brick_backward_f64(const uint32_t* grids, uint32_t ngrids,
+                           const float* density, const float* albedo,
+                           uint32_t nbricks, int levels, const double pos[3],
+                           const double dir0[3], const double du[3],
+                           const double dv[3], int width, int height,
+                           double alpha_scale, double step_vox,
+                           const double* grad_rgba, double* grad_density,
+                           double* grad_albedo);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* YV_ORACLE_H */

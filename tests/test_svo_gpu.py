@@ -1,0 +1,202 @@
+"""GPU parity of the SVO ray cast against the CPU oracle, through the C ABI.
+
+Bar: hit voxel index (node id, child) bit-exact with the FP32 restatement of
+the reference renderer; hit t, fetch counts, RGBA8 colour and shadow results
+bit-exact too (the kernel issues the same IEEE operations).  Against the FP64
+oracle, rays whose hit differs (float ties at cell boundaries) must stay
+under 1e-4 of all rays."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import LIGHT, ROOT, camera_for
+
+pytestmark = pytest.mark.gpu
+
+TIE_BUDGET = 1e-4
+
+
+def render_gpu(yoxel, scene, pos, view, w, h, fov=60.0, shadows=False, cfg=None,
+               arrays=None):
+    r = yoxel.Renderer()
+    if arrays is not None:
+        r.SetSceneArrays(*arrays)
+    else:
+        r.SetScene(scene)
+    r.SetViewPos(pos)
+    r.SetViewDir(view)
+    r.SetViewUp([0, 0, 1])
+    r.SetResolution(w, h)
+    r.SetFOV(fov)
+    r.SetLight(LIGHT, 0.15, 0.85, shadows)
+    if cfg:
+        r.SetLaunchConfig(**cfg)
+    o = r.render_outputs()
+    stats = o.pop("stats")
+    out = {k: v.cpu().numpy() for k, v in o.items()}
+    out["hit"] = out["hit"].view(np.uint32)
+    out["rgba"] = out["rgba"].view(np.uint32)
+    out["fetches"] = out["fetches"].view(np.uint32)
+    out["shadow_fetches"] = out["shadow_fetches"].view(np.uint32)
+    return out, stats
+
+
+def assert_bit_exact(g, o, shadows):
+    miss = g["hit"] != o["hit"]
+    assert miss.sum() == 0, f"{miss.sum()} hit ids differ, first at {np.argwhere(miss)[:3]}"
+    assert np.array_equal(g["hit_t"].view(np.uint32), o["hit_t"].view(np.uint32))
+    assert np.array_equal(g["fetches"], o["fetches"])
+    assert np.array_equal(g["rgba"], o["rgba"])
+    if shadows:
+        assert np.array_equal(g["shadow_fetches"], o["shadow_fetches"])
+
+
+@pytest.fixture(scope="module")
+def spheres(yoxel_mod):
+    return yoxel_mod.SVOScene.spheres(8, 200, 4.0, 24.0, 1234)
+
+
+@pytest.mark.parametrize("shadows", [False, True])
+def test_spheres_256_parity(yoxel_mod, oracle, spheres, shadows):
+    """200 spheres in 256^3 (depth 8), 512x512, FOV 60, Lambert."""
+    pos, view = camera_for()
+    g, st = render_gpu(yoxel_mod, spheres, pos, view, 512, 512, shadows=shadows)
+    o = oracle.svo_render(spheres.nodes_u32, spheres.root, spheres.attrs_u8, pos, view,
+                          [0, 0, 1], 60.0, 512, 512, LIGHT, shadows=shadows, threads=8)
+    assert_bit_exact(g, o, shadows)
+    hits = int((o["hit"] != 0xFFFFFFFF).sum())
+    assert st["hits"] == hits and st["primary_rays"] == 512 * 512
+    if shadows:
+        assert st["shadow_rays"] == hits and st["shadowed"] == int(o["shadowed"].sum())
+    h64, _ = oracle.svo_hits_f64(spheres.nodes_u32, spheres.root, pos, view, [0, 0, 1], 60.0,
+                                 512, 512)
+    ties = (h64 != g["hit"]).mean()
+    assert ties < TIE_BUDGET, f"FP64 tie rate {ties}"
+
+
+def test_terrain_parity_with_shadows(yoxel_mod, oracle):
+    s = yoxel_mod.SVOScene.terrain(9, 2500, 2, 8, 77)
+    pos, view = camera_for()
+    g, _ = render_gpu(yoxel_mod, s, pos, view, 320, 180, shadows=True)
+    o = oracle.svo_render(s.nodes_u32, s.root, s.attrs_u8, pos, view, [0, 0, 1], 60.0, 320,
+                          180, LIGHT, shadows=True, threads=8)
+    assert_bit_exact(g, o, True)
+    assert (o["hit"] != 0xFFFFFFFF).mean() > 0.3
+
+
+@pytest.mark.parametrize("name", ["svo_spheres_d5", "svo_terrain_d6"])
+def test_golden_fixtures(yoxel_mod, name):
+    gf = np.load(os.path.join(ROOT, "tests", "golden", name + ".npz"))
+    nodes = gf["nodes"].view(yoxel_mod.NODE_DTYPE)
+    attrs = gf["attrs"].view(yoxel_mod.ATTR_DTYPE)
+    g, _ = render_gpu(yoxel_mod, None, gf["pos"], gf["view"], int(gf["width"]),
+                      int(gf["height"]), float(gf["fov"]), bool(gf["shadows"]),
+                      arrays=(nodes, int(gf["root"]), attrs))
+    expect = {k: gf[k] for k in ("rgba", "hit", "hit_t", "fetches", "shadow_fetches")}
+    assert_bit_exact(g, expect, True)
+
+
+@pytest.mark.parametrize("cfg", [
+    dict(smem_nodes=0), dict(smem_nodes=9), dict(smem_nodes=4096),
+    dict(block_threads=64), dict(block_threads=128, blocks_per_sm=2),
+])
+def test_launch_configs_give_identical_results(yoxel_mod, spheres, cfg):
+    pos, view = camera_for()
+    base, _ = render_gpu(yoxel_mod, spheres, pos, view, 200, 150, shadows=True)
+    g, _ = render_gpu(yoxel_mod, spheres, pos, view, 200, 150, shadows=True, cfg=cfg)
+    for k in ("hit", "rgba", "fetches", "shadow_fetches"):
+        assert np.array_equal(base[k], g[k]), k
+
+
+@pytest.mark.parametrize("case", ["inside", "axis", "ragged", "tiny", "wide_fov"])
+def test_edge_cases(yoxel_mod, oracle, spheres, case):
+    pos, view = camera_for()
+    w, h, fov = 64, 48, 60.0
+    if case == "inside":       # camera inside the volume (reference quirk path)
+        pos = np.array([0.41, 0.47, 0.52], np.float32)
+        view = np.array([0.3, -1.0, 0.2], np.float32)
+    elif case == "axis":       # axis-aligned view: AdjustDir epsilon path
+        pos = np.array([0.5, 0.5, 2.0], np.float32)
+        view = np.array([0.0, 0.0, -1.0], np.float32)
+        w, h = 65, 65
+    elif case == "ragged":     # width/height not multiples of the 8x4 tile
+        w, h = 37, 23
+    elif case == "tiny":
+        w, h = 1, 1
+    elif case == "wide_fov":
+        fov = 150.0
+    g, _ = render_gpu(yoxel_mod, spheres, pos, view, w, h, fov=fov, shadows=True)
+    o = oracle.svo_render(spheres.nodes_u32, spheres.root, spheres.attrs_u8, pos, view,
+                          [0, 0, 1], fov, w, h, LIGHT, shadows=True)
+    assert_bit_exact(g, o, True)
+
+
+def test_empty_and_single_voxel_scenes(yoxel_mod, oracle):
+    EMPTY = 0x80000000
+    pos, view = camera_for()
+    empty = np.zeros(0, yoxel_mod.NODE_DTYPE)
+    g, st = render_gpu(yoxel_mod, None, pos, view, 32, 32,
+                       arrays=(empty, EMPTY, np.zeros(0, yoxel_mod.ATTR_DTYPE)))
+    assert (g["hit"] == 0xFFFFFFFF).all() and (g["rgba"] == 0).all() and st["hits"] == 0
+    # one leaf: root child 6 of a depth-1 tree
+    node = np.zeros(1, yoxel_mod.NODE_DTYPE)
+    node["child"][0] = [EMPTY] * 6 + [0, EMPTY]
+    node["flags"][0] = (1 << 6) | (0xBF << 8)
+    attrs = np.zeros(1, yoxel_mod.ATTR_DTYPE)
+    attrs["rgb"][0] = [200, 100, 50, 255]
+    attrs["n"][0] = [0, 0, 127, 0]
+    g, st = render_gpu(yoxel_mod, None, pos, view, 48, 48, shadows=True,
+                       arrays=(node, 0, attrs))
+    o = oracle.svo_render(node.view(np.uint32), 0, attrs.view(np.uint8), pos, view, [0, 0, 1],
+                          60.0, 48, 48, LIGHT, shadows=True)
+    assert_bit_exact(g, o, True)
+    assert st["hits"] > 0
+
+
+def test_render_frame_host_matches_device(yoxel_mod, spheres):
+    pos, view = camera_for()
+    g, _ = render_gpu(yoxel_mod, spheres, pos, view, 96, 64)
+    r = yoxel_mod.Renderer()
+    r.SetScene(spheres)
+    r.SetViewPos(pos)
+    r.SetViewDir(view)
+    r.SetResolution(96, 64)
+    r.SetFOV(60.0)
+    r.SetLight(LIGHT, 0.15, 0.85, False)
+    img = r.RenderFrame()
+    assert img.shape == (64, 96, 4)
+    assert np.array_equal(img.reshape(-1, 4).view(np.uint32).reshape(64, 96), g["rgba"])
+
+
+def test_status_codes(yoxel_mod):
+    r = yoxel_mod.Renderer()
+    assert r.RenderFrame() is None  # no scene: RenderFrame returns NULL
+    # a pool with a cycle is rejected by validation
+    node = np.zeros(1, yoxel_mod.NODE_DTYPE)
+    node["child"][0] = [0] + [0x80000000] * 7
+    with pytest.raises(yoxel_mod.YvError) as e:
+        r.SetSceneArrays(node, 0, np.zeros(0, yoxel_mod.ATTR_DTYPE))
+    assert e.value.status == 3
+
+
+def test_vox_roundtrip_renders_identically(yoxel_mod, spheres, tmp_path):
+    p = tmp_path / "scene.vox"
+    spheres.save(p)
+    s2 = yoxel_mod.SVOScene.load(p)
+    pos, view = camera_for()
+    a, _ = render_gpu(yoxel_mod, spheres, pos, view, 64, 64)
+    b, _ = render_gpu(yoxel_mod, s2, pos, view, 64, 64)
+    assert np.array_equal(a["hit"], b["hit"]) and np.array_equal(a["rgba"], b["rgba"])
+
+
+def test_cuda_renderer_driver(yoxel_mod, spheres):
+    """trace_cuda.CudaRenderer-style driver."""
+    cr = yoxel_mod.CudaRenderer((128, 96))
+    cr.updateScene(spheres)
+    cr.setLightPos((0.5, 0.5, 1.0))
+    pos, view = camera_for()
+    stat = cr.render(pos, view)
+    assert "gpu time" in stat
+    img = cr.getImage()
+    assert img.shape == (96, 128, 3) and img.max() > 0

@@ -1,0 +1,341 @@
+// api.cpp - C ABI of the SVO renderer: ISVORenderer (cell/svorenderer.h:5-31,
+// cell/renderer_base.h:7-62) and the CUDA SVORenderer host
+// (demo/SVORenderer.h:8-64, demo/SVORenderer.cpp:39-149), over the kernels of
+// svo_kernels.cu.  No CUDA error aborts: every failure is a yv_status.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "yv_internal.h"
+#include "yv_kernels.h"
+
+using namespace yv;
+
+struct yv_renderer {
+  int device = 0;
+  // camera (RendererBase defaults, cell/renderer_base.h:25; SVORenderer
+  // view dir (1,0,0), demo/SVORenderer.cpp:9)
+  float pos[3] = {0.f, 0.f, 0.f};
+  float dir[3] = {1.f, 0.f, 0.f};
+  float up[3] = {0.f, 0.f, 1.f};
+  float fov = 70.f;
+  int width = 640, height = 480;
+  yv_light light;
+  LaunchCfg cfg;
+  // device scene
+  uint32_t* d_words = nullptr;
+  uint32_t* d_orig = nullptr;
+  yv_leaf_attr* d_attrs = nullptr;
+  SvoDeviceScene scene;
+  bool has_scene = false;
+  uint64_t scene_bytes = 0;
+  // renderer-owned frame buffer (RendererBase::m_colorBuf) and scratch
+  uint32_t* d_rgba = nullptr;
+  size_t rgba_cap = 0;
+  uint32_t* d_counters = nullptr;
+  cudaStream_t last_stream = nullptr;
+  uint64_t last_pixels = 0;
+  int last_shadows = 0;
+  uint32_t last_launches = 0;
+  bool frame_pending = false;
+};
+
+static yv_status cuda_fail(cudaError_t e, const char* what) {
+  set_last_error(std::string(what) + ": " + cudaGetErrorString(e));
+  cudaGetLastError();  // clear the non-sticky error
+  return e == cudaErrorMemoryAllocation ? YV_ERR_OUT_OF_MEMORY : YV_ERR_CUDA;
+}
+
+#define YV_CUDA(call, what)                          \
+  do {                                               \
+    cudaError_t e_ = (call);                         \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+static void free_scene(yv_renderer* r) {
+  cudaFree(r->d_words);
+  cudaFree(r->d_orig);
+  cudaFree(r->d_attrs);
+  r->d_words = nullptr;
+  r->d_orig = nullptr;
+  r->d_attrs = nullptr;
+  r->has_scene = false;
+  r->scene = SvoDeviceScene();
+  r->scene_bytes = 0;
+}
+
+extern "C" {
+
+const char* yv_status_string(yv_status s) {
+  switch (s) {
+    case YV_OK: return "ok";
+    case YV_ERR_INVALID_ARG: return "invalid argument";
+    case YV_ERR_NO_SCENE: return "no scene set";
+    case YV_ERR_BAD_POOL: return "malformed node or brick pool";
+    case YV_ERR_ITERATION_CAP: return "ray iteration cap reached";
+    case YV_ERR_TIMEOUT: return "bounded device wait timed out";
+    case YV_ERR_CUDA: return "CUDA runtime error";
+    case YV_ERR_OUT_OF_MEMORY: return "out of memory";
+    case YV_ERR_IO: return "file I/O error";
+    case YV_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+  }
+}
+
+yv_status yv_renderer_create(yv_renderer** out) {
+  if (!out) return YV_ERR_INVALID_ARG;
+  *out = nullptr;
+  yv_renderer* r = new (std::nothrow) yv_renderer();
+  if (!r) return YV_ERR_OUT_OF_MEMORY;
+  cudaError_t e = cudaGetDevice(&r->device);
+  if (e != cudaSuccess) {
+    delete r;
+    return cuda_fail(e, "cudaGetDevice");
+  }
+  e = cudaMalloc(&r->d_counters, kSvoCounterWords * sizeof(uint32_t));
+  if (e != cudaSuccess) {
+    delete r;
+    return cuda_fail(e, "cudaMalloc(counters)");
+  }
+  cudaMemset(r->d_counters, 0, kSvoCounterWords * sizeof(uint32_t));
+  // default light: the configs' directional light normalize(0.3, 0.5, 0.8)
+  float l[3] = {0.3f, 0.5f, 0.8f};
+  float n = std::sqrt((l[0] * l[0] + l[1] * l[1]) + l[2] * l[2]);
+  for (int i = 0; i < 3; ++i) r->light.dir[i] = l[i] / n;
+  r->light.ambient = 0.15f;
+  r->light.diffuse = 0.85f;
+  r->light.shadows = 0;
+  *out = r;
+  return YV_OK;
+}
+
+void yv_renderer_destroy(yv_renderer* r) {
+  if (!r) return;
+  cudaSetDevice(r->device);
+  if (r->frame_pending) cudaStreamSynchronize(r->last_stream);
+  free_scene(r);
+  cudaFree(r->d_rgba);
+  cudaFree(r->d_counters);
+  delete r;
+}
+
+yv_status yv_set_scene_svo(yv_renderer* r, const yv_vox_node* nodes,
+                           uint32_t count, uint32_t root,
+                           const yv_leaf_attr* attrs, uint32_t nattrs) {
+  if (!r || (count && !nodes) || (nattrs && !attrs)) return YV_ERR_INVALID_ARG;
+  DeviceLayout dl;
+  std::string why;
+  yv_status st = build_device_layout(nodes, count, root, nattrs, &dl, &why);
+  if (st != YV_OK) {
+    set_last_error(why);
+    return st;
+  }
+  YV_CUDA(cudaSetDevice(r->device), "cudaSetDevice");
+  if (r->frame_pending) cudaStreamSynchronize(r->last_stream);
+  free_scene(r);
+  const size_t nn = dl.orig_id.size();
+  if (nn) {
+    YV_CUDA(cudaMalloc(&r->d_words, nn * 32u), "cudaMalloc(nodes)");
+    YV_CUDA(cudaMalloc(&r->d_orig, nn * 4u), "cudaMalloc(orig)");
+    YV_CUDA(cudaMemcpy(r->d_words, dl.words.data(), nn * 32u, cudaMemcpyHostToDevice),
+            "upload nodes");
+    YV_CUDA(cudaMemcpy(r->d_orig, dl.orig_id.data(), nn * 4u, cudaMemcpyHostToDevice),
+            "upload ids");
+  }
+  if (nattrs) {
+    YV_CUDA(cudaMalloc(&r->d_attrs, (size_t)nattrs * 8u), "cudaMalloc(attrs)");
+    YV_CUDA(cudaMemcpy(r->d_attrs, attrs, (size_t)nattrs * 8u, cudaMemcpyHostToDevice),
+            "upload attrs");
+  }
+  r->scene.nodes = reinterpret_cast<const uint4*>(r->d_words);
+  r->scene.orig_id = r->d_orig;
+  r->scene.attrs = reinterpret_cast<const uint2*>(r->d_attrs);
+  r->scene.n_nodes = (uint32_t)nn;
+  r->scene.n_attrs = nattrs;
+  r->scene.root_word = dl.root_word;
+  r->scene_bytes = (uint64_t)nn * 36u + (uint64_t)nattrs * 8u;
+  r->has_scene = true;
+  return YV_OK;
+}
+
+yv_status yv_set_scene_host(yv_renderer* r, const yv_svo_host* svo) {
+  if (!r || !svo) return YV_ERR_INVALID_ARG;
+  return yv_set_scene_svo(r, yv_svo_nodes(svo), yv_svo_node_count(svo), yv_svo_root(svo),
+                          yv_svo_attrs(svo), yv_svo_attr_count(svo));
+}
+
+yv_status yv_load_scene_vox(yv_renderer* r, const char* path) {
+  if (!r || !path) return YV_ERR_INVALID_ARG;
+  yv_svo_host* h = nullptr;
+  yv_status st = yv_svo_load_vox(&h, path);
+  if (st != YV_OK) return st;
+  st = yv_set_scene_host(r, h);
+  yv_svo_free(h);
+  return st;
+}
+
+static bool finite3(const float* v) {
+  return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]);
+}
+
+yv_status yv_set_view_pos(yv_renderer* r, const float pos[3]) {
+  if (!r || !pos || !finite3(pos)) return YV_ERR_INVALID_ARG;
+  std::memcpy(r->pos, pos, sizeof(r->pos));
+  return YV_OK;
+}
+yv_status yv_set_view_dir(yv_renderer* r, const float dir[3]) {
+  if (!r || !dir || !finite3(dir) || (dir[0] == 0 && dir[1] == 0 && dir[2] == 0))
+    return YV_ERR_INVALID_ARG;
+  std::memcpy(r->dir, dir, sizeof(r->dir));
+  return YV_OK;
+}
+yv_status yv_set_view_up(yv_renderer* r, const float up[3]) {
+  if (!r || !up || !finite3(up)) return YV_ERR_INVALID_ARG;
+  std::memcpy(r->up, up, sizeof(r->up));
+  return YV_OK;
+}
+yv_status yv_set_resolution(yv_renderer* r, int width, int height) {
+  if (!r || width <= 0 || height <= 0 || (long long)width * height > (1ll << 31))
+    return YV_ERR_INVALID_ARG;
+  r->width = width;
+  r->height = height;
+  return YV_OK;
+}
+yv_status yv_get_resolution(const yv_renderer* r, int* width, int* height) {
+  if (!r || !width || !height) return YV_ERR_INVALID_ARG;
+  *width = r->width;
+  *height = r->height;
+  return YV_OK;
+}
+yv_status yv_set_fov(yv_renderer* r, float fov_deg) {
+  if (!r || !(fov_deg > 0.f && fov_deg < 180.f)) return YV_ERR_INVALID_ARG;
+  r->fov = fov_deg;
+  return YV_OK;
+}
+yv_status yv_set_light(yv_renderer* r, const yv_light* light) {
+  if (!r || !light || !finite3(light->dir)) return YV_ERR_INVALID_ARG;
+  r->light = *light;
+  return YV_OK;
+}
+yv_status yv_set_launch_config(yv_renderer* r, const yv_launch_config* c) {
+  if (!r || !c) return YV_ERR_INVALID_ARG;
+  LaunchCfg d;
+  r->cfg.block_threads = c->block_threads > 0 ? c->block_threads : d.block_threads;
+  r->cfg.blocks_per_sm = c->blocks_per_sm > 0 ? c->blocks_per_sm : 0;
+  r->cfg.smem_nodes = c->smem_nodes >= 0 ? c->smem_nodes : d.smem_nodes;
+  r->cfg.tile_rays = c->tile_rays > 0 ? c->tile_rays : d.tile_rays;
+  if (r->cfg.block_threads > 256 || (r->cfg.block_threads & 31)) return YV_ERR_INVALID_ARG;
+  return YV_OK;
+}
+yv_status yv_get_launch_config(const yv_renderer* r, yv_launch_config* c) {
+  if (!r || !c) return YV_ERR_INVALID_ARG;
+  c->block_threads = r->cfg.block_threads;
+  c->blocks_per_sm = r->cfg.blocks_per_sm;
+  c->smem_nodes = r->cfg.smem_nodes;
+  c->tile_rays = r->cfg.tile_rays;
+  return YV_OK;
+}
+
+yv_status yv_get_ray_basis(const yv_renderer* r, float dir0[3], float du[3], float dv[3]) {
+  if (!r || !dir0 || !du || !dv) return YV_ERR_INVALID_ARG;
+  init_ray_dir(r->dir, r->up, r->fov, r->width, r->height, dir0, du, dv);
+  return YV_OK;
+}
+
+yv_status yv_get_device_scene_info(const yv_renderer* r, uint64_t* nodes, uint64_t* bytes) {
+  if (!r || !nodes || !bytes) return YV_ERR_INVALID_ARG;
+  *nodes = r->scene.n_nodes;
+  *bytes = r->scene_bytes;
+  return YV_OK;
+}
+
+static yv_status enqueue_frame(yv_renderer* r, const yv_frame_outputs* out, cudaStream_t s) {
+  if (!r->has_scene) return YV_ERR_NO_SCENE;
+  SvoFrameArgs a;
+  std::memset(&a, 0, sizeof(a));
+  std::memcpy(a.pos, r->pos, sizeof(a.pos));
+  init_ray_dir(r->dir, r->up, r->fov, r->width, r->height, a.dir0, a.du, a.dv);
+  std::memcpy(a.light, r->light.dir, sizeof(a.light));
+  std::memcpy(a.light_ray, r->light.dir, sizeof(a.light_ray));
+  adjust_dir(a.light_ray);
+  a.ambient = r->light.ambient;
+  a.diffuse = r->light.diffuse;
+  a.shadows = r->light.shadows ? 1 : 0;
+  a.width = r->width;
+  a.height = r->height;
+  a.rgba = static_cast<uint32_t*>(out->rgba);
+  a.hit = static_cast<uint32_t*>(out->hit);
+  a.hit_t = static_cast<float*>(out->hit_t);
+  a.fetches = static_cast<uint32_t*>(out->fetches);
+  a.shadow_fetches = static_cast<uint32_t*>(out->shadow_fetches);
+  a.counters = r->d_counters;
+  int launches = 0;
+  YV_CUDA(launch_svo_frame(r->scene, a, r->cfg, s, &launches), "svo frame launch");
+  r->last_stream = s;
+  r->last_pixels = (uint64_t)r->width * (uint64_t)r->height;
+  r->last_shadows = a.shadows;
+  r->last_launches = (uint32_t)launches;
+  r->frame_pending = true;
+  return YV_OK;
+}
+
+yv_status yv_render_frame_async(yv_renderer* r, const yv_frame_outputs* out, void* stream) {
+  if (!r || !out) return YV_ERR_INVALID_ARG;
+  YV_CUDA(cudaSetDevice(r->device), "cudaSetDevice");
+  return enqueue_frame(r, out, static_cast<cudaStream_t>(stream));
+}
+
+yv_status yv_renderer_frame_stats(yv_renderer* r, yv_frame_stats* stats) {
+  if (!r || !stats) return YV_ERR_INVALID_ARG;
+  std::memset(stats, 0, sizeof(*stats));
+  YV_CUDA(cudaSetDevice(r->device), "cudaSetDevice");
+  uint32_t c[kSvoCounterWords];
+  YV_CUDA(cudaStreamSynchronize(r->last_stream), "frame sync");
+  YV_CUDA(cudaMemcpy(c, r->d_counters, sizeof(c), cudaMemcpyDeviceToHost), "read counters");
+  r->frame_pending = false;
+  stats->primary_rays = r->last_pixels;
+  stats->hits = c[2];
+  stats->shadow_rays = r->last_shadows ? c[2] : 0;
+  stats->shadowed = c[3];
+  stats->launches = r->last_launches;
+  yv_status st = YV_OK;
+  if (c[1] & YV_DEV_ERR_POOL) st = YV_ERR_BAD_POOL;
+  else if (c[1] & (YV_DEV_ERR_ITER | YV_DEV_ERR_DEPTH)) st = YV_ERR_ITERATION_CAP;
+  else if (c[1] & YV_DEV_ERR_TIMEOUT) st = YV_ERR_TIMEOUT;
+  stats->status = (uint32_t)st;
+  return st;
+}
+
+yv_status yv_render_frame(yv_renderer* r, uint32_t* host_rgba, void* device_rgba, void* stream) {
+  if (!r) return YV_ERR_INVALID_ARG;
+  if (!r->has_scene) return YV_ERR_NO_SCENE;
+  YV_CUDA(cudaSetDevice(r->device), "cudaSetDevice");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  void* dst = device_rgba;
+  const size_t px = (size_t)r->width * (size_t)r->height;
+  if (!dst) {
+    if (r->rgba_cap < px) {
+      if (r->frame_pending) cudaStreamSynchronize(r->last_stream);
+      cudaFree(r->d_rgba);
+      r->d_rgba = nullptr;
+      r->rgba_cap = 0;
+      YV_CUDA(cudaMalloc(&r->d_rgba, px * 4u), "cudaMalloc(frame)");
+      r->rgba_cap = px;
+    }
+    dst = r->d_rgba;
+  }
+  yv_frame_outputs o;
+  std::memset(&o, 0, sizeof(o));
+  o.rgba = dst;
+  yv_status st = enqueue_frame(r, &o, s);
+  if (st != YV_OK) return st;
+  if (host_rgba)
+    YV_CUDA(cudaMemcpyAsync(host_rgba, dst, px * 4u, cudaMemcpyDeviceToHost, s), "read frame");
+  yv_frame_stats stats;
+  return yv_renderer_frame_stats(r, &stats);
+}
+
+}  // extern "C"

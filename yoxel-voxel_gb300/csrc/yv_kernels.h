@@ -1,0 +1,57 @@
+// yv_kernels.h - launch interface between the host C ABI and the CUDA
+// kernels.  Host-callable functions only; no device code here.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace yv {
+
+// Device copy of an SVO scene (layout described in yv_internal.h).
+struct SvoDeviceScene {
+  const uint4* nodes = nullptr;       // 2 x uint4 (8 child words) per node
+  const uint32_t* orig_id = nullptr;  // device index -> caller node id
+  const uint2* attrs = nullptr;       // yv_leaf_attr, 8 bytes each
+  uint32_t n_nodes = 0;
+  uint32_t n_attrs = 0;
+  uint32_t root_word = 0x40000000u;
+};
+
+// One frame of the SVO renderer.
+struct SvoFrameArgs {
+  float pos[3];
+  float dir0[3], du[3], dv[3];   // RendererBase::InitRayDir basis
+  float light[3];                // shading direction (toward the light)
+  float light_ray[3];            // light direction after AdjustDir
+  float ambient, diffuse;
+  int shadows;
+  int width, height;
+  uint32_t* rgba;                // optional outputs (device)
+  uint32_t* hit;
+  float* hit_t;
+  uint32_t* fetches;
+  uint32_t* shadow_fetches;
+  uint32_t* counters;            // device scratch, kSvoCounterWords words
+};
+
+// Scratch words a frame uses: [0] tile queue, [1] status bits, [2] hits,
+// [3] shadowed hits.
+constexpr int kSvoCounterWords = 8;
+
+struct LaunchCfg {
+  int block_threads = 256;
+  int blocks_per_sm = 0;   // 0: occupancy-derived
+  int smem_nodes = 585;    // 1 + 8 + 64 + 512: four full top levels
+  int tile_rays = 32;
+};
+
+// Enqueues one frame (counter reset + persistent kernel) on `stream`.
+cudaError_t launch_svo_frame(const SvoDeviceScene& sc, const SvoFrameArgs& a,
+                             const LaunchCfg& cfg, cudaStream_t stream,
+                             int* launches);
+
+// Number of SMs of the current device (cached per device).
+int device_sm_count();
+
+}  // namespace yv

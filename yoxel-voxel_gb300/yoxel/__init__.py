@@ -1,0 +1,13 @@
+"""yoxel - GB300-native sparse-voxel-octree and brick-volume ray caster.
+
+Python side of the C ABI in include/yv_c_api.h (libyoxel.so, built in-tree by
+yoxel-voxel_gb300/build.py).  Mirrors the reference's Python driver
+trace_cuda.CudaRenderer and its ISVORenderer interface.
+"""
+from . import _lib
+from ._lib import YvError, LIB_PATH
+from .svo import SVOScene, NODE_DTYPE, ATTR_DTYPE
+from .renderer import Renderer, CudaRenderer
+
+__all__ = ["SVOScene", "Renderer", "CudaRenderer", "YvError", "LIB_PATH",
+           "NODE_DTYPE", "ATTR_DTYPE"]

@@ -1,0 +1,207 @@
+"""SVO renderers over the C ABI.
+
+`Renderer` mirrors ISVORenderer (cell/svorenderer.h:5-24): SetScene,
+SetViewPos/Dir/Up, SetResolution/GetResolution, SetFOV, RenderFrame (None
+without a scene, as RenderFrame returns NULL, cell/ppu_renderer.cpp:78-79).
+
+`CudaRenderer` mirrors the Python driver trace_cuda.CudaRenderer
+(trace_cuda.py:17-120): updateScene, setLightPos, getViewSize, render,
+getImage.  Frames live in CUDA memory as torch tensors; torch provides the
+device buffers and streams only, all computation is in libyoxel.so.
+"""
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import _lib as L
+from .svo import SVOScene
+
+
+def _f3(v):
+    v = [float(x) for x in v]
+    if len(v) != 3:
+        raise ValueError("expected 3 components")
+    return L.F3(*v)
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream_ptr(stream):
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+class Renderer:
+    """ISVORenderer on the GPU."""
+
+    def __init__(self):
+        h = C.c_void_p()
+        L.check(L.lib.yv_renderer_create(C.byref(h)), "yv_renderer_create")
+        self._h = h
+        self._scene = None
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            L.lib.yv_renderer_destroy(h)
+            self._h = C.c_void_p(None)
+
+    @property
+    def handle(self):
+        return self._h
+
+    # ---- ISVORenderer ---------------------------------------------------
+    def SetScene(self, scene: SVOScene):
+        L.check(L.lib.yv_set_scene_host(self._h, scene.handle), "SetScene")
+        self._scene = scene
+
+    def SetSceneArrays(self, nodes, root, attrs):
+        from .svo import ATTR_DTYPE, NODE_DTYPE
+        nodes = np.ascontiguousarray(nodes, dtype=NODE_DTYPE)
+        attrs = np.ascontiguousarray(attrs, dtype=ATTR_DTYPE)
+        L.check(L.lib.yv_set_scene_svo(self._h, nodes.ctypes.data, len(nodes), root,
+                                       attrs.ctypes.data, len(attrs)), "SetSceneArrays")
+        self._scene = (nodes, attrs)
+
+    def SetViewPos(self, pos):
+        L.check(L.lib.yv_set_view_pos(self._h, _f3(pos)), "SetViewPos")
+
+    def SetViewDir(self, d):
+        L.check(L.lib.yv_set_view_dir(self._h, _f3(d)), "SetViewDir")
+
+    def SetViewUp(self, up):
+        L.check(L.lib.yv_set_view_up(self._h, _f3(up)), "SetViewUp")
+
+    def SetResolution(self, width, height):
+        L.check(L.lib.yv_set_resolution(self._h, int(width), int(height)), "SetResolution")
+
+    def GetResolution(self):
+        w, h = C.c_int(), C.c_int()
+        L.check(L.lib.yv_get_resolution(self._h, C.byref(w), C.byref(h)), "GetResolution")
+        return (w.value, h.value)
+
+    def SetFOV(self, fov):
+        L.check(L.lib.yv_set_fov(self._h, float(fov)), "SetFOV")
+
+    def SetLight(self, direction, ambient=0.15, diffuse=0.85, shadows=False):
+        lt = L.Light(_f3(direction), float(ambient), float(diffuse), 1 if shadows else 0)
+        L.check(L.lib.yv_set_light(self._h, C.byref(lt)), "SetLight")
+
+    def SetLaunchConfig(self, block_threads=0, blocks_per_sm=0, smem_nodes=-1, tile_rays=0):
+        cfg = L.LaunchConfig(block_threads, blocks_per_sm, smem_nodes, tile_rays)
+        L.check(L.lib.yv_set_launch_config(self._h, C.byref(cfg)), "SetLaunchConfig")
+
+    def GetLaunchConfig(self):
+        cfg = L.LaunchConfig()
+        L.check(L.lib.yv_get_launch_config(self._h, C.byref(cfg)), "GetLaunchConfig")
+        return dict(block_threads=cfg.block_threads, blocks_per_sm=cfg.blocks_per_sm,
+                    smem_nodes=cfg.smem_nodes, tile_rays=cfg.tile_rays)
+
+    def RenderFrame(self):
+        """Synchronous frame into host memory: (h, w, 4) uint8 RGBA, or None
+        when no scene is set."""
+        w, h = self.GetResolution()
+        out = np.empty((h, w), np.uint32)
+        st = L.lib.yv_render_frame(self._h, out.ctypes.data, None, None)
+        if st == L.YV_ERR_NO_SCENE:
+            return None
+        L.check(st, "RenderFrame")
+        return out.view(np.uint8).reshape(h, w, 4)
+
+    # ---- device-side API ----------------------------------------------------
+    def ray_basis(self):
+        d0, du, dv = L.F3(), L.F3(), L.F3()
+        L.check(L.lib.yv_get_ray_basis(self._h, d0, du, dv), "yv_get_ray_basis")
+        return np.array(d0, np.float32), np.array(du, np.float32), np.array(dv, np.float32)
+
+    def render_async(self, rgba=None, hit=None, hit_t=None, fetches=None,
+                     shadow_fetches=None, stream=None):
+        """Enqueues a frame into caller-owned CUDA tensors (each optional)."""
+        def ptr(t):
+            return None if t is None else C.c_void_p(t.data_ptr())
+        o = L.FrameOutputs(ptr(rgba), ptr(hit), ptr(hit_t), ptr(fetches), ptr(shadow_fetches))
+        L.check(L.lib.yv_render_frame_async(self._h, C.byref(o), _stream_ptr(stream)),
+                "yv_render_frame_async")
+
+    def frame_stats(self, check=True):
+        s = L.FrameStats()
+        st = L.lib.yv_renderer_frame_stats(self._h, C.byref(s))
+        if check:
+            L.check(st, "frame")
+        return dict(primary_rays=s.primary_rays, hits=s.hits, shadow_rays=s.shadow_rays,
+                    shadowed=s.shadowed, status=s.status, launches=s.launches)
+
+    def render_outputs(self, stream=None, stats=True):
+        """Renders into fresh CUDA tensors and returns them with the counters:
+        rgba (h,w) int32, hit (h,w) int32, hit_t (h,w) float32, fetches and
+        shadow_fetches (h,w) int32."""
+        torch = _torch()
+        w, h = self.GetResolution()
+        dev = torch.device("cuda", torch.cuda.current_device())
+        out = dict(
+            rgba=torch.empty((h, w), dtype=torch.int32, device=dev),
+            hit=torch.empty((h, w), dtype=torch.int32, device=dev),
+            hit_t=torch.empty((h, w), dtype=torch.float32, device=dev),
+            fetches=torch.empty((h, w), dtype=torch.int32, device=dev),
+            shadow_fetches=torch.empty((h, w), dtype=torch.int32, device=dev),
+        )
+        self.render_async(stream=stream, **out)
+        if stats:
+            out["stats"] = self.frame_stats()
+        return out
+
+    def device_scene_info(self):
+        n, b = C.c_uint64(), C.c_uint64()
+        L.check(L.lib.yv_get_device_scene_info(self._h, C.byref(n), C.byref(b)),
+                "yv_get_device_scene_info")
+        return n.value, b.value
+
+
+class CudaRenderer:
+    """trace_cuda.CudaRenderer (trace_cuda.py:17-120) on libyoxel."""
+
+    def __init__(self, res=(640, 480)):
+        self.resx, self.resy = int(res[0]), int(res[1])
+        self._r = Renderer()
+        self._r.SetResolution(self.resx, self.resy)
+        self._r.SetFOV(70.0)
+        self.detailCoef = 10.0
+        self._img = None
+        self.setLightPos((0.5, 0.5, 1))
+
+    def updateScene(self, scene):
+        self._r.SetScene(scene)
+
+    def setLightPos(self, pos):
+        """Directional light toward `pos` seen from the scene centre."""
+        self.lightPos = tuple(float(v) for v in pos)
+        d = np.array(self.lightPos, np.float64) - 0.5
+        n = np.linalg.norm(d)
+        d = d / n if n > 0 else np.array([0.0, 0.0, 1.0])
+        self._r.SetLight(d)
+
+    def getViewSize(self):
+        return (self.resx, self.resy)
+
+    def render(self, eyePos, viewDir, first=False):
+        torch = _torch()
+        self._r.SetViewPos(eyePos)
+        self._r.SetViewDir(viewDir)
+        if self._img is None:
+            self._img = torch.empty((self.resy, self.resx), dtype=torch.int32, device="cuda")
+        t0 = time.perf_counter()
+        self._r.render_async(rgba=self._img)
+        st = self._r.frame_stats()
+        dt = time.perf_counter() - t0
+        return ("gpu time: %.2f ms\n" % (dt * 1000) +
+                "hits: %d of %d\n" % (st["hits"], st["primary_rays"]) +
+                "detailCoef: %f\n" % self.detailCoef)
+
+    def getImage(self):
+        a = self._img.cpu().numpy().view(np.uint8).reshape(self.resy, self.resx, 4)
+        return a[..., :3]

@@ -1,0 +1,122 @@
+"""Host-side SVO scenes (SVOData, cell/svodata.h:22-55).
+
+An `SVOScene` owns a yv_svo_host container of the C library and exposes its
+40-byte VoxNode records and 8-byte leaf attributes as numpy views.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+NODE_DTYPE = np.dtype([("flags", "<u4"), ("data", "<u4"), ("child", "<u4", (8,))])
+ATTR_DTYPE = np.dtype([("rgb", "u1", (4,)), ("n", "i1", (4,))])
+
+
+class SVOScene:
+    """A sparse voxel octree: `nodes` (VoxNode records), `attrs` (leaf colour +
+    quantised normal), `root` and `depth`."""
+
+    def __init__(self, handle):
+        self._h = C.c_void_p(handle)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            L.lib.yv_svo_free(h)
+            self._h = C.c_void_p(None)
+
+    # ---- constructors -------------------------------------------------
+    @classmethod
+    def spheres(cls, depth=8, n_spheres=200, rmin=4.0, rmax=24.0, seed=1234):
+        """Seeded sphere-union scene (the 200-spheres-in-256^3 workload)."""
+        h = C.c_void_p()
+        L.check(L.lib.yv_svo_gen_spheres(C.byref(h), depth, n_spheres, rmin, rmax, seed),
+                "yv_svo_gen_spheres")
+        return cls(h.value)
+
+    @classmethod
+    def terrain(cls, depth=11, n_cubes=10000, cube_min=2, cube_max=16, seed=1234):
+        """Seeded value-noise terrain + floating cubes (the 2048^3 workload)."""
+        h = C.c_void_p()
+        L.check(L.lib.yv_svo_gen_terrain(C.byref(h), depth, n_cubes, cube_min, cube_max,
+                                         seed), "yv_svo_gen_terrain")
+        return cls(h.value)
+
+    @classmethod
+    def from_arrays(cls, nodes, root, attrs):
+        nodes = np.ascontiguousarray(nodes, dtype=NODE_DTYPE)
+        attrs = np.ascontiguousarray(attrs, dtype=ATTR_DTYPE)
+        h = C.c_void_p()
+        L.check(L.lib.yv_svo_from_arrays(C.byref(h), nodes.ctypes.data, len(nodes), root,
+                                         attrs.ctypes.data, len(attrs)),
+                "yv_svo_from_arrays")
+        return cls(h.value)
+
+    @classmethod
+    def load(cls, path):
+        """SVOData::Load of a .vox file."""
+        h = C.c_void_p()
+        L.check(L.lib.yv_svo_load_vox(C.byref(h), str(path).encode()), "yv_svo_load_vox")
+        return cls(h.value)
+
+    def save(self, path):
+        L.check(L.lib.yv_svo_save_vox(self._h, str(path).encode()), "yv_svo_save_vox")
+
+    # ---- views --------------------------------------------------------
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def root(self):
+        return int(L.lib.yv_svo_root(self._h))
+
+    @property
+    def depth(self):
+        return int(L.lib.yv_svo_depth(self._h))
+
+    @property
+    def node_count(self):
+        return int(L.lib.yv_svo_node_count(self._h))
+
+    @property
+    def attr_count(self):
+        return int(L.lib.yv_svo_attr_count(self._h))
+
+    @property
+    def nodes(self):
+        """(count,) structured view of the VoxNode records (no copy)."""
+        n = self.node_count
+        if n == 0:
+            return np.zeros(0, NODE_DTYPE)
+        buf = (C.c_uint8 * (n * 40)).from_address(L.lib.yv_svo_nodes(self._h))
+        a = np.frombuffer(buf, dtype=NODE_DTYPE)
+        a.flags.writeable = False
+        return a
+
+    @property
+    def nodes_u32(self):
+        """(count*10,) uint32 view of the node pool."""
+        return self.nodes.view(np.uint32).reshape(-1)
+
+    @property
+    def attrs(self):
+        n = self.attr_count
+        if n == 0:
+            return np.zeros(0, ATTR_DTYPE)
+        buf = (C.c_uint8 * (n * 8)).from_address(L.lib.yv_svo_attrs(self._h))
+        a = np.frombuffer(buf, dtype=ATTR_DTYPE)
+        a.flags.writeable = False
+        return a
+
+    @property
+    def attrs_u8(self):
+        return self.attrs.view(np.uint8).reshape(-1)
+
+    def validate(self):
+        return L.lib.yv_svo_validate(L.lib.yv_svo_nodes(self._h), self.node_count, self.root,
+                                     self.attr_count)
+
+    def nbytes(self):
+        return self.node_count * 40 + self.attr_count * 8
