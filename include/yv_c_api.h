@@ -219,6 +219,108 @@ yv_status yv_get_ray_basis(const yv_renderer* r, float dir0[3], float du[3],
 yv_status yv_get_device_scene_info(const yv_renderer* r, uint64_t* nodes,
                                    uint64_t* device_bytes);
 
+/* ------------------------------------------------------------------------ */
+/* Brick volumes: the ntree layout (ntree/ntree/gpu_nodes.h:6-21,            */
+/* ntree/ntree/nodes.h:13-100, ntree/BrickManager.h:5-80)                   */
+/* ------------------------------------------------------------------------ */
+/* Tree of N^3 grid nodes, N = 4; child c = (z*4 + y)*4 + x
+ * (ntree/ntree/nodes.h:99).  A child ref is 0x80000000 (empty Const node),
+ * 0x40000000 | b (brick b, last grid level only) or a grid node index.
+ * Scene size = 8 * 4^levels lattice cells (CalcSceneSize with B = 8).
+ * A brick is a 9^3 lattice (8^3 cells + the far-side apron repeating the
+ * first layer of its +x/+y/+z neighbours), index (z*9 + y)*9 + x. */
+typedef struct yv_volume_host yv_volume_host;
+
+/* Seeded noise volume: density = clamp(amplitude*n(p) - offset, 0, 1) with
+ * n a normalised 4-octave 3D value noise, albedo = per-lattice-point uint8
+ * RGB from three further noise fields; bricks whose 9^3 lattice is all zero
+ * are culled (empty refs). */
+yv_status yv_volume_gen_noise(yv_volume_host** out, int levels, float offset,
+                              float amplitude, uint64_t seed);
+/* RangeBuilder (ntree/ntree/ntree.h:11-63) from a dense (S+1)^3 lattice,
+ * x fastest; albedo_rgb may be NULL (white). */
+yv_status yv_volume_from_dense(yv_volume_host** out, int levels,
+                               const float* density, const uint8_t* albedo_rgb);
+void            yv_volume_free(yv_volume_host* v);
+int             yv_volume_levels(const yv_volume_host* v);
+uint32_t        yv_volume_grid_count(const yv_volume_host* v);
+const uint32_t* yv_volume_grids(const yv_volume_host* v);
+uint32_t        yv_volume_brick_count(const yv_volume_host* v);
+const float*    yv_volume_density(const yv_volume_host* v);   /* nbricks*729 */
+const uint8_t*  yv_volume_albedo(const yv_volume_host* v);    /* nbricks*729*3 */
+const int32_t*  yv_volume_brick_cells(const yv_volume_host* v); /* nbricks*3 */
+/* Apron neighbour table, nbricks*7 (-1 = absent), index m-1 for the offset
+ * m = dx | dy<<1 | dz<<2: upper != 0 -> brick at +offset (owner of my
+ * apron slots), upper == 0 -> brick at -offset. */
+const int32_t*  yv_volume_neighbors(const yv_volume_host* v, int upper);
+
+#define YV_PRECISION_F16 0  /* fp16 density, uchar4 albedo (render only) */
+#define YV_PRECISION_F32 1  /* fp32 density, fp32 RGB albedo (learnable)  */
+
+/* Device view of a volume: all pointers are device pointers. */
+typedef struct yv_volume_device {
+  const uint32_t* grids;
+  uint32_t ngrids;
+  int32_t levels;
+  const void* density;
+  const void* albedo;
+  uint32_t nbricks;
+  int32_t precision;
+  const int32_t* nbr_up;
+  const int32_t* nbr_dn;
+} yv_volume_device;
+
+/* Device copy owned by the library (BrickPool<T>, ntree/BrickManager.h). */
+typedef struct yv_volume_gpu yv_volume_gpu;
+yv_status yv_volume_upload(const yv_volume_host* v, int32_t precision,
+                           yv_volume_gpu** out);
+void      yv_volume_gpu_free(yv_volume_gpu* g);
+yv_status yv_volume_gpu_desc(const yv_volume_gpu* g, yv_volume_device* out);
+
+/* Pinhole camera (RendererBase fields, cell/renderer_base.h:13-21). */
+typedef struct yv_camera {
+  float pos[3];
+  float dir[3];
+  float up[3];
+  float fov_deg;
+} yv_camera;
+
+/* March parameters: alpha = saturate(alpha_scale * density) per sample,
+ * samples every step_vox lattice cells (reaction/trace/trace.cu:44). */
+typedef struct yv_march_params {
+  float alpha_scale;
+  float step_vox;
+} yv_march_params;
+
+/* Front-to-back composited RGBA (4 floats per pixel, camera-major) of
+ * ncams cameras; the volume counterpart of RunTrace
+ * (ntree/ntree_trace.cuh:27).  samples / bricks (optional, uint32 per
+ * pixel) count samples taken and occupied bricks entered. */
+yv_status yv_volume_render(const yv_volume_device* vol, const yv_camera* cams,
+                           int32_t ncams, int32_t width, int32_t height,
+                           const yv_march_params* mp, float* rgba,
+                           uint32_t* samples, uint32_t* bricks, void* stream);
+
+/* Adjoint of yv_volume_render (fp32 volumes): re-marches every ray and
+ * accumulates dL/ddensity and dL/dalbedo (pool layout, ADDED to the
+ * buffers) from dL/drgba, given the forward output rgba. */
+yv_status yv_volume_backward(const yv_volume_device* vol,
+                             const yv_camera* cams, int32_t ncams,
+                             int32_t width, int32_t height,
+                             const yv_march_params* mp, const float* rgba,
+                             const float* grad_rgba, float* grad_density,
+                             float* grad_albedo, void* stream);
+
+/* Sums the gradient of every apron copy into its lattice point's owner and
+ * writes the total back to all copies (zero where the owner brick is
+ * absent), so that copies of a parameter stay equal under any update. */
+yv_status yv_volume_fold_aprons(const yv_volume_device* vol,
+                                float* grad_density, float* grad_albedo,
+                                void* stream);
+/* Copies owner values into the apron slots of fp32 density / albedo. */
+yv_status yv_volume_sync_aprons(const yv_volume_device* vol, float* density,
+                                float* albedo, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

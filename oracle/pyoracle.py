@@ -203,3 +203,66 @@ def setup_trace(pos, dir_):
     fl = np.zeros(1, np.uint32)
     ok = lib().orc_setup_trace_f32(_p(f32(pos)), _p(f32(dir_)), _p(t1), _p(t2), _p(fl))
     return bool(ok), t1, t2, int(fl[0])
+
+
+def _vol_arrays(grids, density, albedo):
+    g = np.ascontiguousarray(np.asarray(grids).reshape(-1).view(np.uint32)
+                             if np.asarray(grids).dtype != np.uint32 else np.asarray(grids).reshape(-1))
+    d = np.ascontiguousarray(np.asarray(density, np.float32).reshape(-1))
+    a = np.ascontiguousarray(np.asarray(albedo, np.float32).reshape(-1))
+    return g, d, a
+
+
+@_keeps
+def brick_render_f64(grids, density, albedo, levels, pos, dir_, up, fov, width, height,
+                     alpha_scale=1.0, step_vox=0.5, rows=None):
+    """FP64 brick march.  density (nb,729) float, albedo (nb,729,3) float in
+    [0,1].  Returns (h,w,4) float64 rgba, samples, bricks (h,w) uint32."""
+    g, d, a = _vol_arrays(grids, density, albedo)
+    d0, du, dv = init_ray_dir_f64(dir_, up, fov, width, height)
+    rgba = np.zeros(width * height * 4, np.float64)
+    ns = np.zeros(width * height, np.uint32)
+    nb = np.zeros(width * height, np.uint32)
+    y0, y1 = (0, height) if rows is None else rows
+    st = lib().orc_brick_render_f64(_p(g), len(g) // 64, _p(d), _p(a), len(d) // 729, levels,
+                                    _p(f64(pos)), _p(d0), _p(du), _p(dv), width, height,
+                                    float(alpha_scale), float(step_vox), y0, y1, _p(rgba),
+                                    _p(ns), _p(nb))
+    if st != 0:
+        raise RuntimeError(f"oracle brick render failed: {st}")
+    return rgba.reshape(height, width, 4), ns.reshape(height, width), nb.reshape(height, width)
+
+
+@_keeps
+def brick_render_f32_mt(grids, density, albedo, levels, pos, dir_, up, fov, width, height,
+                        alpha_scale=1.0, step_vox=0.5, threads=1):
+    g, d, a = _vol_arrays(grids, density, albedo)
+    d0, du, dv = init_ray_dir_f32(dir_, up, fov, width, height)
+    rgba = np.zeros(width * height * 4, np.float32)
+    ns = np.zeros(width * height, np.uint32)
+    nb = np.zeros(width * height, np.uint32)
+    st = lib().orc_brick_render_mt_f32(threads, _p(g), len(g) // 64, _p(d), _p(a),
+                                       len(d) // 729, levels, _p(f32(pos)), _p(d0), _p(du),
+                                       _p(dv), width, height, float(alpha_scale),
+                                       float(step_vox), _p(rgba), _p(ns), _p(nb))
+    if st != 0:
+        raise RuntimeError(f"oracle brick render failed: {st}")
+    return rgba.reshape(height, width, 4), ns.reshape(height, width), nb.reshape(height, width)
+
+
+@_keeps
+def brick_backward_f64(grids, density, albedo, levels, pos, dir_, up, fov, width, height,
+                       grad_rgba, alpha_scale=1.0, step_vox=0.5):
+    """FP64 adjoint: returns (grad_density (nb*729), grad_albedo (nb*729*3))
+    in pool layout, apron slots holding their own share."""
+    g, d, a = _vol_arrays(grids, density, albedo)
+    d0, du, dv = init_ray_dir_f64(dir_, up, fov, width, height)
+    gr = np.ascontiguousarray(np.asarray(grad_rgba, np.float64).reshape(-1))
+    gd = np.zeros(len(d), np.float64)
+    ga = np.zeros(len(a), np.float64)
+    st = lib().orc_brick_backward_f64(_p(g), len(g) // 64, _p(d), _p(a), len(d) // 729, levels,
+                                      _p(f64(pos)), _p(d0), _p(du), _p(dv), width, height,
+                                      float(alpha_scale), float(step_vox), _p(gr), _p(gd), _p(ga))
+    if st != 0:
+        raise RuntimeError(f"oracle brick backward failed: {st}")
+    return gd, ga

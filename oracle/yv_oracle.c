@@ -375,7 +375,9 @@ static void bwd_sample(void* user, const uint32_t* idx, const double* w,
     dalpha += u->g[k] * term;
   }
   double s = sigma * u->alpha_scale;
-  double dsigma = (s > 0.0 && s < 1.0) ? dalpha * u->alpha_scale : 0.0;
+  /* saturate'(s): 1 on [0, 1) (right derivative at 0, so empty lattice
+   * points still receive gradient), 0 elsewhere */
+  double dsigma = (s >= 0.0 && s < 1.0) ? dalpha * u->alpha_scale : 0.0;
   for (int j = 0; j < 8; ++j) {
     u->grad_density[idx[j]] += w[j] * dsigma;
     for (int k = 0; k < 3; ++k)

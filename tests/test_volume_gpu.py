@@ -1,0 +1,265 @@
+"""GPU brick-volume march, adjoint and apron maintenance vs the FP64 oracle.
+
+Bars: composited radiance within 1e-5 relative (+1e-6 absolute for values
+near zero) of the FP64 oracle, except rays whose sample set differs by a
+rounding tie (early-exit threshold or a cell boundary hit exactly), which are
+counted and must stay under 1e-3 of the rays; gradient relative error
+(L2 over the pool) <= 1e-4 against the FP64 adjoint."""
+import numpy as np
+import pytest
+
+from volume_util import fold_numpy
+
+pytestmark = pytest.mark.gpu
+
+RTOL, ATOL = 1e-5, 1e-6
+
+
+def gpu_inputs(vol, precision):
+    """Oracle-side float copies of exactly the values the GPU reads."""
+    if precision == 0:
+        den = vol.density.astype(np.float16).astype(np.float32)
+        alb = vol.albedo_u8.astype(np.float32) * np.float32(1.0 / 255.0)
+    else:
+        den = vol.density.astype(np.float32)
+        alb = vol.albedo_u8.astype(np.float32) * np.float32(1.0 / 255.0)
+    return den, alb
+
+
+def cam_at(pos, fov=60.0):
+    pos = np.asarray(pos, np.float32)
+    return (pos, (0.5 - pos).astype(np.float32), (0, 0, 1), fov)
+
+
+def compare_radiance(g, ref, ns_g, ns_ref):
+    g = g.astype(np.float64)
+    err = np.abs(g - ref)
+    ok = err <= RTOL * np.abs(ref) + ATOL
+    bad_rays = ~ok.all(axis=-1)
+    tie = bad_rays & (ns_g != ns_ref)
+    real = bad_rays & ~tie
+    return int(real.sum()), int(tie.sum()), float((err / (np.abs(ref) + ATOL)).max())
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_forward_matches_fp64_oracle(yoxel_mod, oracle, precision):
+    import torch
+    vol = yoxel_mod.BrickVolume.noise(2, 0.4, 1.4, 21)
+    gv = vol.upload(precision)
+    desc = gv.desc()
+    w, h = 96, 80
+    cams = [cam_at([1.6, 1.3, 1.1]), cam_at([-0.7, 0.4, 0.9], 50.0)]
+    ns = torch.zeros((len(cams), h, w), dtype=torch.int32, device="cuda")
+    out = yoxel_mod.render_volume(desc, cams, w, h, alpha_scale=1.0, step_vox=0.5,
+                                  samples=ns).cpu().numpy()
+    ns = ns.cpu().numpy().view(np.uint32)
+    den, alb = gpu_inputs(vol, precision)
+    tot_rays = 0
+    for i, (p, d, up, fov) in enumerate(cams):
+        ref, ns_ref, _ = oracle.brick_render_f64(vol.grids, den, alb, vol.levels, p, d, up,
+                                                 fov, w, h, alpha_scale=1.0, step_vox=0.5)
+        real, tie, worst = compare_radiance(out[i], ref, ns[i], ns_ref)
+        assert real == 0, f"cam {i}: {real} rays beyond tolerance (worst rel {worst:.3g})"
+        assert tie <= 1e-3 * w * h, f"cam {i}: {tie} tie rays"
+        assert ref[..., 3].max() > 0.5
+        tot_rays += w * h
+
+
+def test_forward_known_answer(yoxel_mod):
+    """Constant density 0.5, alpha_scale 1: A = 1 - 0.5^7 after 7 samples."""
+    s = 33
+    vol = yoxel_mod.BrickVolume.from_dense(1, np.full((s, s, s), 0.5, np.float32),
+                                           np.full((s, s, s, 3), 128, np.uint8))
+    gv = vol.upload(1)
+    out = yoxel_mod.render_volume(gv.desc(), [cam_at([-1.0, 0.5, 0.5], 10.0)], 4, 4,
+                                  alpha_scale=1.0).cpu().numpy()
+    a = np.float32(0.0)
+    for _ in range(7):
+        a = np.float32(a + np.float32(np.float32(1) - a) * np.float32(0.5))
+    assert np.all(out[..., 3] == a)
+    assert np.allclose(out[..., 0], (128 / 255) * (1 - 0.5 ** 7), rtol=1e-6)
+
+
+def test_samples_and_bricks_counters(yoxel_mod, oracle):
+    import torch
+    vol = yoxel_mod.BrickVolume.noise(1, 0.4, 1.4, 3)
+    gv = vol.upload(1)
+    w, h = 48, 48
+    ns = torch.zeros((1, h, w), dtype=torch.int32, device="cuda")
+    nb = torch.zeros((1, h, w), dtype=torch.int32, device="cuda")
+    c = cam_at([1.6, 1.3, 1.1])
+    yoxel_mod.render_volume(gv.desc(), [c], w, h, samples=ns, bricks=nb)
+    den, alb = gpu_inputs(vol, 1)
+    _, ns_ref, nb_ref = oracle.brick_render_f64(vol.grids, den, alb, 1, c[0], c[1], c[2], c[3],
+                                                w, h)
+    ns = ns.cpu().numpy()[0].view(np.uint32)
+    nb = nb.cpu().numpy()[0].view(np.uint32)
+    assert (ns != ns_ref).mean() < 1e-2 and (nb != nb_ref).mean() < 1e-2
+    assert ns.sum() > 0
+
+
+def test_backward_matches_fp64_adjoint(yoxel_mod, oracle):
+    import torch
+    vol = yoxel_mod.BrickVolume.noise(1, 0.4, 1.4, 3)
+    tv = vol.to_torch()
+    desc = yoxel_mod.torch_desc(tv)
+    w, h = 40, 32
+    cams = [cam_at([1.6, 1.3, 1.1]), cam_at([-0.8, 0.3, 0.2], 45.0)]
+    rgba = yoxel_mod.render_volume(desc, cams, w, h, alpha_scale=2.0)
+    rng = np.random.default_rng(5)
+    g = rng.standard_normal((len(cams), h, w, 4)).astype(np.float32)
+    gd = torch.zeros_like(tv["density"])
+    ga = torch.zeros_like(tv["albedo"])
+    yoxel_mod.volume_backward(desc, cams, w, h, rgba, torch.from_numpy(g).cuda(), gd, ga,
+                              alpha_scale=2.0, fold=False)
+    den, alb = gpu_inputs(vol, 1)
+    rd = np.zeros(vol.nbricks * 729)
+    ra = np.zeros(vol.nbricks * 729 * 3)
+    for i, (p, d, up, fov) in enumerate(cams):
+        a, b = oracle.brick_backward_f64(vol.grids, den, alb, 1, p, d, up, fov, w, h,
+                                         g[i].astype(np.float64), alpha_scale=2.0)
+        rd += a
+        ra += b
+    gd = gd.cpu().numpy().reshape(-1).astype(np.float64)
+    ga = ga.cpu().numpy().reshape(-1).astype(np.float64)
+    ed = np.linalg.norm(gd - rd) / np.linalg.norm(rd)
+    ea = np.linalg.norm(ga - ra) / np.linalg.norm(ra)
+    assert ed < 1e-4 and ea < 1e-4, (ed, ea)
+
+
+def test_apron_fold_and_sync(yoxel_mod):
+    import torch
+    vol = yoxel_mod.BrickVolume.noise(1, 0.4, 1.4, 4)
+    tv = vol.to_torch()
+    desc = yoxel_mod.torch_desc(tv)
+    rng = np.random.default_rng(2)
+    gd = rng.standard_normal(vol.nbricks * 729).astype(np.float32)
+    ga = rng.standard_normal(vol.nbricks * 729 * 3).astype(np.float32)
+    tgd = torch.from_numpy(gd.copy()).cuda()
+    tga = torch.from_numpy(ga.copy()).cuda()
+    import ctypes as C
+    from yoxel import _lib as L
+    L.check(L.lib.yv_volume_fold_aprons(C.byref(desc), C.c_void_p(tgd.data_ptr()),
+                                        C.c_void_p(tga.data_ptr()), None), "fold")
+    torch.cuda.synchronize()
+    assert np.allclose(tgd.cpu().numpy(), fold_numpy(vol, gd, 1), atol=1e-5)
+    assert np.allclose(tga.cpu().numpy(), fold_numpy(vol, ga, 3), atol=1e-5)
+    # sync: perturb owners, then aprons must repeat them again
+    den = tv["density"].clone()
+    den[:, 0] += 0.25
+    L.check(L.lib.yv_volume_sync_aprons(C.byref(yoxel_mod.torch_desc(tv, den)),
+                                        C.c_void_p(den.data_ptr()), None, None), "sync")
+    d = den.cpu().numpy().reshape(-1, 9, 9, 9)
+    up = vol.neighbors(True)
+    for b in range(vol.nbricks):
+        if up[b, 0] >= 0:
+            assert np.array_equal(d[b, :, :, 8], d[up[b, 0], :, :, 0])
+
+
+def naive_torch_march(torch, vol, den_t, alb_t, cam, w, h, alpha_scale, step_vox, oracle):
+    """Plain PyTorch FP64 ray-marcher over the same sample positions (found
+    by a Python restatement of the DDA) for the autograd cross-check."""
+    d0, du, dv = oracle.init_ray_dir_f64(cam[1], cam[2], cam[3], w, h)
+    S = 8 * 4 ** vol.levels
+    grids = vol.grids
+    nbc = 4 ** vol.levels
+    dt = step_vox / S
+
+    def lookup(c):
+        node = 0
+        for lev in range(vol.levels):
+            sh = 2 * (vol.levels - 1 - lev)
+            r = int(grids[node, ((((c[2] >> sh) & 3) * 4 + ((c[1] >> sh) & 3)) * 4 +
+                                 ((c[0] >> sh) & 3))])
+            if r & 0x80000000:
+                return -1
+            if r & 0x40000000:
+                return r & 0x3FFFFFFF
+            node = r
+        return -1
+
+    out = []
+    o = np.asarray(cam[0], np.float64)
+    for y in range(h):
+        for x in range(w):
+            d = d0 + du * x + dv * y
+            d = d / np.sqrt((d * d).sum())
+            d = np.where(np.abs(d) < 1e-5, np.copysign(1e-5, d), d)
+            inv = 1.0 / d
+            lo, hi = (0 - o) * inv, (1 - o) * inv
+            t1, t2 = np.minimum(lo, hi), np.maximum(lo, hi)
+            te, tx_ = max(t1.max(), 0.0), t2.min()
+            C = torch.zeros(3, dtype=torch.float64)
+            A = torch.zeros((), dtype=torch.float64)
+            if tx_ >= 0 and te <= tx_:
+                h_ = 8.0 / S
+                cell = [min(max(int(np.floor((o[i] + te * d[i]) / h_)), 0), nbc - 1)
+                        for i in range(3)]
+                t_in, done = te, False
+                while not done:
+                    txs = [((cell[i] + 1 if d[i] > 0 else cell[i]) * h_ - o[i]) * inv[i]
+                           for i in range(3)]
+                    e = int(np.argmin(txs))
+                    t_out = txs[e]
+                    b = lookup(cell)
+                    if b >= 0:
+                        k = int(np.ceil(t_in / dt))
+                        while k * dt < t_out:
+                            t = k * dt
+                            ll = (o + t * d) * S - 8 * np.asarray(cell)
+                            i0 = np.clip(np.floor(ll).astype(int), 0, 7)
+                            f = np.clip(ll - i0, 0, 1)
+                            sig = 0
+                            col = 0
+                            for j in range(8):
+                                dx_, dy_, dz_ = j & 1, (j >> 1) & 1, j >> 2
+                                wgt = ((f[0] if dx_ else 1 - f[0]) * (f[1] if dy_ else 1 - f[1]) *
+                                       (f[2] if dz_ else 1 - f[2]))
+                                idx = b * 729 + ((i0[2] + dz_) * 9 + i0[1] + dy_) * 9 + i0[0] + dx_
+                                sig = sig + wgt * den_t[idx]
+                                col = col + wgt * alb_t[idx]
+                            a = torch.clamp(sig * alpha_scale, 0, 1)
+                            wt = (1 - A) * a
+                            C = C + wt * col
+                            A = A + wt
+                            k += 1
+                            if A.item() > 0.99:
+                                done = True
+                                break
+                    if done:
+                        break
+                    t_in = t_out
+                    cell[e] += 1 if d[e] > 0 else -1
+                    if not 0 <= cell[e] < nbc:
+                        break
+            out.append(torch.cat([C, A.reshape(1)]))
+    return torch.stack(out).reshape(h, w, 4)
+
+
+def test_autograd_function_matches_naive_torch_marcher(yoxel_mod, oracle):
+    import torch
+    vol = yoxel_mod.BrickVolume.noise(1, 0.4, 1.4, 3)
+    tv = vol.to_torch()
+    den = tv["density"].clone().requires_grad_(True)
+    alb = tv["albedo"].clone().requires_grad_(True)
+    w, h = 10, 8
+    cam = cam_at([1.6, 1.3, 1.1], 40.0)
+    rgba = yoxel_mod.volume_march(den, alb, tv, [cam], w, h, 2.0, 0.5)
+    rng = np.random.default_rng(9)
+    wts = torch.from_numpy(rng.standard_normal((1, h, w, 4)).astype(np.float32)).cuda()
+    (rgba * wts).sum().backward()
+    # naive marcher differentiates every pool slot separately; fold its result
+    den64 = torch.from_numpy(den.detach().cpu().numpy().reshape(-1).astype(np.float64))
+    alb64 = torch.from_numpy(alb.detach().cpu().numpy().reshape(-1, 3).astype(np.float64))
+    den64.requires_grad_(True)
+    alb64.requires_grad_(True)
+    ref = naive_torch_march(torch, vol, den64, alb64, cam, w, h, 2.0, 0.5, oracle)
+    assert np.allclose(ref.detach().numpy(), rgba.detach().cpu().numpy()[0], rtol=1e-4,
+                       atol=1e-6)
+    (ref * wts.cpu().double()[0]).sum().backward()
+    gref_d = fold_numpy(vol, den64.grad.numpy(), 1)
+    gref_a = fold_numpy(vol, alb64.grad.numpy().reshape(-1), 3)
+    gd = den.grad.cpu().numpy().reshape(-1)
+    ga = alb.grad.cpu().numpy().reshape(-1)
+    assert np.linalg.norm(gd - gref_d) / np.linalg.norm(gref_d) < 1e-4
+    assert np.linalg.norm(ga - gref_a) / np.linalg.norm(gref_a) < 1e-4

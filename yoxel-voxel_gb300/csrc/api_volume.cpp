@@ -1,0 +1,274 @@
+// api_volume.cpp - C ABI of the brick-volume path: device upload of the
+// ntree pool (BrickPool<T>, ntree/BrickManager.h:5-80), the multi-camera
+// march (the working kernel behind ntree's RunTrace entry,
+// ntree/ntree_trace.cuh:22-28) and its adjoint.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "yv_internal.h"
+#include "yv_volume.h"
+
+using namespace yv;
+
+struct yv_volume_gpu {
+  int device = 0;
+  yv_volume_device desc;
+  void* mem[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+};
+
+namespace {
+
+yv_status fail(cudaError_t e, const char* what) {
+  set_last_error(std::string(what) + ": " + cudaGetErrorString(e));
+  cudaGetLastError();
+  return e == cudaErrorMemoryAllocation ? YV_ERR_OUT_OF_MEMORY : YV_ERR_CUDA;
+}
+
+// IEEE binary32 -> binary16, round to nearest even (host side, own code).
+uint16_t f32_to_f16(float f) {
+  uint32_t x;
+  std::memcpy(&x, &f, 4);
+  const uint32_t sign = (x >> 16) & 0x8000u;
+  const int32_t exp = (int32_t)((x >> 23) & 0xFFu);
+  uint32_t man = x & 0x7FFFFFu;
+  if (exp == 0xFF) return (uint16_t)(sign | 0x7C00u | (man ? 0x200u : 0u));
+  int32_t e = exp - 127 + 15;
+  if (e >= 0x1F) return (uint16_t)(sign | 0x7C00u);
+  if (e <= 0) {
+    if (e < -10) return (uint16_t)sign;
+    man |= 0x800000u;
+    const int shift = 14 - e;
+    uint32_t h = man >> shift;
+    const uint32_t rem = man & ((1u << shift) - 1u), half = 1u << (shift - 1);
+    if (rem > half || (rem == half && (h & 1u))) ++h;
+    return (uint16_t)(sign | h);
+  }
+  uint32_t h = ((uint32_t)e << 10) | (man >> 13);
+  const uint32_t rem = man & 0x1FFFu;
+  if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) ++h;
+  return (uint16_t)(sign | h);
+}
+
+bool fill_args(const yv_volume_device* v, const yv_march_params* mp, int width, int height,
+               VolumeArgs* a) {
+  if (!v || !mp || !v->grids || v->levels < 1 || v->levels > 5 || width <= 0 || height <= 0 ||
+      !(mp->step_vox > 0.f) || !std::isfinite(mp->alpha_scale))
+    return false;
+  std::memset(a, 0, sizeof(*a));
+  a->grids = v->grids;
+  a->ngrids = v->ngrids;
+  a->levels = v->levels;
+  a->nb = 1 << (2 * v->levels);
+  a->density = v->density;
+  a->albedo = v->albedo;
+  a->nbricks = v->nbricks;
+  a->precision = v->precision;
+  a->nbr_up = v->nbr_up;
+  a->nbr_dn = v->nbr_dn;
+  a->S = (float)(8 * a->nb);
+  a->cell_size = 8.0f / a->S;
+  a->alpha_scale = mp->alpha_scale;
+  a->dt = mp->step_vox / a->S;
+  a->inv_dt = a->S / mp->step_vox;
+  a->width = width;
+  a->height = height;
+  return true;
+}
+
+void set_cams(VolumeArgs* a, const yv_camera* cams, int n) {
+  a->ncams = n;
+  for (int i = 0; i < n; ++i) {
+    CamBasis& b = a->cam[i];
+    std::memcpy(b.pos, cams[i].pos, sizeof(b.pos));
+    init_ray_dir(cams[i].dir, cams[i].up, cams[i].fov_deg, a->width, a->height, b.dir0, b.du,
+                 b.dv);
+  }
+}
+
+bool cams_ok(const yv_camera* c, int n) {
+  if (!c || n <= 0) return false;
+  for (int i = 0; i < n; ++i) {
+    for (int k = 0; k < 3; ++k)
+      if (!std::isfinite(c[i].pos[k]) || !std::isfinite(c[i].dir[k]) || !std::isfinite(c[i].up[k]))
+        return false;
+    if (!(c[i].fov_deg > 0.f && c[i].fov_deg < 180.f)) return false;
+  }
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+yv_status yv_volume_upload(const yv_volume_host* v, int32_t precision, yv_volume_gpu** out) {
+  if (!v || !out || (precision != YV_PRECISION_F16 && precision != YV_PRECISION_F32))
+    return YV_ERR_INVALID_ARG;
+  *out = nullptr;
+  yv_volume_gpu* g = new (std::nothrow) yv_volume_gpu();
+  if (!g) return YV_ERR_OUT_OF_MEMORY;
+  cudaGetDevice(&g->device);
+  const uint32_t ng = yv_volume_grid_count(v), nb = yv_volume_brick_count(v);
+  const size_t n = (size_t)nb * 729u;
+  const float* den = yv_volume_density(v);
+  const uint8_t* alb = yv_volume_albedo(v);
+  // host-side validation of the refs (the kernels also bound-check)
+  const uint32_t* grids = yv_volume_grids(v);
+  for (size_t i = 0; i < (size_t)ng * 64; ++i) {
+    uint32_t r = grids[i];
+    if (r & 0x80000000u) continue;
+    if ((r & 0x40000000u) ? (r & 0x3FFFFFFFu) >= nb : r >= ng) {
+      delete g;
+      set_last_error("volume child ref out of range");
+      return YV_ERR_BAD_POOL;
+    }
+  }
+  std::vector<uint8_t> dbuf, abuf;
+  size_t dbytes, abytes;
+  if (precision == YV_PRECISION_F16) {
+    dbytes = n * 2;
+    abytes = n * 4;
+    dbuf.resize(dbytes);
+    abuf.resize(abytes);
+    uint16_t* d16 = reinterpret_cast<uint16_t*>(dbuf.data());
+    for (size_t i = 0; i < n; ++i) {
+      d16[i] = f32_to_f16(den[i]);
+      abuf[i * 4] = alb[i * 3];
+      abuf[i * 4 + 1] = alb[i * 3 + 1];
+      abuf[i * 4 + 2] = alb[i * 3 + 2];
+      abuf[i * 4 + 3] = 255;
+    }
+  } else {
+    dbytes = n * 4;
+    abytes = n * 12;
+    dbuf.resize(dbytes);
+    abuf.resize(abytes);
+    std::memcpy(dbuf.data(), den, dbytes);
+    float* af = reinterpret_cast<float*>(abuf.data());
+    for (size_t i = 0; i < n * 3; ++i) af[i] = (float)alb[i] * (1.0f / 255.0f);
+  }
+  const void* src[5] = {grids, dbuf.data(), abuf.data(), yv_volume_neighbors(v, 1),
+                        yv_volume_neighbors(v, 0)};
+  const size_t bytes[5] = {(size_t)ng * 256u, dbytes, abytes, (size_t)nb * 28u, (size_t)nb * 28u};
+  for (int i = 0; i < 5; ++i) {
+    if (!bytes[i]) continue;
+    cudaError_t e = cudaMalloc(&g->mem[i], bytes[i]);
+    if (e == cudaSuccess) e = cudaMemcpy(g->mem[i], src[i], bytes[i], cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      yv_volume_gpu_free(g);
+      return fail(e, "volume upload");
+    }
+  }
+  g->desc.grids = static_cast<const uint32_t*>(g->mem[0]);
+  g->desc.ngrids = ng;
+  g->desc.levels = yv_volume_levels(v);
+  g->desc.density = g->mem[1];
+  g->desc.albedo = g->mem[2];
+  g->desc.nbricks = nb;
+  g->desc.precision = precision;
+  g->desc.nbr_up = static_cast<const int32_t*>(g->mem[3]);
+  g->desc.nbr_dn = static_cast<const int32_t*>(g->mem[4]);
+  *out = g;
+  return YV_OK;
+}
+
+void yv_volume_gpu_free(yv_volume_gpu* g) {
+  if (!g) return;
+  cudaSetDevice(g->device);
+  for (void* p : g->mem) cudaFree(p);
+  delete g;
+}
+
+yv_status yv_volume_gpu_desc(const yv_volume_gpu* g, yv_volume_device* out) {
+  if (!g || !out) return YV_ERR_INVALID_ARG;
+  *out = g->desc;
+  return YV_OK;
+}
+
+yv_status yv_volume_render(const yv_volume_device* vol, const yv_camera* cams, int32_t ncams,
+                           int32_t width, int32_t height, const yv_march_params* mp, float* rgba,
+                           uint32_t* samples, uint32_t* bricks, void* stream) {
+  VolumeArgs* a = new (std::nothrow) VolumeArgs;
+  if (!a) return YV_ERR_OUT_OF_MEMORY;
+  if (!fill_args(vol, mp, width, height, a) || !cams_ok(cams, ncams) || !rgba ||
+      !vol->density || !vol->albedo) {
+    delete a;
+    return YV_ERR_INVALID_ARG;
+  }
+  const size_t px = (size_t)width * (size_t)height;
+  for (int c0 = 0; c0 < ncams; c0 += kMaxVolumeCams) {
+    const int n = ncams - c0 < kMaxVolumeCams ? ncams - c0 : kMaxVolumeCams;
+    set_cams(a, cams + c0, n);
+    a->rgba = rgba + (size_t)c0 * px * 4;
+    a->samples = samples ? samples + (size_t)c0 * px : nullptr;
+    a->bricks_entered = bricks ? bricks + (size_t)c0 * px : nullptr;
+    cudaError_t e = launch_volume_forward(*a, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) {
+      delete a;
+      return fail(e, "volume forward launch");
+    }
+  }
+  delete a;
+  return YV_OK;
+}
+
+yv_status yv_volume_backward(const yv_volume_device* vol, const yv_camera* cams, int32_t ncams,
+                             int32_t width, int32_t height, const yv_march_params* mp,
+                             const float* rgba, const float* grad_rgba, float* grad_density,
+                             float* grad_albedo, void* stream) {
+  VolumeArgs* a = new (std::nothrow) VolumeArgs;
+  if (!a) return YV_ERR_OUT_OF_MEMORY;
+  if (!fill_args(vol, mp, width, height, a) || !cams_ok(cams, ncams) || !rgba || !grad_rgba ||
+      !grad_density || !grad_albedo || vol->precision != YV_PRECISION_F32) {
+    delete a;
+    return YV_ERR_INVALID_ARG;
+  }
+  const size_t px = (size_t)width * (size_t)height;
+  for (int c0 = 0; c0 < ncams; c0 += kMaxVolumeCams) {
+    const int n = ncams - c0 < kMaxVolumeCams ? ncams - c0 : kMaxVolumeCams;
+    set_cams(a, cams + c0, n);
+    a->rgba_fwd = rgba + (size_t)c0 * px * 4;
+    a->grad_rgba = grad_rgba + (size_t)c0 * px * 4;
+    a->grad_density = grad_density;
+    a->grad_albedo = grad_albedo;
+    cudaError_t e = launch_volume_backward(*a, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) {
+      delete a;
+      return fail(e, "volume backward launch");
+    }
+  }
+  delete a;
+  return YV_OK;
+}
+
+yv_status yv_volume_fold_aprons(const yv_volume_device* vol, float* grad_density,
+                                float* grad_albedo, void* stream) {
+  if (!vol || !vol->nbr_up || !vol->nbr_dn) return YV_ERR_INVALID_ARG;
+  VolumeArgs a;
+  yv_march_params mp = {1.f, 1.f};
+  if (!fill_args(vol, &mp, 1, 1, &a)) return YV_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaSuccess;
+  if (grad_density) e = launch_apron_fold(a, 1, grad_density, true, s);
+  if (e == cudaSuccess && grad_albedo) e = launch_apron_fold(a, 3, grad_albedo, true, s);
+  return e == cudaSuccess ? YV_OK : fail(e, "apron fold");
+}
+
+yv_status yv_volume_sync_aprons(const yv_volume_device* vol, float* density, float* albedo,
+                                void* stream) {
+  if (!vol || !vol->nbr_up || vol->precision != YV_PRECISION_F32) return YV_ERR_INVALID_ARG;
+  VolumeArgs a;
+  yv_march_params mp = {1.f, 1.f};
+  if (!fill_args(vol, &mp, 1, 1, &a)) return YV_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaSuccess;
+  if (density) e = launch_apron_fold(a, 1, density, false, s);
+  if (e == cudaSuccess && albedo) e = launch_apron_fold(a, 3, albedo, false, s);
+  return e == cudaSuccess ? YV_OK : fail(e, "apron sync");
+}
+
+}  // extern "C"

@@ -1,0 +1,57 @@
+// yv_volume.h - launch interface of the brick-volume kernels (host side).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace yv {
+
+constexpr int kMaxVolumeCams = 64;  // cameras per launch (kernel-parameter table)
+
+// RendererBase::InitRayDir basis of one camera.
+struct CamBasis {
+  float pos[3];
+  float dir0[3], du[3], dv[3];
+};
+
+struct VolumeArgs {
+  // tree + pool (device pointers)
+  const uint32_t* grids;
+  uint32_t ngrids;
+  int levels;
+  int nb;                // brick cells per axis = 4^levels
+  const void* density;   // precision 0: fp16, 1: fp32 (nbricks*729)
+  const void* albedo;    // precision 0: uchar4, 1: fp32x3
+  uint32_t nbricks;
+  int precision;
+  const int32_t* nbr_up;  // nbricks*7
+  const int32_t* nbr_dn;  // nbricks*7
+  // march
+  float S;               // lattice cells per axis
+  float cell_size;       // world size of a brick cell = 8/S
+  float alpha_scale;
+  float dt, inv_dt;      // world step and its inverse
+  // cameras
+  int ncams, width, height;
+  CamBasis cam[kMaxVolumeCams];
+  // outputs / adjoint inputs
+  float* rgba;            // ncams*h*w float4
+  uint32_t* samples;      // optional per-ray counters
+  uint32_t* bricks_entered;
+  const float* rgba_fwd;  // backward: forward output
+  const float* grad_rgba; // backward: dL/d rgba
+  float* grad_density;    // backward outputs (pool layout)
+  float* grad_albedo;
+  uint32_t* status;       // optional device status word
+};
+
+cudaError_t launch_volume_forward(const VolumeArgs& a, cudaStream_t s);
+cudaError_t launch_volume_backward(const VolumeArgs& a, cudaStream_t s);
+// gather=true: fold apron gradients into owners, then copy owners to aprons;
+// gather=false: copy owners to aprons only (parameter sync).
+cudaError_t launch_apron_fold(const VolumeArgs& a, int channels, float* g, bool gather,
+                              cudaStream_t s);
+int device_sm_count_vol();
+
+}  // namespace yv

@@ -8,6 +8,9 @@ from . import _lib
 from ._lib import YvError, LIB_PATH
 from .svo import SVOScene, NODE_DTYPE, ATTR_DTYPE
 from .renderer import Renderer, CudaRenderer
+from .volume import (BrickVolume, VolumeGPU, render_volume, volume_backward, volume_march,
+                     torch_desc, cameras, sphere_cameras)
 
 __all__ = ["SVOScene", "Renderer", "CudaRenderer", "YvError", "LIB_PATH",
-           "NODE_DTYPE", "ATTR_DTYPE"]
+           "NODE_DTYPE", "ATTR_DTYPE", "BrickVolume", "VolumeGPU", "render_volume",
+           "volume_backward", "volume_march", "torch_desc", "cameras", "sphere_cameras"]

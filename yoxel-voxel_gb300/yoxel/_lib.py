@@ -67,6 +67,24 @@ class LaunchConfig(C.Structure):
                 ("smem_nodes", C.c_int32), ("tile_rays", C.c_int32)]
 
 
+class VolumeDevice(C.Structure):
+    _fields_ = [("grids", C.c_void_p), ("ngrids", C.c_uint32), ("levels", C.c_int32),
+                ("density", C.c_void_p), ("albedo", C.c_void_p), ("nbricks", C.c_uint32),
+                ("precision", C.c_int32), ("nbr_up", C.c_void_p), ("nbr_dn", C.c_void_p)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("dir", C.c_float * 3), ("up", C.c_float * 3),
+                ("fov_deg", C.c_float)]
+
+
+class MarchParams(C.Structure):
+    _fields_ = [("alpha_scale", C.c_float), ("step_vox", C.c_float)]
+
+
+YV_PRECISION_F16 = 0
+YV_PRECISION_F32 = 1
+
 F3 = C.c_float * 3
 P = C.c_void_p
 U32 = C.c_uint32
@@ -109,6 +127,26 @@ _SIGS = {
     "yv_renderer_frame_stats": (S, [P, C.POINTER(FrameStats)]),
     "yv_get_ray_basis": (S, [P, F3, F3, F3]),
     "yv_get_device_scene_info": (S, [P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    "yv_volume_gen_noise": (S, [C.POINTER(P), I32, C.c_float, C.c_float, C.c_uint64]),
+    "yv_volume_from_dense": (S, [C.POINTER(P), I32, P, P]),
+    "yv_volume_free": (None, [P]),
+    "yv_volume_levels": (I32, [P]),
+    "yv_volume_grid_count": (U32, [P]),
+    "yv_volume_grids": (P, [P]),
+    "yv_volume_brick_count": (U32, [P]),
+    "yv_volume_density": (P, [P]),
+    "yv_volume_albedo": (P, [P]),
+    "yv_volume_brick_cells": (P, [P]),
+    "yv_volume_neighbors": (P, [P, I32]),
+    "yv_volume_upload": (S, [P, C.c_int32, C.POINTER(P)]),
+    "yv_volume_gpu_free": (None, [P]),
+    "yv_volume_gpu_desc": (S, [P, C.POINTER(VolumeDevice)]),
+    "yv_volume_render": (S, [C.POINTER(VolumeDevice), C.POINTER(Camera), C.c_int32, C.c_int32,
+                             C.c_int32, C.POINTER(MarchParams), P, P, P, P]),
+    "yv_volume_backward": (S, [C.POINTER(VolumeDevice), C.POINTER(Camera), C.c_int32,
+                               C.c_int32, C.c_int32, C.POINTER(MarchParams), P, P, P, P, P]),
+    "yv_volume_fold_aprons": (S, [C.POINTER(VolumeDevice), P, P, P]),
+    "yv_volume_sync_aprons": (S, [C.POINTER(VolumeDevice), P, P, P]),
 }
 
 

@@ -1,0 +1,274 @@
+"""Brick volumes in the ntree layout and the differentiable ray-march.
+
+`BrickVolume` wraps the host tree + brick pool (ntree::Node / RangeBuilder /
+BrickPool<T>, ntree/ntree/nodes.h, ntree/ntree/ntree.h, ntree/BrickManager.h);
+`render_volume` is the multi-camera march (the kernel behind ntree's RunTrace
+entry, ntree/ntree_trace.cuh:27); `VolumeMarch` is a torch.autograd.Function
+whose backward re-marches every ray in the CUDA adjoint kernel.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream(stream):
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+class BrickVolume:
+    """Host brick volume (grid tree + 9^3-lattice brick pool)."""
+
+    def __init__(self, handle):
+        self._h = C.c_void_p(handle)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            L.lib.yv_volume_free(h)
+            self._h = C.c_void_p(None)
+
+    @classmethod
+    def noise(cls, levels=3, offset=0.4, amplitude=1.0, seed=1234):
+        h = C.c_void_p()
+        L.check(L.lib.yv_volume_gen_noise(C.byref(h), levels, offset, amplitude, seed),
+                "yv_volume_gen_noise")
+        return cls(h.value)
+
+    @classmethod
+    def from_dense(cls, levels, density, albedo=None):
+        density = np.ascontiguousarray(density, np.float32)
+        s = 8 * 4 ** levels + 1
+        if density.shape != (s, s, s):
+            raise ValueError(f"density must be {(s, s, s)} (z, y, x) lattice")
+        a = None
+        if albedo is not None:
+            albedo = np.ascontiguousarray(albedo, np.uint8)
+            if albedo.shape != (s, s, s, 3):
+                raise ValueError("albedo must be (S+1)^3 x 3 uint8")
+            a = albedo.ctypes.data
+        h = C.c_void_p()
+        L.check(L.lib.yv_volume_from_dense(C.byref(h), levels, density.ctypes.data, a),
+                "yv_volume_from_dense")
+        return cls(h.value)
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def levels(self):
+        return int(L.lib.yv_volume_levels(self._h))
+
+    @property
+    def size(self):
+        """Lattice cells per axis (CalcSceneSize with N = 4, B = 8)."""
+        return 8 * 4 ** self.levels
+
+    @property
+    def nbricks(self):
+        return int(L.lib.yv_volume_brick_count(self._h))
+
+    @property
+    def ngrids(self):
+        return int(L.lib.yv_volume_grid_count(self._h))
+
+    def _view(self, ptr, ctype, count, shape):
+        if count == 0:
+            return np.zeros(shape, np.dtype(ctype))
+        buf = (ctype * count).from_address(ptr)
+        a = np.frombuffer(buf, dtype=np.dtype(ctype)).reshape(shape)
+        a.flags.writeable = False
+        return a
+
+    @property
+    def grids(self):
+        return self._view(L.lib.yv_volume_grids(self._h), C.c_uint32, self.ngrids * 64,
+                          (self.ngrids, 64))
+
+    @property
+    def density(self):
+        return self._view(L.lib.yv_volume_density(self._h), C.c_float, self.nbricks * 729,
+                          (self.nbricks, 729))
+
+    @property
+    def albedo_u8(self):
+        return self._view(L.lib.yv_volume_albedo(self._h), C.c_uint8, self.nbricks * 2187,
+                          (self.nbricks, 729, 3))
+
+    @property
+    def cells(self):
+        return self._view(L.lib.yv_volume_brick_cells(self._h), C.c_int32, self.nbricks * 3,
+                          (self.nbricks, 3))
+
+    def neighbors(self, upper):
+        return self._view(L.lib.yv_volume_neighbors(self._h, 1 if upper else 0), C.c_int32,
+                          self.nbricks * 7, (self.nbricks, 7))
+
+    @property
+    def occupancy(self):
+        return self.nbricks / float(4 ** (3 * self.levels))
+
+    def upload(self, precision=L.YV_PRECISION_F16):
+        return VolumeGPU(self, precision)
+
+    def to_torch(self, device="cuda"):
+        """Learnable fp32 copy: dict of torch tensors (grids, density (nb,729),
+        albedo (nb,729,3) in [0,1], nbr_up, nbr_dn) on `device`."""
+        torch = _torch()
+        return dict(
+            levels=self.levels,
+            grids=torch.from_numpy(self.grids.astype(np.int32)).to(device),
+            density=torch.from_numpy(self.density.copy()).to(device),
+            albedo=torch.from_numpy((self.albedo_u8.astype(np.float32) *
+                                     np.float32(1.0 / 255.0))).to(device),
+            nbr_up=torch.from_numpy(self.neighbors(True).copy()).to(device),
+            nbr_dn=torch.from_numpy(self.neighbors(False).copy()).to(device),
+        )
+
+
+class VolumeGPU:
+    """Library-owned device copy of a BrickVolume (fp16 or fp32 pool)."""
+
+    def __init__(self, vol, precision):
+        h = C.c_void_p()
+        L.check(L.lib.yv_volume_upload(vol.handle, precision, C.byref(h)), "yv_volume_upload")
+        self._h = h
+        self.precision = precision
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            L.lib.yv_volume_gpu_free(h)
+            self._h = C.c_void_p(None)
+
+    def desc(self):
+        d = L.VolumeDevice()
+        L.check(L.lib.yv_volume_gpu_desc(self._h, C.byref(d)), "yv_volume_gpu_desc")
+        return d
+
+
+def torch_desc(tv, density=None, albedo=None):
+    """VolumeDevice over torch tensors from BrickVolume.to_torch()."""
+    density = tv["density"] if density is None else density
+    albedo = tv["albedo"] if albedo is None else albedo
+    d = L.VolumeDevice()
+    d.grids = tv["grids"].data_ptr()
+    d.ngrids = tv["grids"].shape[0]
+    d.levels = tv["levels"]
+    d.density = density.data_ptr()
+    d.albedo = albedo.data_ptr()
+    d.nbricks = density.shape[0]
+    d.precision = L.YV_PRECISION_F32
+    d.nbr_up = tv["nbr_up"].data_ptr()
+    d.nbr_dn = tv["nbr_dn"].data_ptr()
+    return d
+
+
+def cameras(cams):
+    """ctypes array of yv_camera from (pos, dir, up, fov_deg) tuples."""
+    arr = (L.Camera * len(cams))()
+    for i, (p, d, u, f) in enumerate(cams):
+        arr[i].pos = L.F3(*[float(v) for v in p])
+        arr[i].dir = L.F3(*[float(v) for v in d])
+        arr[i].up = L.F3(*[float(v) for v in u])
+        arr[i].fov_deg = float(f)
+    return arr
+
+
+def sphere_cameras(n, radius=1.5, fov=60.0, center=(0.5, 0.5, 0.5)):
+    """n cameras on a Fibonacci sphere looking at the centre."""
+    cams = []
+    ga = np.pi * (3.0 - np.sqrt(5.0))
+    c = np.asarray(center, np.float64)
+    for i in range(n):
+        z = 1.0 - 2.0 * (i + 0.5) / n
+        r = np.sqrt(max(0.0, 1.0 - z * z))
+        d = np.array([np.cos(ga * i) * r, np.sin(ga * i) * r, z])
+        pos = c + radius * d
+        up = (0, 0, 1) if abs(d[2]) < 0.99 else (0, 1, 0)
+        cams.append((pos.astype(np.float32), (-d).astype(np.float32), up, fov))
+    return cams
+
+
+def render_volume(desc, cams, width, height, alpha_scale=1.0, step_vox=0.5, out=None,
+                  samples=None, bricks=None, stream=None):
+    """Composited RGBA, (ncams, h, w, 4) float32 CUDA tensor."""
+    torch = _torch()
+    ca = cams if isinstance(cams, C.Array) else cameras(cams)
+    n = len(ca)
+    if out is None:
+        out = torch.empty((n, height, width, 4), dtype=torch.float32, device="cuda")
+    mp = L.MarchParams(float(alpha_scale), float(step_vox))
+    L.check(L.lib.yv_volume_render(C.byref(desc), ca, n, width, height, C.byref(mp),
+                                   C.c_void_p(out.data_ptr()),
+                                   None if samples is None else C.c_void_p(samples.data_ptr()),
+                                   None if bricks is None else C.c_void_p(bricks.data_ptr()),
+                                   _stream(stream)), "yv_volume_render")
+    return out
+
+
+def volume_backward(desc, cams, width, height, rgba, grad_rgba, grad_density, grad_albedo,
+                    alpha_scale=1.0, step_vox=0.5, fold=True, stream=None):
+    ca = cams if isinstance(cams, C.Array) else cameras(cams)
+    mp = L.MarchParams(float(alpha_scale), float(step_vox))
+    L.check(L.lib.yv_volume_backward(C.byref(desc), ca, len(ca), width, height, C.byref(mp),
+                                     C.c_void_p(rgba.data_ptr()),
+                                     C.c_void_p(grad_rgba.data_ptr()),
+                                     C.c_void_p(grad_density.data_ptr()),
+                                     C.c_void_p(grad_albedo.data_ptr()), _stream(stream)),
+            "yv_volume_backward")
+    if fold:
+        L.check(L.lib.yv_volume_fold_aprons(C.byref(desc), C.c_void_p(grad_density.data_ptr()),
+                                            C.c_void_p(grad_albedo.data_ptr()),
+                                            _stream(stream)), "yv_volume_fold_aprons")
+
+
+def _make_function():
+    torch = _torch()
+
+    class VolumeMarch(torch.autograd.Function):
+        """rgba = march(density, albedo); backward re-marches each ray."""
+
+        @staticmethod
+        def forward(ctx, density, albedo, tv, cams, width, height, alpha_scale, step_vox):
+            density = density.contiguous()
+            albedo = albedo.contiguous()
+            desc = torch_desc(tv, density, albedo)
+            ca = cams if isinstance(cams, C.Array) else cameras(cams)
+            rgba = render_volume(desc, ca, width, height, alpha_scale, step_vox)
+            ctx.save_for_backward(density, albedo, rgba)
+            ctx.meta = (tv, ca, width, height, alpha_scale, step_vox)
+            return rgba
+
+        @staticmethod
+        def backward(ctx, grad_rgba):
+            density, albedo, rgba = ctx.saved_tensors
+            tv, ca, width, height, alpha_scale, step_vox = ctx.meta
+            gd = torch.zeros_like(density)
+            ga = torch.zeros_like(albedo)
+            desc = torch_desc(tv, density, albedo)
+            volume_backward(desc, ca, width, height, rgba, grad_rgba.contiguous(), gd, ga,
+                            alpha_scale, step_vox)
+            return gd, ga, None, None, None, None, None, None
+
+    return VolumeMarch
+
+
+_VolumeMarch = None
+
+
+def volume_march(density, albedo, tv, cams, width, height, alpha_scale=1.0, step_vox=0.5):
+    """Differentiable multi-camera march (torch.autograd)."""
+    global _VolumeMarch
+    if _VolumeMarch is None:
+        _VolumeMarch = _make_function()
+    return _VolumeMarch.apply(density, albedo, tv, cams, width, height, alpha_scale, step_vox)
