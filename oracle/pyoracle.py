@@ -44,6 +44,8 @@ def load_library(build_if_missing=True):
         "orc_setup_trace_f32": (I, [P, P, P, P, P]),
         "orc_brick_render_f64": (I, [P, U, P, P, U, I, P, P, P, P, I, I, D, D, I, I, P, P, P]),
         "orc_brick_render_f32": (I, [P, U, P, P, U, I, P, P, P, P, I, I, F, F, I, I, P, P, P]),
+        "orc_brick_render_f64_f32ray": (I, [P, U, P, P, U, I, P, P, P, P, I, I, D, D, I, I,
+                                            P, P, P]),
         "orc_brick_render_mt_f32": (I, [I, P, U, P, P, U, I, P, P, P, P, I, I, F, F, P, P, P]),
         "orc_brick_backward_f64": (I, [P, U, P, P, U, I, P, P, P, P, I, I, D, D, P, P, P]),
     }
@@ -266,3 +268,23 @@ def brick_backward_f64(grids, density, albedo, levels, pos, dir_, up, fov, width
     if st != 0:
         raise RuntimeError(f"oracle brick backward failed: {st}")
     return gd, ga
+
+
+@_keeps
+def brick_render_f64_f32ray(grids, density, albedo, levels, pos, dir_, up, fov, width, height,
+                            alpha_scale=1.0, step_vox=0.5, rows=None):
+    """FP64 march of the FP32-generated primary rays (the rays the CUDA path
+    casts), so the comparison measures the march arithmetic alone."""
+    g, d, a = _vol_arrays(grids, density, albedo)
+    d0, du, dv = init_ray_dir_f32(dir_, up, fov, width, height)
+    rgba = np.zeros(width * height * 4, np.float64)
+    ns = np.zeros(width * height, np.uint32)
+    nb = np.zeros(width * height, np.uint32)
+    y0, y1 = (0, height) if rows is None else rows
+    st = lib().orc_brick_render_f64_f32ray(_p(g), len(g) // 64, _p(d), _p(a), len(d) // 729,
+                                           levels, _p(f32(pos)), _p(d0), _p(du), _p(dv), width,
+                                           height, float(alpha_scale), float(step_vox), y0, y1,
+                                           _p(rgba), _p(ns), _p(nb))
+    if st != 0:
+        raise RuntimeError(f"oracle brick render failed: {st}")
+    return rgba.reshape(height, width, 4), ns.reshape(height, width), nb.reshape(height, width)

@@ -344,6 +344,44 @@ int orc_setup_trace_f32(const float pos[3], const float dir[3], float t1[3],
   return setup_trace_f32(pos, d, t1, t2, dir_flags);
 }
 
+/* FP64 march of the FP32 primary rays: the ray directions are generated
+ * exactly as the float path does (InitRayDir, RenderRect, AdjustDir in
+ * float), then promoted; the march itself runs in double.  This isolates
+ * the accuracy of the march arithmetic from ray generation. */
+int orc_brick_render_f64_f32ray(const uint32_t* grids, uint32_t ngrids,
+                                const float* density, const float* albedo,
+                                uint32_t nbricks, int levels, const float pos[3],
+                                const float dir0[3], const float du[3],
+                                const float dv[3], int width, int height,
+                                double alpha_scale, double step_vox, int y0,
+                                int y1, double* rgba, uint32_t* samples,
+                                uint32_t* bricks) {
+  brick_ctx_f64 c;
+  if (brick_ctx_init_f64(&c, grids, ngrids, density, albedo, nbricks, levels,
+                         alpha_scale, step_vox))
+    return 1;
+  if (y0 < 0) y0 = 0;
+  if (y1 > height) y1 = height;
+  double o[3] = {pos[0], pos[1], pos[2]};
+  for (int y = y0; y < y1; ++y)
+    for (int x = 0; x < width; ++x) {
+      size_t off = (size_t)y * (size_t)width + (size_t)x;
+      float df[3];
+      pixel_dir_f32(dir0, du, dv, x, y, df);
+      adjust_dir_f32(df);
+      double d[3] = {df[0], df[1], df[2]};
+      double out[4];
+      uint32_t ns = 0, nbk = 0;
+      int st = brick_march_f64(&c, o, d, out, &ns, &nbk, 0, 0);
+      if (st) return st;
+      if (rgba)
+        for (int i = 0; i < 4; ++i) rgba[off * 4 + (size_t)i] = out[i];
+      if (samples) samples[off] = ns;
+      if (bricks) bricks[off] = nbk;
+    }
+  return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 /* FP64 adjoint of the brick march                                          */
 /* ------------------------------------------------------------------------ */

@@ -97,6 +97,15 @@ int orc_brick_render_f64(const uint32_t* grids, uint32_t ngrids,
                          const double dv[3], int width, int height,
                          double alpha_scale, double step_vox, int y0, int y1,
                          double* rgba, uint32_t* samples, uint32_t* bricks);
+/* FP64 march of the FP32-generated primary rays (float camera basis). */
+int orc_brick_render_f64_f32ray(const uint32_t* grids, uint32_t ngrids,
+                                const float* density, const float* albedo,
+                                uint32_t nbricks, int levels, const float pos[3],
+                                const float dir0[3], const float du[3],
+                                const float dv[3], int width, int height,
+                                double alpha_scale, double step_vox, int y0,
+                                int y1, double* rgba, uint32_t* samples,
+                                uint32_t* bricks);
 int orc_brick_render_f32(const uint32_t* grids, uint32_t ngrids,
                          const float* density, const float* albedo,
                          uint32_t nbricks, int levels, const float pos[3],

@@ -342,9 +342,9 @@ static int FN(brick_march)(FN(brick_ctx) * c, const REAL* o, const REAL* d,
       for (;; ++k) {
         REAL t = (REAL)k * c->dt;
         if (!(t < t_out)) break;
-        REAL l[3];
+        REAL l[3];  /* brick-local lattice coordinates */
         for (int i = 0; i < 3; ++i)
-          l[i] = (o[i] + t * d[i]) * c->S - (REAL)(8 * cell[i]);
+          l[i] = t * (d[i] * c->S) + (o[i] * c->S - (REAL)(8 * cell[i]));
         uint32_t idx[8];
         REAL w[8];
         FN(brick_corners)(l, (uint32_t)b * 729u, idx, w);

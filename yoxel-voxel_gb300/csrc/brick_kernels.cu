@@ -86,11 +86,11 @@ struct SampleCtx {
   float col[3];
 };
 
+// lx, ly, lz: brick-local lattice coordinates of the sample, in [0, 8].
 template <int P>
-__device__ __forceinline__ void eval_sample(const VolumeArgs& a, int b, const int* cell,
-                                            float qx, float qy, float qz, SampleCtx& s) {
-  float l[3] = {fsub(qx, (float)(8 * cell[0])), fsub(qy, (float)(8 * cell[1])),
-                fsub(qz, (float)(8 * cell[2]))};
+__device__ __forceinline__ void eval_sample(const VolumeArgs& a, int b, float lx, float ly,
+                                            float lz, SampleCtx& s) {
+  float l[3] = {lx, ly, lz};
   int i0[3];
   float f[3];
 #pragma unroll
@@ -214,13 +214,18 @@ __device__ __forceinline__ void march(const VolumeArgs& a, const uint32_t* sg, u
     }
     if (b >= 0) {
       ++r.bricks;
+      // Q - 8c is exact (8c is a multiple of ulp(Q)), so fma(t, D, Q - 8c)
+      // rounds the brick-local coordinate in [0, 8] once: the sample point
+      // is accurate to ulp(8) instead of ulp(|Q|).
+      const float L0 = fsub(Q[0], (float)(8 * cell[0]));
+      const float L1 = fsub(Q[1], (float)(8 * cell[1]));
+      const float L2 = fsub(Q[2], (float)(8 * cell[2]));
       int k = __float2int_ru(fmul(t_in, a.inv_dt));
       for (int it = 0; it < 1 << 16; ++it, ++k) {
         const float t = fmul((float)k, a.dt);
         if (!(t < t_out)) break;
         SampleCtx s;
-        eval_sample<P>(a, b, cell, ffma(t, D[0], Q[0]), ffma(t, D[1], Q[1]),
-                       ffma(t, D[2], Q[2]), s);
+        eval_sample<P>(a, b, ffma(t, D[0], L0), ffma(t, D[1], L1), ffma(t, D[2], L2), s);
         const float T = fsub(1.f, A);
         vis(s, T, A, C0, C1, C2);
         const float w = fmul(T, s.alpha);
