@@ -7,19 +7,22 @@
 // optional hard-shadow ray per hit, fused.
 //
 // Design (GB300):
-//  * persistent grid (SMs x resident blocks); each warp pops 8x4 pixel tiles
-//    from a global counter, so long rays never stall a whole block;
+//  * persistent grid (SMs x resident blocks).  Every lane runs its own small
+//    state machine (primary ray -> shadow ray -> idle) one traversal step per
+//    loop iteration; idle lanes of a warp are refilled together from a
+//    global ray counter (one atomic per refill), so a warp never waits for
+//    the slowest ray of a tile and the shadow rays of some lanes overlap the
+//    primary rays of others.  Consecutive ray ids map to 8x4 pixel tiles, so
+//    lanes refilled together trace neighbouring pixels;
 //  * node records are 32 B (one L2 sector) read with two 128-bit loads; the
 //    breadth-first first `smem_nodes` records (the top tree levels, touched
 //    by every ray) are staged once per block in shared memory;
-//  * the recursion of RecTrace becomes a loop with a per-level node-id stack
-//    in shared memory and a 3-bit-per-level child path in a register.  On a
-//    pop the parent's slab values are not stored: they are recomputed by
-//    replaying FindFirstChild/GoNext from the root along the path, which
-//    repeats the reference's float operations and so reproduces its values
-//    bit for bit (no FMA contraction: every operation is an explicit
-//    round-to-nearest intrinsic);
-//  * every loop is bounded: a ray that exceeds the iteration cap or the stack
+//  * the recursion of RecTrace becomes an explicit per-lane stack of
+//    (node id, child, slab box) frames, so a pop restores the parent's exact
+//    float values: every operation is an explicit round-to-nearest intrinsic
+//    (no FMA contraction), which keeps hit ids bit-identical to the FP32
+//    restatement of the reference;
+//  * every loop is bounded: a ray that exceeds the step cap or the stack
 //    depth stops, is reported as a miss and sets a status bit.
 #include <cuda_runtime.h>
 
@@ -31,7 +34,7 @@
 namespace yv {
 namespace {
 
-constexpr uint32_t kIterCap = 1u << 20;
+constexpr uint32_t kStepCap = 1u << 20;
 
 struct Box {
   float x1, y1, z1, x2, y2, z2;
@@ -85,17 +88,15 @@ __device__ __forceinline__ bool go_next(uint32_t& ch, Box& t) {
   return true;
 }
 
-__device__ __forceinline__ uint32_t sel_child(const uint4& a, const uint4& b,
-                                              uint32_t c) {
+__device__ __forceinline__ uint32_t sel_child(const uint4& a, const uint4& b, uint32_t c) {
   const uint4 v = (c & 4u) ? b : a;
   const uint32_t lo = (c & 1u) ? v.y : v.x;
   const uint32_t hi = (c & 1u) ? v.w : v.z;
   return (c & 2u) ? hi : lo;
 }
 
-__device__ __forceinline__ void fetch_node(const SvoDeviceScene& sc,
-                                           const uint4* sm, uint32_t nsm,
-                                           uint32_t id, uint4& a, uint4& b) {
+__device__ __forceinline__ void fetch_node(const SvoDeviceScene& sc, const uint4* sm,
+                                           uint32_t nsm, uint32_t id, uint4& a, uint4& b) {
   if (id < nsm) {
     a = sm[2 * id];
     b = sm[2 * id + 1];
@@ -106,31 +107,32 @@ __device__ __forceinline__ void fetch_node(const SvoDeviceScene& sc,
   }
 }
 
-__device__ __forceinline__ uint64_t set_path(uint64_t path, int level,
-                                             uint32_t ch) {
-  const int sh = 3 * level;
-  return (path & ~(7ull << sh)) | ((uint64_t)ch << sh);
-}
-
-struct HitRec {
-  uint32_t node;   // device node index
-  uint32_t child;  // reference child index (ch ^ dirFlags)
-  uint32_t leaf;   // VoxData (attribute index)
-  uint32_t dir_flags;
-  int level;
-  float t;
-  Box box;         // leaf box (t1, t2)
+// One stack frame: the node of a level, the child taken and that child's
+// slab box, exactly as RecTrace holds them in its activation record.
+struct __align__(16) Frame {
+  uint32_t idch;  // node << 3 | ch
+  float x1, y1, z1;
+  float x2, y2, z2;
+  uint32_t pad;
 };
 
-// AdjustDir + SetupTrace + RecTrace for one ray.  kCull: also skip leaves
-// lying entirely behind the origin (shadow rays start inside the scene).
-template <bool kCull>
-__device__ bool svo_trace(const SvoDeviceScene& sc, const uint4* sm,
-                          uint32_t nsm, uint32_t* stk, uint32_t stride,
-                          float px, float py, float pz, float dx, float dy,
-                          float dz, HitRec& hr, uint32_t& fetches,
-                          uint32_t& err) {
-  // SetupTrace: octant mirroring (reaction/report/voxel.tex:312-326)
+enum : uint32_t { kIdle = 0, kPrimary = 1, kShadow = 2, kDone = 3 };
+enum : int { kContinue = 0, kHit = 1, kMiss = 2 };
+
+// Traversal state of one lane.
+struct Trace {
+  uint32_t node, ch, df, steps, fetches;
+  int level;
+  Box t;
+  uint4 na, nb;
+};
+
+// SetupTrace (reaction/report/voxel.tex:312-326) + RecTrace entry test
+// (cell/ppu_renderer.cpp:20-21) + the root fetch.  False: the ray misses.
+__device__ __forceinline__ bool begin_trace(const SvoDeviceScene& sc, const uint4* sm,
+                                            uint32_t nsm, float px, float py, float pz,
+                                            float dx, float dy, float dz, Trace& tr,
+                                            uint32_t& err) {
   uint32_t df = 0;
   if (dx < 0.f) { px = __fsub_rn(1.f, px); dx = -dx; df |= 1u; }
   if (dy < 0.f) { py = __fsub_rn(1.f, py); dy = -dy; df |= 2u; }
@@ -142,95 +144,85 @@ __device__ bool svo_trace(const SvoDeviceScene& sc, const uint4* sm,
   R.y2 = __fdiv_rn(__fsub_rn(1.f, py), dy);
   R.z1 = __fdiv_rn(__fsub_rn(0.f, pz), dz);
   R.z2 = __fdiv_rn(__fsub_rn(1.f, pz), dz);
+  tr.fetches = 0;
   if (!(max3f(R.x1, R.y1, R.z1) < min3f(R.x2, R.y2, R.z2))) return false;
-  uint32_t node = sc.root_word;
-  // RecTrace entry test (cell/ppu_renderer.cpp:20-21)
-  if ((node & (YV_DW_NULL | YV_DW_LEAF)) || min3f(R.x2, R.y2, R.z2) <= 0.f)
-    return false;
-  if (node >= sc.n_nodes) {
+  const uint32_t root = sc.root_word;
+  if ((root & (YV_DW_NULL | YV_DW_LEAF)) || min3f(R.x2, R.y2, R.z2) <= 0.f) return false;
+  if (root >= sc.n_nodes) {
     err |= YV_DEV_ERR_POOL;
     return false;
   }
-  uint4 na, nb;
-  fetch_node(sc, sm, nsm, node, na, nb);
-  ++fetches;
-  Box t = R;
-  uint32_t ch = ffc(t);
-  uint64_t path = ch;
-  int level = 0;
-  for (uint32_t it = 0;; ++it) {
-    if (it >= kIterCap) {
-      err |= YV_DEV_ERR_ITER;
-      return false;
-    }
-    const uint32_t c = ch ^ df;
-    const uint32_t w = sel_child(na, nb, c);
-    if (w & YV_DW_LEAF) {
-      if (!kCull || min3f(t.x2, t.y2, t.z2) > 0.f) {
-        hr.node = node;
-        hr.child = c;
-        hr.leaf = w & 0x7FFFFFFFu;
-        hr.dir_flags = df;
-        hr.level = level;
-        hr.t = max3f(t.x1, t.y1, t.z1);
-        hr.box = t;
-        return true;
-      }
-    } else if (!(w & YV_DW_NULL) && min3f(t.x2, t.y2, t.z2) > 0.f) {
-      // descend (the recursive call of cell/ppu_renderer.cpp:34)
-      if (level + 1 >= YV_MAX_DEPTH) {
-        err |= YV_DEV_ERR_DEPTH;
-        return false;
-      }
-      if (w >= sc.n_nodes) {
-        err |= YV_DEV_ERR_POOL;
-        return false;
-      }
-      stk[level * stride] = node;
-      ++level;
-      node = w;
-      fetch_node(sc, sm, nsm, node, na, nb);
-      ++fetches;
-      ch = ffc(t);
-      path = set_path(path, level, ch);
-      continue;
-    }
-    if (go_next(ch, t)) {
-      path = set_path(path, level, ch);
-      continue;
-    }
-    // Pop: find the deepest ancestor level whose GoNext succeeds, replaying
-    // the exact slab arithmetic from the root along the recorded path.
-    int best = -1;
-    Box bb = R;
-    uint32_t bch = 0;
-    Box r = R;
-    for (int lv = 0; lv < level; ++lv) {
-      const uint32_t tgt = (uint32_t)(path >> (3 * lv)) & 7u;
-      uint32_t cc = ffc(r);
-#pragma unroll 1
-      for (int k = 0; k < 3 && cc != tgt; ++k) go_next(cc, r);
-      Box q = r;
-      uint32_t qc = tgt;
-      if (go_next(qc, q)) {
-        best = lv;
-        bb = q;
-        bch = qc;
-      }
-    }
-    if (best < 0) return false;
-    level = best;
-    node = stk[level * stride];
-    fetch_node(sc, sm, nsm, node, na, nb);
-    t = bb;
-    ch = bch;
-    path = set_path(path, level, ch);
+  tr.node = root;
+  tr.df = df;
+  tr.level = 0;
+  tr.steps = 0;
+  tr.fetches = 1;
+  fetch_node(sc, sm, nsm, root, tr.na, tr.nb);
+  tr.t = R;
+  tr.ch = ffc(tr.t);
+  return true;
+}
+
+// One step of RecTrace: test the current child (leaf -> hit, subtree ->
+// descend), else move to the next sibling, popping finished levels.
+template <bool kCull>
+__device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint4* sm,
+                                          uint32_t nsm, Frame* stk, Trace& tr, uint32_t& leaf,
+                                          uint32_t& err) {
+  if (++tr.steps > kStepCap) {
+    err |= YV_DEV_ERR_ITER;
+    return kMiss;
   }
+  const uint32_t c = tr.ch ^ tr.df;
+  const uint32_t w = sel_child(tr.na, tr.nb, c);
+  if (w & YV_DW_LEAF) {
+    if (!kCull || min3f(tr.t.x2, tr.t.y2, tr.t.z2) > 0.f) {
+      leaf = w & 0x7FFFFFFFu;
+      return kHit;
+    }
+  } else if (!(w & YV_DW_NULL) && min3f(tr.t.x2, tr.t.y2, tr.t.z2) > 0.f) {
+    // descend: the recursive call of cell/ppu_renderer.cpp:34
+    if (tr.level + 1 >= YV_MAX_DEPTH) {
+      err |= YV_DEV_ERR_DEPTH;
+      return kMiss;
+    }
+    if (w >= sc.n_nodes) {
+      err |= YV_DEV_ERR_POOL;
+      return kMiss;
+    }
+    Frame f;
+    f.idch = (tr.node << 3) | tr.ch;
+    f.x1 = tr.t.x1; f.y1 = tr.t.y1; f.z1 = tr.t.z1;
+    f.x2 = tr.t.x2; f.y2 = tr.t.y2; f.z2 = tr.t.z2;
+    f.pad = 0;
+    stk[tr.level] = f;
+    ++tr.level;
+    tr.node = w;
+    fetch_node(sc, sm, nsm, w, tr.na, tr.nb);
+    ++tr.fetches;
+    tr.ch = ffc(tr.t);
+    return kContinue;
+  }
+  if (go_next(tr.ch, tr.t)) return kContinue;
+  // this level is exhausted: return to the parents until one has a next child
+  while (tr.level > 0) {
+    --tr.level;
+    const Frame f = stk[tr.level];
+    tr.ch = f.idch & 7u;
+    tr.t.x1 = f.x1; tr.t.y1 = f.y1; tr.t.z1 = f.z1;
+    tr.t.x2 = f.x2; tr.t.y2 = f.y2; tr.t.z2 = f.z2;
+    if (go_next(tr.ch, tr.t)) {
+      tr.node = f.idch >> 3;
+      fetch_node(sc, sm, nsm, tr.node, tr.na, tr.nb);
+      return kContinue;
+    }
+  }
+  return kMiss;
 }
 
 // Per-pixel ray direction (cell/ppu_renderer.cpp:56) + AdjustDir (eps 1e-5).
-__device__ __forceinline__ void pixel_dir(const SvoFrameArgs& a, int x, int y,
-                                          float& dx, float& dy, float& dz) {
+__device__ __forceinline__ void pixel_dir(const SvoFrameArgs& a, int x, int y, float& dx,
+                                          float& dy, float& dz) {
   const float fx = (float)x, fy = (float)y;
   dx = __fadd_rn(__fadd_rn(a.dir0[0], __fmul_rn(a.du[0], fx)), __fmul_rn(a.dv[0], fy));
   dy = __fadd_rn(__fadd_rn(a.dir0[1], __fmul_rn(a.du[1], fx)), __fmul_rn(a.dv[1], fy));
@@ -247,8 +239,7 @@ __device__ __forceinline__ void pixel_dir(const SvoFrameArgs& a, int x, int y,
 }
 
 // Lambert: ambient + diffuse*max(0, n.L) (ambient only in shadow).
-__device__ __forceinline__ uint32_t shade(uint2 at, const SvoFrameArgs& a,
-                                          bool shadowed) {
+__device__ __forceinline__ uint32_t shade(uint2 at, const SvoFrameArgs& a, bool shadowed) {
   const float nx = (float)(int8_t)(at.y & 0xFFu);
   const float ny = (float)(int8_t)((at.y >> 8) & 0xFFu);
   const float nz = (float)(int8_t)((at.y >> 16) & 0xFFu);
@@ -273,84 +264,134 @@ __device__ __forceinline__ uint32_t shade(uint2 at, const SvoFrameArgs& a,
   return out;
 }
 
-__global__ void __launch_bounds__(256) svo_frame_kernel(SvoDeviceScene sc,
-                                                        SvoFrameArgs a,
-                                                        uint32_t nsm) {
+__device__ __forceinline__ void write_pixel(const SvoFrameArgs& a, uint32_t off, uint32_t rgba,
+                                            uint32_t hitw, float ht, uint32_t f, uint32_t fs) {
+  if (a.rgba) a.rgba[off] = rgba;
+  if (a.hit) a.hit[off] = hitw;
+  if (a.hit_t) a.hit_t[off] = ht;
+  if (a.fetches) a.fetches[off] = f;
+  if (a.shadow_fetches) a.shadow_fetches[off] = fs;
+}
+
+__global__ void __launch_bounds__(256) svo_frame_kernel(SvoDeviceScene sc, SvoFrameArgs a,
+                                                        uint32_t nsm, uint32_t refill_min) {
   extern __shared__ uint4 smem[];
-  uint4* snodes = smem;
-  uint32_t* sstack = reinterpret_cast<uint32_t*>(smem + 2 * nsm);
-  for (uint32_t i = threadIdx.x; i < 2 * nsm; i += blockDim.x)
-    snodes[i] = __ldg(sc.nodes + i);
+  for (uint32_t i = threadIdx.x; i < 2 * nsm; i += blockDim.x) smem[i] = __ldg(sc.nodes + i);
   __syncthreads();
 
+  Frame stk[YV_MAX_DEPTH];
   const uint32_t lane = threadIdx.x & 31u;
-  uint32_t* stk = sstack + threadIdx.x;
-  const uint32_t stride = blockDim.x;
-  const int tiles_x = (a.width + 7) >> 3;
-  const int n_tiles = tiles_x * ((a.height + 3) >> 2);
-  uint32_t err = 0;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  const uint32_t tiles_x = (uint32_t)((a.width + 7) >> 3);
+  const uint32_t n_ids = tiles_x * (uint32_t)((a.height + 3) >> 2) * 32u;
+  uint32_t err = 0, my_hits = 0, my_shadowed = 0;
+
+  uint32_t mode = kIdle, off = 0;
+  Trace tr;
+  float dx = 0.f, dy = 0.f, dz = 0.f;
+  uint32_t hitw = 0xFFFFFFFFu, fp = 0;
+  float ht = 0.f;
+  uint2 attr = make_uint2(0u, 0u);
 
   for (;;) {
-    uint32_t tile = 0;
-    if (lane == 0) tile = atomicAdd(&a.counters[0], 1u);
-    tile = __shfl_sync(0xFFFFFFFFu, tile, 0);
-    if (tile >= (uint32_t)n_tiles) break;
-    const int x = (int)(tile % (uint32_t)tiles_x) * 8 + (int)(lane & 7u);
-    const int y = (int)(tile / (uint32_t)tiles_x) * 4 + (int)(lane >> 3);
-    const bool valid = x < a.width && y < a.height;
-    bool hit = false, shadowed = false;
-    if (valid) {
-      float dx, dy, dz;
-      pixel_dir(a, x, y, dx, dy, dz);
-      HitRec hr;
-      uint32_t f = 0, fs = 0;
-      hit = svo_trace<false>(sc, snodes, nsm, stk, stride, a.pos[0], a.pos[1],
-                             a.pos[2], dx, dy, dz, hr, f, err);
-      uint32_t rgba = 0, hw = 0xFFFFFFFFu;
-      float ht = 0.f;
-      if (hit) {
-        hw = (__ldg(sc.orig_id + hr.node) << 3) | hr.child;
-        ht = hr.t;
-        uint2 at = make_uint2(0u, 0u);
-        if (hr.leaf < sc.n_attrs)
-          at = __ldg(sc.attrs + hr.leaf);
-        else
-          err |= YV_DEV_ERR_POOL;
-        if (a.shadows) {
-          // hit point, moved half a leaf out through the entry face
-          float o[3];
-          o[0] = __fadd_rn(a.pos[0], __fmul_rn(dx, ht));
-          o[1] = __fadd_rn(a.pos[1], __fmul_rn(dy, ht));
-          o[2] = __fadd_rn(a.pos[2], __fmul_rn(dz, ht));
-          int e = 0;
-          float m = hr.box.x1;
-          if (hr.box.y1 > m) { e = 1; m = hr.box.y1; }
-          if (hr.box.z1 > m) { e = 2; }
-          const float half = __int_as_float((127 - (hr.level + 2)) << 23);
-          const float off = ((hr.dir_flags >> e) & 1u) ? half : -half;
-          o[e] = __fadd_rn(o[e], off);
-          HitRec hs;
-          shadowed = svo_trace<true>(sc, snodes, nsm, stk, stride, o[0], o[1],
-                                     o[2], a.light_ray[0], a.light_ray[1],
-                                     a.light_ray[2], hs, fs, err);
+    // ---- refill idle lanes from the global ray counter ----
+    const uint32_t idle = __ballot_sync(0xFFFFFFFFu, mode == kIdle);
+    const uint32_t busy = __ballot_sync(0xFFFFFFFFu, mode == kPrimary || mode == kShadow);
+    if (idle && (__popc(idle) >= (int)refill_min || busy == 0)) {
+      const uint32_t leader = (uint32_t)__ffs(idle) - 1u;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(&a.counters[0], (uint32_t)__popc(idle));
+      base = __shfl_sync(0xFFFFFFFFu, base, (int)leader);
+      if (mode == kIdle) {
+        const uint32_t id = base + (uint32_t)__popc(idle & lt_mask);
+        if (id >= n_ids) {
+          mode = kDone;
+        } else {
+          const uint32_t tile = id >> 5, w = id & 31u;
+          const int x = (int)((tile % tiles_x) * 8u + (w & 7u));
+          const int y = (int)((tile / tiles_x) * 4u + (w >> 3));
+          if (x < a.width && y < a.height) {
+            off = (uint32_t)y * (uint32_t)a.width + (uint32_t)x;
+            pixel_dir(a, x, y, dx, dy, dz);
+            if (begin_trace(sc, smem, nsm, a.pos[0], a.pos[1], a.pos[2], dx, dy, dz, tr, err)) {
+              mode = kPrimary;
+            } else {
+              write_pixel(a, off, 0u, 0xFFFFFFFFu, 0.f, tr.fetches, 0u);
+            }
+          }
         }
-        rgba = shade(at, a, shadowed);
       }
-      const size_t off = (size_t)y * (size_t)a.width + (size_t)x;
-      if (a.rgba) a.rgba[off] = rgba;
-      if (a.hit) a.hit[off] = hw;
-      if (a.hit_t) a.hit_t[off] = ht;
-      if (a.fetches) a.fetches[off] = f;
-      if (a.shadow_fetches) a.shadow_fetches[off] = fs;
     }
-    const uint32_t hm = __ballot_sync(0xFFFFFFFFu, hit);
-    const uint32_t sm_ = __ballot_sync(0xFFFFFFFFu, shadowed);
-    if (lane == 0 && hm) {
-      atomicAdd(&a.counters[2], (uint32_t)__popc(hm));
-      if (sm_) atomicAdd(&a.counters[3], (uint32_t)__popc(sm_));
+    if (__all_sync(0xFFFFFFFFu, mode == kDone)) break;
+    if (mode != kPrimary && mode != kShadow) continue;
+
+    // ---- one traversal step ----
+    uint32_t leaf = 0;
+    const int r = mode == kPrimary
+                      ? trace_step<false>(sc, smem, nsm, stk, tr, leaf, err)
+                      : trace_step<true>(sc, smem, nsm, stk, tr, leaf, err);
+    if (r == kContinue) continue;
+    if (mode == kPrimary) {
+      if (r == kMiss) {
+        write_pixel(a, off, 0u, 0xFFFFFFFFu, 0.f, tr.fetches, 0u);
+        mode = kIdle;
+        continue;
+      }
+      ++my_hits;
+      hitw = (__ldg(sc.orig_id + tr.node) << 3) | (tr.ch ^ tr.df);
+      ht = max3f(tr.t.x1, tr.t.y1, tr.t.z1);
+      fp = tr.fetches;
+      attr = make_uint2(0u, 0u);
+      if (leaf < sc.n_attrs)
+        attr = __ldg(sc.attrs + leaf);
+      else
+        err |= YV_DEV_ERR_POOL;
+      if (!a.shadows) {
+        write_pixel(a, off, shade(attr, a, false), hitw, ht, fp, 0u);
+        mode = kIdle;
+        continue;
+      }
+      // shadow ray: the hit point moved half a leaf out through the entry face
+      float o[3];
+      o[0] = __fadd_rn(a.pos[0], __fmul_rn(dx, ht));
+      o[1] = __fadd_rn(a.pos[1], __fmul_rn(dy, ht));
+      o[2] = __fadd_rn(a.pos[2], __fmul_rn(dz, ht));
+      int e = 0;
+      float m = tr.t.x1;
+      if (tr.t.y1 > m) { e = 1; m = tr.t.y1; }
+      if (tr.t.z1 > m) e = 2;
+      const float half = __int_as_float((127 - (tr.level + 2)) << 23);
+      const float d_off = ((tr.df >> e) & 1u) ? half : -half;
+      o[e] = __fadd_rn(o[e], d_off);
+      if (begin_trace(sc, smem, nsm, o[0], o[1], o[2], a.light_ray[0], a.light_ray[1],
+                      a.light_ray[2], tr, err)) {
+        mode = kShadow;
+      } else {
+        write_pixel(a, off, shade(attr, a, false), hitw, ht, fp, tr.fetches);
+        mode = kIdle;
+      }
+      continue;
     }
+    // end of a shadow ray
+    const bool sh = r == kHit;
+    my_shadowed += sh ? 1u : 0u;
+    write_pixel(a, off, shade(attr, a, sh), hitw, ht, fp, tr.fetches);
+    mode = kIdle;
   }
-  if (err) atomicOr(&a.counters[1], err);
+
+  // block totals of the counters, one atomic per block and counter
+  __shared__ uint32_t red[3];
+  if (threadIdx.x < 3) red[threadIdx.x] = 0;
+  __syncthreads();
+  if (my_hits) atomicAdd(&red[0], my_hits);
+  if (my_shadowed) atomicAdd(&red[1], my_shadowed);
+  if (err) atomicOr(&red[2], err);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (red[0]) atomicAdd(&a.counters[2], red[0]);
+    if (red[1]) atomicAdd(&a.counters[3], red[1]);
+    if (red[2]) atomicOr(&a.counters[1], red[2]);
+  }
 }
 
 }  // namespace
@@ -369,14 +410,15 @@ int device_sm_count() {
 }
 
 cudaError_t launch_svo_frame(const SvoDeviceScene& sc, const SvoFrameArgs& a,
-                             const LaunchCfg& cfg, cudaStream_t stream,
-                             int* launches) {
+                             const LaunchCfg& cfg, cudaStream_t stream, int* launches) {
   int bt = cfg.block_threads;
   if (bt < 32 || bt > 256 || (bt & 31)) bt = 256;
   uint32_t nsm = (uint32_t)(cfg.smem_nodes < 0 ? 0 : cfg.smem_nodes);
   if (nsm > sc.n_nodes) nsm = sc.n_nodes;
   if (nsm > 4096) nsm = 4096;
-  const size_t smem = (size_t)nsm * 32u + (size_t)YV_MAX_DEPTH * (size_t)bt * 4u;
+  uint32_t refill = (uint32_t)(cfg.tile_rays <= 0 ? 16 : cfg.tile_rays);
+  if (refill > 32) refill = 32;
+  const size_t smem = (size_t)nsm * 32u;
   if (smem > 48u * 1024u) {
     static bool opted_in[64] = {false};
     int dev = 0;
@@ -399,7 +441,7 @@ cudaError_t launch_svo_frame(const SvoDeviceScene& sc, const SvoFrameArgs& a,
   const int grid = device_sm_count() * per_sm;
   cudaError_t e = cudaMemsetAsync(a.counters, 0, kSvoCounterWords * sizeof(uint32_t), stream);
   if (e != cudaSuccess) return e;
-  svo_frame_kernel<<<grid, bt, smem, stream>>>(sc, a, nsm);
+  svo_frame_kernel<<<grid, bt, smem, stream>>>(sc, a, nsm, refill);
   if (launches) *launches = 1;
   return cudaGetLastError();
 }
