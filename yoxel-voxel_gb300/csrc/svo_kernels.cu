@@ -17,12 +17,11 @@
 //  * node records are 32 B (one L2 sector) read with two 128-bit loads; the
 //    breadth-first first `smem_nodes` records (the top tree levels, touched
 //    by every ray) are staged once per block in shared memory;
-//  * the recursion of RecTrace becomes a per-lane node-id stack in shared
-//    memory plus 3-bit child / FindFirstChild records per level; a pop
-//    restores the parent's exact slab box from a register cache or rebuilds
-//    it from the root with the same float operations.  Every operation is an
-//    explicit round-to-nearest intrinsic (no FMA contraction), which keeps
-//    hit ids bit-identical to the FP32 restatement of the reference;
+//  * the recursion of RecTrace becomes an explicit per-lane stack of
+//    (node id, child, slab box) frames, so a pop restores the parent's exact
+//    float values: every operation is an explicit round-to-nearest intrinsic
+//    (no FMA contraction), which keeps hit ids bit-identical to the FP32
+//    restatement of the reference;
 //  * every loop is bounded: a ray that exceeds the step cap or the stack
 //    depth stops, is reported as a miss and sets a status bit.
 #include <cuda_runtime.h>
@@ -108,56 +107,32 @@ __device__ __forceinline__ void fetch_node(const SvoDeviceScene& sc, const uint4
   }
 }
 
+// One stack frame: the node of a level, the child taken and that child's
+// slab box, exactly as RecTrace holds them in its activation record.
+struct __align__(16) Frame {
+  uint32_t idch;  // node << 3 | ch
+  float x1, y1, z1;
+  float x2, y2, z2;
+  uint32_t pad;
+};
+
 enum : uint32_t { kIdle = 0, kPrimary = 1, kShadow = 2, kDone = 3 };
 enum : int { kContinue = 0, kHit = 1, kMiss = 2 };
 
-// Traversal state of one lane.  The recursion of RecTrace is kept as: the
-// node id of every level (shared-memory stack), and per level the child
-// taken and the children FindFirstChild chose (3 bits each, in pch / pffc).
-// A child's slab box at a level follows from its parent's box and these two
-// bit sets alone (per axis: below the midpoint, above it from
-// FindFirstChild, or above it after one GoNext step), so any ancestor's box
-// can be rebuilt exactly; the boxes of the two nearest ancestors are also
-// cached (c1, c2) so that most pops need no rebuild.
+// Traversal state of one lane.
 struct Trace {
   uint32_t node, ch, df, steps, fetches;
   int level;
-  Box t;       // current child's box
-  Box c1, c2;  // child box at level-1 / level-2 (entry boxes of the node / its parent)
-  uint32_t valid;  // bit 0: c1 valid, bit 1: c2 valid
-  uint64_t pch, pffc;
+  Box t;
   uint4 na, nb;
 };
-
-__device__ __forceinline__ uint64_t set3(uint64_t path, int level, uint32_t v) {
-  const int sh = 3 * level;
-  return (path & ~(7ull << sh)) | ((uint64_t)v << sh);
-}
-
-// Child box along one axis from the parent's (t1, t2): f = FindFirstChild
-// chose the upper half, c = the upper half is taken (by FindFirstChild or
-// by one GoNext step).  Same operations as ffc / go_next.
-__device__ __forceinline__ void axis_child(float& t1, float& t2, uint32_t f, uint32_t c) {
-  const float tm = __fmul_rn(0.5f, __fadd_rn(t1, t2));
-  const float gn = __fadd_rn(tm, __fsub_rn(tm, t1));
-  const float n1 = c ? tm : t1;
-  const float n2 = f ? t2 : (c ? gn : tm);
-  t1 = n1;
-  t2 = n2;
-}
-
-__device__ __forceinline__ void child_box(Box& b, uint32_t f, uint32_t c) {
-  axis_child(b.x1, b.x2, f & 1u, c & 1u);
-  axis_child(b.y1, b.y2, (f >> 1) & 1u, (c >> 1) & 1u);
-  axis_child(b.z1, b.z2, (f >> 2) & 1u, (c >> 2) & 1u);
-}
 
 // SetupTrace (reaction/report/voxel.tex:312-326) + RecTrace entry test
 // (cell/ppu_renderer.cpp:20-21) + the root fetch.  False: the ray misses.
 __device__ __forceinline__ bool begin_trace(const SvoDeviceScene& sc, const uint4* sm,
-                                            uint32_t nsm, float* sR, uint32_t stride, float px,
-                                            float py, float pz, float dx, float dy, float dz,
-                                            Trace& tr, uint32_t& err) {
+                                            uint32_t nsm, float px, float py, float pz,
+                                            float dx, float dy, float dz, Trace& tr,
+                                            uint32_t& err) {
   uint32_t df = 0;
   if (dx < 0.f) { px = __fsub_rn(1.f, px); dx = -dx; df |= 1u; }
   if (dy < 0.f) { py = __fsub_rn(1.f, py); dy = -dy; df |= 2u; }
@@ -183,17 +158,8 @@ __device__ __forceinline__ bool begin_trace(const SvoDeviceScene& sc, const uint
   tr.steps = 0;
   tr.fetches = 1;
   fetch_node(sc, sm, nsm, root, tr.na, tr.nb);
-  sR[0] = R.x1;
-  sR[stride] = R.y1;
-  sR[2 * stride] = R.z1;
-  sR[3 * stride] = R.x2;
-  sR[4 * stride] = R.y2;
-  sR[5 * stride] = R.z2;
   tr.t = R;
   tr.ch = ffc(tr.t);
-  tr.pch = tr.ch;
-  tr.pffc = tr.ch;
-  tr.valid = 0;
   return true;
 }
 
@@ -201,8 +167,7 @@ __device__ __forceinline__ bool begin_trace(const SvoDeviceScene& sc, const uint
 // descend), else move to the next sibling, popping finished levels.
 template <bool kCull>
 __device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint4* sm,
-                                          uint32_t nsm, uint32_t* sid, const float* sR,
-                                          uint32_t stride, Trace& tr, uint32_t& leaf,
+                                          uint32_t nsm, Frame* stk, Trace& tr, uint32_t& leaf,
                                           uint32_t& err) {
   if (++tr.steps > kStepCap) {
     err |= YV_DEV_ERR_ITER;
@@ -225,88 +190,34 @@ __device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint4*
       err |= YV_DEV_ERR_POOL;
       return kMiss;
     }
-    sid[tr.level * stride] = tr.node;
-    tr.c2 = tr.c1;
-    tr.c1 = tr.t;
-    tr.valid = ((tr.valid << 1) & 2u) | 1u;
+    Frame f;
+    f.idch = (tr.node << 3) | tr.ch;
+    f.x1 = tr.t.x1; f.y1 = tr.t.y1; f.z1 = tr.t.z1;
+    f.x2 = tr.t.x2; f.y2 = tr.t.y2; f.z2 = tr.t.z2;
+    f.pad = 0;
+    stk[tr.level] = f;
     ++tr.level;
     tr.node = w;
     fetch_node(sc, sm, nsm, w, tr.na, tr.nb);
     ++tr.fetches;
     tr.ch = ffc(tr.t);
-    tr.pch = set3(tr.pch, tr.level, tr.ch);
-    tr.pffc = set3(tr.pffc, tr.level, tr.ch);
     return kContinue;
   }
-  if (go_next(tr.ch, tr.t)) {
-    tr.pch = set3(tr.pch, tr.level, tr.ch);
-    return kContinue;
-  }
-  // This level is exhausted: resume the deepest ancestor that has a next
-  // child.  The parent and grandparent come from the cached boxes.
-  int limit = tr.level;  // ancestor levels [0, limit) not yet examined
-  if (tr.level >= 1 && (tr.valid & 1u)) {
-    Box q = tr.c1;
-    uint32_t qc = (uint32_t)(tr.pch >> (3 * (tr.level - 1))) & 7u;
-    if (go_next(qc, q)) {
-      --tr.level;
-      tr.t = q;
-      tr.ch = qc;
-      tr.c1 = tr.c2;
-      tr.valid >>= 1;
-      tr.node = sid[tr.level * stride];
+  if (go_next(tr.ch, tr.t)) return kContinue;
+  // this level is exhausted: return to the parents until one has a next child
+  while (tr.level > 0) {
+    --tr.level;
+    const Frame f = stk[tr.level];
+    tr.ch = f.idch & 7u;
+    tr.t.x1 = f.x1; tr.t.y1 = f.y1; tr.t.z1 = f.z1;
+    tr.t.x2 = f.x2; tr.t.y2 = f.y2; tr.t.z2 = f.z2;
+    if (go_next(tr.ch, tr.t)) {
+      tr.node = f.idch >> 3;
       fetch_node(sc, sm, nsm, tr.node, tr.na, tr.nb);
-      tr.pch = set3(tr.pch, tr.level, tr.ch);
       return kContinue;
     }
-    limit = tr.level - 1;
-    if (tr.level >= 2 && (tr.valid & 2u)) {
-      q = tr.c2;
-      qc = (uint32_t)(tr.pch >> (3 * (tr.level - 2))) & 7u;
-      if (go_next(qc, q)) {
-        tr.level -= 2;
-        tr.t = q;
-        tr.ch = qc;
-        tr.valid = 0;
-        tr.node = sid[tr.level * stride];
-        fetch_node(sc, sm, nsm, tr.node, tr.na, tr.nb);
-        tr.pch = set3(tr.pch, tr.level, tr.ch);
-        return kContinue;
-      }
-      limit = tr.level - 2;
-    }
   }
-  // rebuild the boxes of the remaining ancestors from the root
-  int best = -1;
-  Box r;
-  r.x1 = sR[0];
-  r.y1 = sR[stride];
-  r.z1 = sR[2 * stride];
-  r.x2 = sR[3 * stride];
-  r.y2 = sR[4 * stride];
-  r.z2 = sR[5 * stride];
-  Box bb = r;
-  uint32_t bch = 0;
-  for (int lv = 0; lv < limit; ++lv) {
-    const uint32_t cl = (uint32_t)(tr.pch >> (3 * lv)) & 7u;
-    child_box(r, (uint32_t)(tr.pffc >> (3 * lv)) & 7u, cl);
-    Box q = r;
-    uint32_t qc = cl;
-    if (go_next(qc, q)) {
-      best = lv;
-      bb = q;
-      bch = qc;
-    }
-  }
-  if (best < 0) return kMiss;
-  tr.level = best;
-  tr.t = bb;
-  tr.ch = bch;
-  tr.valid = 0;
-  tr.node = sid[best * stride];
-  fetch_node(sc, sm, nsm, tr.node, tr.na, tr.nb);
-  tr.pch = set3(tr.pch, best, bch);
-  return kContinue;
+  return kMiss;
 }
 
 // Per-pixel ray direction (cell/ppu_renderer.cpp:56) + AdjustDir (eps 1e-5).
@@ -369,11 +280,9 @@ __global__ void __launch_bounds__(256, kMinBlocks)
     svo_frame_kernel(SvoDeviceScene sc, SvoFrameArgs a, uint32_t nsm, uint32_t refill_min) {
   extern __shared__ uint4 smem[];
   for (uint32_t i = threadIdx.x; i < 2 * nsm; i += blockDim.x) smem[i] = __ldg(sc.nodes + i);
-  uint32_t* sid = reinterpret_cast<uint32_t*>(smem + 2 * nsm) + threadIdx.x;
-  const uint32_t stride = blockDim.x;
-  float* sR = reinterpret_cast<float*>(smem + 2 * nsm) + (size_t)YV_MAX_DEPTH * stride + threadIdx.x;
   __syncthreads();
 
+  Frame stk[YV_MAX_DEPTH];
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t lt_mask = (1u << lane) - 1u;
   const uint32_t tiles_x = (uint32_t)((a.width + 7) >> 3);
@@ -407,8 +316,7 @@ __global__ void __launch_bounds__(256, kMinBlocks)
           if (x < a.width && y < a.height) {
             off = (uint32_t)y * (uint32_t)a.width + (uint32_t)x;
             pixel_dir(a, x, y, dx, dy, dz);
-            if (begin_trace(sc, smem, nsm, sR, stride, a.pos[0], a.pos[1], a.pos[2], dx, dy, dz, tr,
-                            err)) {
+            if (begin_trace(sc, smem, nsm, a.pos[0], a.pos[1], a.pos[2], dx, dy, dz, tr, err)) {
               mode = kPrimary;
             } else {
               write_pixel(a, off, 0u, 0xFFFFFFFFu, 0.f, tr.fetches, 0u);
@@ -423,8 +331,8 @@ __global__ void __launch_bounds__(256, kMinBlocks)
     // ---- one traversal step ----
     uint32_t leaf = 0;
     const int r = mode == kPrimary
-                      ? trace_step<false>(sc, smem, nsm, sid, sR, stride, tr, leaf, err)
-                      : trace_step<true>(sc, smem, nsm, sid, sR, stride, tr, leaf, err);
+                      ? trace_step<false>(sc, smem, nsm, stk, tr, leaf, err)
+                      : trace_step<true>(sc, smem, nsm, stk, tr, leaf, err);
     if (r == kContinue) continue;
     if (mode == kPrimary) {
       if (r == kMiss) {
@@ -458,8 +366,8 @@ __global__ void __launch_bounds__(256, kMinBlocks)
       const float half = __int_as_float((127 - (tr.level + 2)) << 23);
       const float d_off = ((tr.df >> e) & 1u) ? half : -half;
       o[e] = __fadd_rn(o[e], d_off);
-      if (begin_trace(sc, smem, nsm, sR, stride, o[0], o[1], o[2], a.light_ray[0],
-                      a.light_ray[1], a.light_ray[2], tr, err)) {
+      if (begin_trace(sc, smem, nsm, o[0], o[1], o[2], a.light_ray[0], a.light_ray[1],
+                      a.light_ray[2], tr, err)) {
         mode = kShadow;
       } else {
         write_pixel(a, off, shade(attr, a, false), hitw, ht, fp, tr.fetches);
@@ -508,8 +416,7 @@ template <int kMinBlocks>
 static cudaError_t launch_with(const SvoDeviceScene& sc, const SvoFrameArgs& a, int bt,
                                uint32_t nsm, uint32_t refill, int per_sm, cudaStream_t stream) {
   auto kern = svo_frame_kernel<kMinBlocks>;
-  const size_t smem = (size_t)nsm * 32u + (size_t)YV_MAX_DEPTH * (size_t)bt * 4u +
-                      6u * (size_t)bt * 4u;
+  const size_t smem = (size_t)nsm * 32u;
   if (smem > 48u * 1024u) {
     static bool opted_in[64] = {false};
     int dev = 0;
@@ -545,11 +452,11 @@ cudaError_t launch_svo_frame(const SvoDeviceScene& sc, const SvoFrameArgs& a,
   uint32_t nsm = (uint32_t)(cfg.smem_nodes < 0 ? 0 : cfg.smem_nodes);
   if (nsm > sc.n_nodes) nsm = sc.n_nodes;
   if (nsm > 4096) nsm = 4096;
-  uint32_t refill = (uint32_t)(cfg.tile_rays <= 0 ? 16 : cfg.tile_rays);
+  uint32_t refill = (uint32_t)(cfg.tile_rays <= 0 ? 32 : cfg.tile_rays);
   if (refill > 32) refill = 32;
   // register budget: blocks_per_sm 2 (up to 128 regs), 3 (80), 4 (64);
-  // 0 = default 3
-  const int mb = cfg.blocks_per_sm <= 0 ? 3 : (cfg.blocks_per_sm > 4 ? 4 : cfg.blocks_per_sm);
+  // 0 = default 4
+  const int mb = cfg.blocks_per_sm <= 0 ? 4 : (cfg.blocks_per_sm > 4 ? 4 : cfg.blocks_per_sm);
   cudaError_t e;
   if (mb <= 2)
     e = launch_with<2>(sc, a, bt, nsm, refill, 0, stream);
