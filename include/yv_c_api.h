@@ -321,6 +321,34 @@ yv_status yv_volume_fold_aprons(const yv_volume_device* vol,
 yv_status yv_volume_sync_aprons(const yv_volume_device* vol, float* density,
                                 float* albedo, void* stream);
 
+/* ------------------------------------------------------------------------ */
+/* Allocation-free frame (no counterpart in the reference)                  */
+/* ------------------------------------------------------------------------ */
+/* For callers that cannot call cudaMalloc: code running while a stream is
+ * captured into a CUDA graph, real-time loops that cannot take the device
+ * synchronisation an allocation may cost, and hosts whose device memory is
+ * owned by another allocator.  Renders one frame of an SVO that the caller
+ * holds in DEVICE memory in the reference layout (nodes: count VoxNode
+ * records, attrs: nattrs leaf attributes) into the caller's device outputs,
+ * with the same results as yv_render_frame_async (hit ids are the pool's own
+ * node indices).  Nothing is allocated: the frame's scratch (ray-queue
+ * counter, status word, hit counters) is a 256-byte static device array that
+ * every GPU loading the library keeps until exit.  The first call on a
+ * device looks up that array's address (cudaGetSymbolAddress); make it
+ * before any stream capture.  Every call shares the array and clears it on
+ * `stream` first, so calls that overlap on the GPU (other streams, other
+ * threads) race and must be serialised by the caller.  Asynchronous: returns
+ * launch errors only; malformed pools are contained by the kernel's bounds
+ * checks (validate the host copy with yv_svo_validate).  Frames needing more
+ * than 2^31 rays (8x4-tile padded) or pools over 2^29 nodes return
+ * YV_ERR_INVALID_ARG. */
+yv_status yv_render_svo_noalloc(const yv_vox_node* nodes, uint32_t count,
+                                uint32_t root, const yv_leaf_attr* attrs,
+                                uint32_t nattrs, const yv_camera* cam,
+                                const yv_light* light, int32_t width,
+                                int32_t height, const yv_frame_outputs* out,
+                                void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,422 @@
+// svo_trace.cuh - device code of the sparse-voxel-octree first-hit ray cast
+// for sm_103a (included by svo_kernels.cu and svo_noalloc.cu).
+//
+// One persistent kernel per frame: ray generation (RendererBase::InitRayDir /
+// RenderRect, cell/renderer_base.h:50-61, cell/ppu_renderer.cpp:43-70),
+// octree descent (RecTrace, cell/ppu_renderer.cpp:18-41, with FindFirstChild
+// and GoNext of cell/spu/trace_spu.cpp:48-93), Lambert shading and an
+// optional hard-shadow ray per hit, fused.
+//
+// Design (GB300):
+//  * persistent grid (SMs x resident blocks).  Every lane runs its own small
+//    state machine (primary ray -> shadow ray -> idle) one traversal step per
+//    loop iteration; idle lanes of a warp are refilled together from a
+//    global ray counter (one atomic per refill), so a warp never waits for
+//    the slowest ray of a tile and the shadow rays of some lanes overlap the
+//    primary rays of others.  Consecutive ray ids map to 8x4 pixel tiles, so
+//    lanes refilled together trace neighbouring pixels;
+//  * node records are 32 B (one L2 sector) read with two 128-bit loads; the
+//    breadth-first first `smem_nodes` records (the top tree levels, touched
+//    by every ray) are staged once per block in shared memory;
+//  * the recursion of RecTrace becomes an explicit per-lane stack of
+//    (node id, child, slab box) frames, so a pop restores the parent's exact
+//    float values: every operation is an explicit round-to-nearest intrinsic
+//    (no FMA contraction), which keeps hit ids bit-identical to the FP32
+//    restatement of the reference;
+//  * every loop is bounded: a ray that exceeds the step cap or the stack
+//    depth stops, is reported as a miss and sets a status bit.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "yv_internal.h"
+#include "yv_kernels.h"
+
+namespace yv {
+namespace {
+
+constexpr uint32_t kStepCap = 1u << 20;
+
+struct Box {
+  float x1, y1, z1, x2, y2, z2;
+};
+
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float m = a > b ? a : b;  // max_vec_float3 order
+  return m > c ? m : c;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float m = a < b ? a : b;
+  return m < c ? m : c;
+}
+
+// FindFirstChild (cell/spu/trace_spu.cpp:48-68).
+__device__ __forceinline__ uint32_t ffc(Box& t) {
+  const float te = max3f(t.x1, t.y1, t.z1);
+  uint32_t ch = 0;
+  float tm = __fmul_rn(0.5f, __fadd_rn(t.x1, t.x2));
+  if (te > tm) { ch |= 1u; t.x1 = tm; } else { t.x2 = tm; }
+  tm = __fmul_rn(0.5f, __fadd_rn(t.y1, t.y2));
+  if (te > tm) { ch |= 2u; t.y1 = tm; } else { t.y2 = tm; }
+  tm = __fmul_rn(0.5f, __fadd_rn(t.z1, t.z2));
+  if (te > tm) { ch |= 4u; t.z1 = tm; } else { t.z2 = tm; }
+  return ch;
+}
+
+// GoNext (cell/spu/trace_spu.cpp:70-93), argmin tie order of :75-78.
+__device__ __forceinline__ bool go_next(uint32_t& ch, Box& t) {
+  int e;
+  if (t.x2 > t.y2)
+    e = (t.y2 < t.z2) ? 1 : 2;
+  else
+    e = (t.x2 < t.z2) ? 0 : 2;
+  const uint32_t mask = 1u << e;
+  if (ch & mask) return false;
+  ch ^= mask;
+  if (e == 0) {
+    const float dt = __fsub_rn(t.x2, t.x1);
+    t.x1 = t.x2;
+    t.x2 = __fadd_rn(t.x2, dt);
+  } else if (e == 1) {
+    const float dt = __fsub_rn(t.y2, t.y1);
+    t.y1 = t.y2;
+    t.y2 = __fadd_rn(t.y2, dt);
+  } else {
+    const float dt = __fsub_rn(t.z2, t.z1);
+    t.z1 = t.z2;
+    t.z2 = __fadd_rn(t.z2, dt);
+  }
+  return true;
+}
+
+__device__ __forceinline__ uint32_t sel_child(const uint4& a, const uint4& b, uint32_t c) {
+  const uint4 v = (c & 4u) ? b : a;
+  const uint32_t lo = (c & 1u) ? v.y : v.x;
+  const uint32_t hi = (c & 1u) ? v.w : v.z;
+  return (c & 2u) ? hi : lo;
+}
+
+// Node fetch.  kRef = false: the library's 32-byte device records (two
+// 128-bit loads, top levels from shared memory).  kRef = true: the
+// reference's 40-byte VoxNode {flags, data, child[8]} read in place (five
+// 64-bit loads), its leaf / null flags folded into the same child words.
+template <bool kRef>
+__device__ __forceinline__ void fetch_node(const SvoDeviceScene& sc, const uint4* sm,
+                                           uint32_t nsm, uint32_t id, uint4& a, uint4& b) {
+  if (kRef) {
+    const uint2* p = reinterpret_cast<const uint2*>(sc.nodes) + 5 * (size_t)id;
+    const uint2 q0 = __ldg(p), q1 = __ldg(p + 1), q2 = __ldg(p + 2), q3 = __ldg(p + 3),
+                q4 = __ldg(p + 4);
+    const uint32_t fl = q0.x;
+    uint32_t c[8] = {q1.x, q1.y, q2.x, q2.y, q3.x, q3.y, q4.x, q4.y};
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+      c[i] = ((fl >> i) & 1u) ? (YV_DW_LEAF | c[i]) : ((c[i] & 0x80000000u) ? YV_DW_NULL : c[i]);
+    a = make_uint4(c[0], c[1], c[2], c[3]);
+    b = make_uint4(c[4], c[5], c[6], c[7]);
+  } else if (id < nsm) {
+    a = sm[2 * id];
+    b = sm[2 * id + 1];
+  } else {
+    const uint4* p = sc.nodes + 2 * (size_t)id;
+    a = __ldg(p);
+    b = __ldg(p + 1);
+  }
+}
+
+// One stack frame: the node of a level, the child taken and that child's
+// slab box, exactly as RecTrace holds them in its activation record.
+struct __align__(16) Frame {
+  uint32_t idch;  // node << 3 | ch
+  float x1, y1, z1;
+  float x2, y2, z2;
+  uint32_t pad;
+};
+
+enum : uint32_t { kIdle = 0, kPrimary = 1, kShadow = 2, kDone = 3 };
+enum : int { kContinue = 0, kHit = 1, kMiss = 2 };
+
+// Traversal state of one lane.
+struct Trace {
+  uint32_t node, ch, df, steps, fetches;
+  int level;
+  Box t;
+  uint4 na, nb;
+};
+
+// SetupTrace (reaction/report/voxel.tex:312-326) + RecTrace entry test
+// (cell/ppu_renderer.cpp:20-21) + the root fetch.  False: the ray misses.
+template <bool kRef>
+__device__ __forceinline__ bool begin_trace(const SvoDeviceScene& sc, const uint4* sm,
+                                            uint32_t nsm, float px, float py, float pz,
+                                            float dx, float dy, float dz, Trace& tr,
+                                            uint32_t& err) {
+  uint32_t df = 0;
+  if (dx < 0.f) { px = __fsub_rn(1.f, px); dx = -dx; df |= 1u; }
+  if (dy < 0.f) { py = __fsub_rn(1.f, py); dy = -dy; df |= 2u; }
+  if (dz < 0.f) { pz = __fsub_rn(1.f, pz); dz = -dz; df |= 4u; }
+  Box R;
+  R.x1 = __fdiv_rn(__fsub_rn(0.f, px), dx);
+  R.x2 = __fdiv_rn(__fsub_rn(1.f, px), dx);
+  R.y1 = __fdiv_rn(__fsub_rn(0.f, py), dy);
+  R.y2 = __fdiv_rn(__fsub_rn(1.f, py), dy);
+  R.z1 = __fdiv_rn(__fsub_rn(0.f, pz), dz);
+  R.z2 = __fdiv_rn(__fsub_rn(1.f, pz), dz);
+  tr.fetches = 0;
+  if (!(max3f(R.x1, R.y1, R.z1) < min3f(R.x2, R.y2, R.z2))) return false;
+  const uint32_t root = sc.root_word;
+  if ((root & (YV_DW_NULL | YV_DW_LEAF)) || min3f(R.x2, R.y2, R.z2) <= 0.f) return false;
+  if (root >= sc.n_nodes) {
+    err |= YV_DEV_ERR_POOL;
+    return false;
+  }
+  tr.node = root;
+  tr.df = df;
+  tr.level = 0;
+  tr.steps = 0;
+  tr.fetches = 1;
+  fetch_node<kRef>(sc, sm, nsm, root, tr.na, tr.nb);
+  tr.t = R;
+  tr.ch = ffc(tr.t);
+  return true;
+}
+
+// One step of RecTrace: test the current child (leaf -> hit, subtree ->
+// descend), else move to the next sibling, popping finished levels.
+template <bool kCull, bool kRef>
+__device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint4* sm,
+                                          uint32_t nsm, Frame* stk, Trace& tr, uint32_t& leaf,
+                                          uint32_t& err) {
+  if (++tr.steps > kStepCap) {
+    err |= YV_DEV_ERR_ITER;
+    return kMiss;
+  }
+  const uint32_t c = tr.ch ^ tr.df;
+  const uint32_t w = sel_child(tr.na, tr.nb, c);
+  if (w & YV_DW_LEAF) {
+    if (!kCull || min3f(tr.t.x2, tr.t.y2, tr.t.z2) > 0.f) {
+      leaf = w & 0x7FFFFFFFu;
+      return kHit;
+    }
+  } else if (!(w & YV_DW_NULL) && min3f(tr.t.x2, tr.t.y2, tr.t.z2) > 0.f) {
+    // descend: the recursive call of cell/ppu_renderer.cpp:34
+    if (tr.level + 1 >= YV_MAX_DEPTH) {
+      err |= YV_DEV_ERR_DEPTH;
+      return kMiss;
+    }
+    if (w >= sc.n_nodes) {
+      err |= YV_DEV_ERR_POOL;
+      return kMiss;
+    }
+    Frame f;
+    f.idch = (tr.node << 3) | tr.ch;
+    f.x1 = tr.t.x1; f.y1 = tr.t.y1; f.z1 = tr.t.z1;
+    f.x2 = tr.t.x2; f.y2 = tr.t.y2; f.z2 = tr.t.z2;
+    f.pad = 0;
+    stk[tr.level] = f;
+    ++tr.level;
+    tr.node = w;
+    fetch_node<kRef>(sc, sm, nsm, w, tr.na, tr.nb);
+    ++tr.fetches;
+    tr.ch = ffc(tr.t);
+    return kContinue;
+  }
+  if (go_next(tr.ch, tr.t)) return kContinue;
+  // this level is exhausted: return to the parents until one has a next child
+  while (tr.level > 0) {
+    --tr.level;
+    const Frame f = stk[tr.level];
+    tr.ch = f.idch & 7u;
+    tr.t.x1 = f.x1; tr.t.y1 = f.y1; tr.t.z1 = f.z1;
+    tr.t.x2 = f.x2; tr.t.y2 = f.y2; tr.t.z2 = f.z2;
+    if (go_next(tr.ch, tr.t)) {
+      tr.node = f.idch >> 3;
+      fetch_node<kRef>(sc, sm, nsm, tr.node, tr.na, tr.nb);
+      return kContinue;
+    }
+  }
+  return kMiss;
+}
+
+// Per-pixel ray direction (cell/ppu_renderer.cpp:56) + AdjustDir (eps 1e-5).
+__device__ __forceinline__ void pixel_dir(const SvoFrameArgs& a, int x, int y, float& dx,
+                                          float& dy, float& dz) {
+  const float fx = (float)x, fy = (float)y;
+  dx = __fadd_rn(__fadd_rn(a.dir0[0], __fmul_rn(a.du[0], fx)), __fmul_rn(a.dv[0], fy));
+  dy = __fadd_rn(__fadd_rn(a.dir0[1], __fmul_rn(a.du[1], fx)), __fmul_rn(a.dv[1], fy));
+  dz = __fadd_rn(__fadd_rn(a.dir0[2], __fmul_rn(a.du[2], fx)), __fmul_rn(a.dv[2], fy));
+  const float len = __fsqrt_rn(
+      __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+  dx = __fdiv_rn(dx, len);
+  dy = __fdiv_rn(dy, len);
+  dz = __fdiv_rn(dz, len);
+  const float eps = 1e-5f;
+  if (fabsf(dx) < eps) dx = copysignf(eps, dx);
+  if (fabsf(dy) < eps) dy = copysignf(eps, dy);
+  if (fabsf(dz) < eps) dz = copysignf(eps, dz);
+}
+
+// Lambert: ambient + diffuse*max(0, n.L) (ambient only in shadow).
+__device__ __forceinline__ uint32_t shade(uint2 at, const SvoFrameArgs& a, bool shadowed) {
+  const float nx = (float)(int8_t)(at.y & 0xFFu);
+  const float ny = (float)(int8_t)((at.y >> 8) & 0xFFu);
+  const float nz = (float)(int8_t)((at.y >> 16) & 0xFFu);
+  const float len2 =
+      __fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)), __fmul_rn(nz, nz));
+  float ndl = 0.f;
+  if (len2 > 0.f) {
+    const float len = __fsqrt_rn(len2);
+    const float ux = __fdiv_rn(nx, len), uy = __fdiv_rn(ny, len), uz = __fdiv_rn(nz, len);
+    ndl = __fadd_rn(__fadd_rn(__fmul_rn(ux, a.light[0]), __fmul_rn(uy, a.light[1])),
+                    __fmul_rn(uz, a.light[2]));
+  }
+  const float dif = ndl > 0.f ? ndl : 0.f;
+  const float inten = shadowed ? a.ambient : __fadd_rn(a.ambient, __fmul_rn(a.diffuse, dif));
+  uint32_t out = 0xFF000000u;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float v = __fadd_rn(__fmul_rn((float)((at.x >> (8 * c)) & 0xFFu), inten), 0.5f);
+    const uint32_t u = v >= 255.f ? 255u : __float2uint_rz(v);
+    out |= u << (8 * c);
+  }
+  return out;
+}
+
+__device__ __forceinline__ void write_pixel(const SvoFrameArgs& a, uint32_t off, uint32_t rgba,
+                                            uint32_t hitw, float ht, uint32_t f, uint32_t fs) {
+  if (a.rgba) a.rgba[off] = rgba;
+  if (a.hit) a.hit[off] = hitw;
+  if (a.hit_t) a.hit_t[off] = ht;
+  if (a.fetches) a.fetches[off] = f;
+  if (a.shadow_fetches) a.shadow_fetches[off] = fs;
+}
+
+// kMinBlocks: resident 256-thread blocks per SM the register allocation is
+// sized for (the occupancy / register-spill trade-off is autotuned).
+// kRef: the node pool is the reference VoxNode layout (hit ids are then the
+// pool's own node indices); otherwise the library's device layout.
+template <int kMinBlocks, bool kRef>
+__global__ void __launch_bounds__(256, kMinBlocks)
+    svo_frame_kernel(SvoDeviceScene sc, SvoFrameArgs a, uint32_t nsm, uint32_t refill_min) {
+  extern __shared__ uint4 smem[];
+  for (uint32_t i = threadIdx.x; i < 2 * nsm; i += blockDim.x) smem[i] = __ldg(sc.nodes + i);
+  __syncthreads();
+
+  Frame stk[YV_MAX_DEPTH];
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  const uint32_t tiles_x = (uint32_t)((a.width + 7) >> 3);
+  const uint32_t n_ids = tiles_x * (uint32_t)((a.height + 3) >> 2) * 32u;
+  uint32_t err = 0, my_hits = 0, my_shadowed = 0;
+
+  uint32_t mode = kIdle, off = 0;
+  Trace tr;
+  float dx = 0.f, dy = 0.f, dz = 0.f;
+  uint32_t hitw = 0xFFFFFFFFu, fp = 0;
+  float ht = 0.f;
+  uint2 attr = make_uint2(0u, 0u);
+
+  for (;;) {
+    // ---- refill idle lanes from the global ray counter ----
+    const uint32_t idle = __ballot_sync(0xFFFFFFFFu, mode == kIdle);
+    const uint32_t busy = __ballot_sync(0xFFFFFFFFu, mode == kPrimary || mode == kShadow);
+    if (idle && (__popc(idle) >= (int)refill_min || busy == 0)) {
+      const uint32_t leader = (uint32_t)__ffs(idle) - 1u;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(&a.counters[0], (uint32_t)__popc(idle));
+      base = __shfl_sync(0xFFFFFFFFu, base, (int)leader);
+      if (mode == kIdle) {
+        const uint32_t id = base + (uint32_t)__popc(idle & lt_mask);
+        if (id >= n_ids) {
+          mode = kDone;
+        } else {
+          const uint32_t tile = id >> 5, w = id & 31u;
+          const int x = (int)((tile % tiles_x) * 8u + (w & 7u));
+          const int y = (int)((tile / tiles_x) * 4u + (w >> 3));
+          if (x < a.width && y < a.height) {
+            off = (uint32_t)y * (uint32_t)a.width + (uint32_t)x;
+            pixel_dir(a, x, y, dx, dy, dz);
+            if (begin_trace<kRef>(sc, smem, nsm, a.pos[0], a.pos[1], a.pos[2], dx, dy, dz, tr, err)) {
+              mode = kPrimary;
+            } else {
+              write_pixel(a, off, 0u, 0xFFFFFFFFu, 0.f, tr.fetches, 0u);
+            }
+          }
+        }
+      }
+    }
+    if (__all_sync(0xFFFFFFFFu, mode == kDone)) break;
+    if (mode != kPrimary && mode != kShadow) continue;
+
+    // ---- one traversal step ----
+    uint32_t leaf = 0;
+    const int r = mode == kPrimary
+                      ? trace_step<false, kRef>(sc, smem, nsm, stk, tr, leaf, err)
+                      : trace_step<true, kRef>(sc, smem, nsm, stk, tr, leaf, err);
+    if (r == kContinue) continue;
+    if (mode == kPrimary) {
+      if (r == kMiss) {
+        write_pixel(a, off, 0u, 0xFFFFFFFFu, 0.f, tr.fetches, 0u);
+        mode = kIdle;
+        continue;
+      }
+      ++my_hits;
+      hitw = ((kRef ? tr.node : __ldg(sc.orig_id + tr.node)) << 3) | (tr.ch ^ tr.df);
+      ht = max3f(tr.t.x1, tr.t.y1, tr.t.z1);
+      fp = tr.fetches;
+      attr = make_uint2(0u, 0u);
+      if (leaf < sc.n_attrs)
+        attr = __ldg(sc.attrs + leaf);
+      else
+        err |= YV_DEV_ERR_POOL;
+      if (!a.shadows) {
+        write_pixel(a, off, shade(attr, a, false), hitw, ht, fp, 0u);
+        mode = kIdle;
+        continue;
+      }
+      // shadow ray: the hit point moved half a leaf out through the entry face
+      float o[3];
+      o[0] = __fadd_rn(a.pos[0], __fmul_rn(dx, ht));
+      o[1] = __fadd_rn(a.pos[1], __fmul_rn(dy, ht));
+      o[2] = __fadd_rn(a.pos[2], __fmul_rn(dz, ht));
+      int e = 0;
+      float m = tr.t.x1;
+      if (tr.t.y1 > m) { e = 1; m = tr.t.y1; }
+      if (tr.t.z1 > m) e = 2;
+      const float half = __int_as_float((127 - (tr.level + 2)) << 23);
+      const float d_off = ((tr.df >> e) & 1u) ? half : -half;
+      o[e] = __fadd_rn(o[e], d_off);
+      if (begin_trace<kRef>(sc, smem, nsm, o[0], o[1], o[2], a.light_ray[0], a.light_ray[1],
+                      a.light_ray[2], tr, err)) {
+        mode = kShadow;
+      } else {
+        write_pixel(a, off, shade(attr, a, false), hitw, ht, fp, tr.fetches);
+        mode = kIdle;
+      }
+      continue;
+    }
+    // end of a shadow ray
+    const bool sh = r == kHit;
+    my_shadowed += sh ? 1u : 0u;
+    write_pixel(a, off, shade(attr, a, sh), hitw, ht, fp, tr.fetches);
+    mode = kIdle;
+  }
+
+  // block totals of the counters, one atomic per block and counter
+  __shared__ uint32_t red[3];
+  if (threadIdx.x < 3) red[threadIdx.x] = 0;
+  __syncthreads();
+  if (my_hits) atomicAdd(&red[0], my_hits);
+  if (my_shadowed) atomicAdd(&red[1], my_shadowed);
+  if (err) atomicOr(&red[2], err);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (red[0]) atomicAdd(&a.counters[2], red[0]);
+    if (red[1]) atomicAdd(&a.counters[3], red[1]);
+    if (red[2]) atomicOr(&a.counters[1], red[2]);
+  }
+}
+
+}  // namespace
+}  // namespace yv

@@ -147,6 +147,8 @@ _SIGS = {
                                C.c_int32, C.c_int32, C.POINTER(MarchParams), P, P, P, P, P]),
     "yv_volume_fold_aprons": (S, [C.POINTER(VolumeDevice), P, P, P]),
     "yv_volume_sync_aprons": (S, [C.POINTER(VolumeDevice), P, P, P]),
+    "yv_render_svo_noalloc": (S, [P, U32, U32, P, U32, C.POINTER(Camera), C.POINTER(Light),
+                                  C.c_int32, C.c_int32, C.POINTER(FrameOutputs), P]),
 }
 
 
