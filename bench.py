@@ -54,6 +54,21 @@ CONFIGS = {
                  workload="2048^3 (SVO depth 11) seeded 6-octave value-noise terrain + 10k "
                           "floating cubes, 1920x1080 FP32 primary rays + 1 hard-shadow ray "
                           "per hit"),
+    "cfg3": dict(kind="brick", levels=3, width=1024, height=1024, alpha_scale=1.0,
+                 step_vox=0.5,
+                 workload="N=4 brick tree, 3 grid levels + 8^3 bricks = 512^3, fp16 density "
+                          "(4-octave noise - 0.4, empty bricks culled, ~20% occupancy) + uint8 "
+                          "RGB albedo, 1024x1024 rays, 0.5-voxel steps, trilinear, "
+                          "front-to-back, early exit at T<0.01"),
+    "cfg4": dict(kind="train", levels=2, cams=64, width=256, height=256, alpha_scale=1.0,
+                 step_vox=0.5,
+                 workload="differentiable 128^3 brick volume (fp32 density + fp32 RGB albedo), "
+                          "64 cameras on a sphere at 256x256, L2 loss to images of the volume "
+                          "+ N(0,0.1) noise; forward + re-marching adjoint (value = fwd+bwd)"),
+    "cfg5": dict(kind="batch", n=32,
+                 workload="32 seeded scenes (cfg1-type SVO or cfg3-type fp16 bricks), depth "
+                          "6..11, resolution 128^2..1024^2, one persistent launch from a global "
+                          "ray queue replayed from a CUDA graph (value) vs 32 per-scene launches"),
 }
 
 
@@ -173,15 +188,36 @@ def run_reference(args, cfg):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    scene = make_scene(cfg)
+    if cfg["kind"] not in ("svo", "brick"):
+        print(json.dumps({"impl": "reference", "unavailable":
+                          f"{args.config}: the reference has no CPU form of this workload"}))
+        return
     # each step: the same view at half the resolution per axis (1/4 of rays)
     w, h = cfg["width"] // 2, cfg["height"] // 2
+    if cfg["kind"] == "svo":
+        scene = make_scene(cfg)
+        step = lambda: cpu_svo(cfg, scene, w, h, threads)
+    else:
+        import yoxel
+        from oracle import pyoracle
+        vol = yoxel.BrickVolume.noise(cfg["levels"], 0.4, 1.4, 1234)
+        den = vol.density.astype(np.float16).astype(np.float32)
+        alb = vol.albedo_u8.astype(np.float32) * np.float32(1.0 / 255.0)
+        pos, view = camera()
+
+        def step():
+            t0 = time.perf_counter()
+            pyoracle.brick_render_f32_mt(vol.grids, den, alb, vol.levels, pos, view, (0, 0, 1),
+                                         60.0, w, h, cfg["alpha_scale"], cfg["step_vox"],
+                                         threads=threads)
+            s = time.perf_counter() - t0
+            return w * h / s / 1e6, s, w * h
     for _ in range(args.warmup):
-        cpu_svo(cfg, scene, w, h, threads)
+        step()
     vals, secs = [], []
     rays = 0
     for _ in range(args.steps):
-        v, s, rays = cpu_svo(cfg, scene, w, h, threads)
+        v, s, rays = step()
         vals.append(v)
         secs.append(s)
     value = rays * len(secs) / sum(secs) / 1e6
@@ -357,6 +393,281 @@ def run_svo(args, cfg):
         pg.destroy_process_group()
 
 
+def _timed_steps(torch, steps, fn, flush=None, stream=None):
+    """Per-step CUDA-event times (ms) of fn(), flush() between steps outside
+    the events; bracketed by synchronize."""
+    stream = stream or torch.cuda.current_stream()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(steps)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(steps):
+        if flush is not None:
+            flush()
+        evs[i][0].record(stream)
+        fn()
+        evs[i][1].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    return [a.elapsed_time(b) for a, b in evs], wall
+
+
+def _base_line(args, cfg, value, ms, dtype):
+    ws, _, _ = dist_env()
+    return {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+            "data": "synthetic",
+            "config": {"workload": cfg["workload"], "config": args.config,
+                       "l2": "flushed between steps (256 MiB write)"}}
+
+
+def run_brick(args, cfg):
+    """cfg3: plain brick march, fp16 pool."""
+    import torch
+    import yoxel
+    from yoxel import workloads as W
+    torch.cuda.set_device(dist_env()[2])
+    t_scene = time.perf_counter()
+    vol = yoxel.BrickVolume.noise(cfg["levels"], 0.4, 1.4, 1234)
+    t_scene = time.perf_counter() - t_scene
+    gv = vol.upload(0)
+    desc = gv.desc()
+    pos, view = W.camera()
+    cam = [(pos, view, (0, 0, 1), 60.0)]
+    w, h = cfg["width"], cfg["height"]
+    rays = w * h
+    ns = torch.zeros((1, h, w), dtype=torch.int32, device="cuda")
+    nb = torch.zeros((1, h, w), dtype=torch.int32, device="cuda")
+    out = yoxel.render_volume(desc, cam, w, h, cfg["alpha_scale"], cfg["step_vox"],
+                              samples=ns, bricks=nb)
+    S, B = int(ns.to(torch.int64).sum()), int(nb.to(torch.int64).sum())
+    # 8 trilinear corners x (2 B fp16 density + 3 B RGB) per sample, 4 B per
+    # tree level per occupied brick entered, 16 B RGBA fp32 out
+    alg = 40 * S + 4 * cfg["levels"] * B + 16 * rays
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    fn = lambda: yoxel.render_volume(desc, cam, w, h, cfg["alpha_scale"], cfg["step_vox"],
+                                     out=out)
+    for _ in range(args.warmup):
+        flush.fill_(1)
+        fn()
+    sampler = ClockSampler(dist_env()[2])
+    sampler.start()
+    time.sleep(0.4)
+    ms, wall = _timed_steps(torch, args.steps, fn, lambda: flush.fill_(1))
+    clocks = sampler.stop()
+    mean_ms = sum(ms) / len(ms)
+    host = torch.empty((1, h, w, 4), dtype=torch.float32, pin_memory=True)
+    torch.cuda.synchronize()
+    te = time.perf_counter()
+    for _ in range(args.steps):
+        fn()
+        host.copy_(out)  # synchronous D2H into pinned memory
+    e2e_s = (time.perf_counter() - te) / args.steps
+    peaks, kind = measured_peaks()
+    achieved = alg / (mean_ms / 1e3) / 1e9
+    line = _base_line(args, cfg, rays / (mean_ms / 1e3) / 1e6, mean_ms, "f32 (fp16 storage)")
+    line["config"].update(volume_bricks=vol.nbricks, occupancy=round(vol.occupancy, 4),
+                          mean_samples_per_ray=round(S / rays, 2))
+    line.update({
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
+                     "traffic": profile_traffic("volume_forward_cfg3"), "peak_source": kind,
+                     "algorithmic_bytes_per_step": alg},
+        "e2e": {"value": round(rays / e2e_s / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": 40,
+                "d2h_bytes_per_step": rays * 16,
+                "path": "yoxel.render_volume + copy into pinned host memory"},
+        "gpu_launches": args.steps, "clocks": clocks, "wall_s_timed_region": round(wall, 4),
+        "scene_build_s": round(t_scene, 2)})
+    if not args.no_cpu_baseline:
+        from oracle import pyoracle
+        den = vol.density.astype(np.float16).astype(np.float32)
+        alb = vol.albedo_u8.astype(np.float32) * np.float32(1.0 / 255.0)
+        threads = os.cpu_count() or 1
+        sw, sh = w // 4, h // 4
+        t0, runs = time.perf_counter(), 0
+        while runs == 0 or (time.perf_counter() - t0 < 10.0 and runs < 50):
+            pyoracle.brick_render_f32_mt(vol.grids, den, alb, vol.levels, pos, view, (0, 0, 1),
+                                         60.0, sw, sh, cfg["alpha_scale"], cfg["step_vox"],
+                                         threads=threads)
+            runs += 1
+        v = sw * sh * runs / (time.perf_counter() - t0) / 1e6
+        line["cpu_baseline"] = {"value": round(v, 4), "unit": UNIT, "cores": threads,
+                                "kind": "port",
+                                "sample": f"{sw}x{sh} frame of the same volume and camera, "
+                                          f"repeated {runs}x; FP32 C restatement of "
+                                          "reaction/trace/trace.cu castRay over the ntree pool"}
+    print(json.dumps(line), flush=True)
+
+
+def run_train(args, cfg):
+    """cfg4: differentiable volume, forward + adjoint."""
+    import torch
+    import yoxel
+    torch.cuda.set_device(dist_env()[2])
+    vol = yoxel.BrickVolume.noise(cfg["levels"], 0.4, 1.4, 1234)
+    tv = vol.to_torch()
+    g = torch.Generator(device="cuda").manual_seed(1234)
+    # target volume: the first + N(0, 0.1), owners perturbed then aprons synced
+    tgt_d = (tv["density"] + 0.1 * torch.randn(tv["density"].shape, generator=g,
+                                               device="cuda")).clamp_(0, 1)
+    tgt_a = (tv["albedo"] + 0.1 * torch.randn(tv["albedo"].shape, generator=g,
+                                              device="cuda")).clamp_(0, 1)
+    import ctypes as C
+    from yoxel import _lib as L
+    L.check(L.lib.yv_volume_sync_aprons(C.byref(yoxel.torch_desc(tv, tgt_d, tgt_a)),
+                                        C.c_void_p(tgt_d.data_ptr()),
+                                        C.c_void_p(tgt_a.data_ptr()), None), "sync")
+    cams = yoxel.cameras(yoxel.sphere_cameras(cfg["cams"]))
+    w, h = cfg["width"], cfg["height"]
+    a_s, st = cfg["alpha_scale"], cfg["step_vox"]
+    target = yoxel.render_volume(yoxel.torch_desc(tv, tgt_d, tgt_a), cams, w, h, a_s, st)
+    rays = cfg["cams"] * w * h
+    density = tv["density"].clone().requires_grad_(True)
+    albedo = tv["albedo"].clone().requires_grad_(True)
+
+    def fwd_bwd():
+        density.grad = None
+        albedo.grad = None
+        rgba = yoxel.volume_march(density, albedo, tv, cams, w, h, a_s, st)
+        loss = ((rgba - target) ** 2).sum()
+        loss.backward()
+
+    fwd_out = torch.empty((cfg["cams"], h, w, 4), dtype=torch.float32, device="cuda")
+    desc = yoxel.torch_desc(tv, density.detach(), albedo.detach())
+
+    def fwd():
+        yoxel.render_volume(desc, cams, w, h, a_s, st, out=fwd_out)
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        fwd_bwd()
+        fwd()
+    ns = torch.zeros((cfg["cams"], h, w), dtype=torch.int32, device="cuda")
+    yoxel.render_volume(desc, cams, w, h, a_s, st, out=fwd_out, samples=ns)
+    S = int(ns.to(torch.int64).sum())
+    sampler = ClockSampler(dist_env()[2])
+    sampler.start()
+    time.sleep(0.4)
+    ms_fb, wall = _timed_steps(torch, args.steps, fwd_bwd, lambda: flush.fill_(1))
+    ms_f, _ = _timed_steps(torch, args.steps, fwd, lambda: flush.fill_(1))
+    # the adjoint kernel alone (dominant kernel of the step)
+    grad = torch.randn(fwd_out.shape, device="cuda")
+    gd = torch.zeros_like(tv["density"])
+    ga = torch.zeros_like(tv["albedo"])
+    ms_b, _ = _timed_steps(torch, args.steps,
+                           lambda: yoxel.volume_backward(desc, cams, w, h, fwd_out, grad, gd, ga,
+                                                         a_s, st, fold=False),
+                           lambda: flush.fill_(1))
+    clocks = sampler.stop()
+    fb = sum(ms_fb) / len(ms_fb)
+    f = sum(ms_f) / len(ms_f)
+    b = sum(ms_b) / len(ms_b)
+    peaks, kind = measured_peaks()
+    # adjoint bytes: replay of the fp32 forward reads (8 x (4 + 12) B per
+    # sample) + the same again as gradient atomics + 32 B/ray (rgba, dL/drgba)
+    alg_b = 2 * 128 * S + 32 * rays
+    achieved = alg_b / (b / 1e3) / 1e9
+    line = _base_line(args, cfg, rays / (fb / 1e3) / 1e6, fb, "f32")
+    line["config"].update(rays_per_step=rays, mean_samples_per_ray=round(S / rays, 2),
+                          bricks=vol.nbricks)
+    line.update({
+        "forward_mrays_s": round(rays / (f / 1e3) / 1e6, 3),
+        "fwd_bwd_over_fwd": round(f / fb, 4),
+        "backward_kernel_ms": round(b, 4),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
+                     "traffic": profile_traffic("volume_backward_cfg4"), "peak_source": kind,
+                     "kernel": "volume_backward_kernel", "algorithmic_bytes_per_launch": alg_b},
+        "gradient_check": "GPU adjoint vs FP64 adjoint / naive PyTorch marcher / FP64 central "
+                          "differences: rel. error <= 1e-4 (tests/test_volume_gpu.py)",
+        "gpu_launches": args.steps * 3, "clocks": clocks, "wall_s_timed_region": round(wall, 4)})
+    host = torch.empty((), dtype=torch.float32, pin_memory=True)
+    torch.cuda.synchronize()
+    te = time.perf_counter()
+    for _ in range(args.steps):
+        density.grad = None
+        albedo.grad = None
+        rgba = yoxel.volume_march(density, albedo, tv, cams, w, h, a_s, st)
+        loss = ((rgba - target) ** 2).sum()
+        loss.backward()
+        host.copy_(loss.detach())  # D2H of the step's loss
+    e2e = (time.perf_counter() - te) / args.steps
+    line["e2e"] = {"value": round(rays / e2e / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 4,
+                   "path": "yoxel.volume_march + L2 loss + backward, loss read on the host"}
+    print(json.dumps(line), flush=True)
+
+
+def run_batch(args, cfg):
+    """cfg5: batched persistent launch vs per-scene launches."""
+    import torch
+    import yoxel
+    from yoxel import autotune
+    from yoxel import workloads as W
+    torch.cuda.set_device(dist_env()[2])
+    specs = W.cfg5_specs(1234, cfg["n"])
+    batch = yoxel.Batch()
+    keep = []
+    t_scene = time.perf_counter()
+    rays = 0
+    for sp in specs:
+        res = sp["res"]
+        pos, view = W.camera(sp["cam_dir"])
+        if sp["kind"] == "svo":
+            s = W.spheres(sp["depth"], seed=sp["seed"])
+            r = yoxel.Renderer()
+            r.SetScene(s)
+            r.SetViewPos(pos)
+            r.SetViewDir(view)
+            r.SetResolution(res, res)
+            r.SetFOV(60.0)
+            r.SetLight(LIGHT, 0.15, 0.85, False)
+            out = torch.empty((res, res), dtype=torch.int32, device="cuda")
+            batch.add_svo(r, out)
+            keep += [r, out]
+            del s
+        else:
+            v = yoxel.BrickVolume.noise(W.brick_levels_for_depth(sp["depth"]), 0.4, 1.4,
+                                        sp["seed"])
+            gv = v.upload(0)
+            out = torch.empty((res, res, 4), dtype=torch.float32, device="cuda")
+            batch.add_volume(gv.desc(), (pos, view, (0, 0, 1), 60.0), res, res, out)
+            keep += [gv, out]
+            del v
+        rays += res * res
+    t_scene = time.perf_counter() - t_scene
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    best, _ = autotune.tune_batch(batch, f"cfg5-{cfg['n']}", reps=2,
+                                  flush=lambda: flush.fill_(1))
+    for _ in range(args.warmup):
+        batch.render(graph=True)
+        batch.render_separate()
+    sampler = ClockSampler(dist_env()[2])
+    sampler.start()
+    time.sleep(0.4)
+    ms_b, wall = _timed_steps(torch, args.steps, lambda: batch.render(graph=True),
+                              lambda: flush.fill_(1))
+    ms_s, _ = _timed_steps(torch, args.steps, batch.render_separate, lambda: flush.fill_(1))
+    ms_p, _ = _timed_steps(torch, args.steps, lambda: batch.render(graph=False),
+                           lambda: flush.fill_(1))
+    clocks = sampler.stop()
+    tb, ts, tp = (sum(x) / len(x) for x in (ms_b, ms_s, ms_p))
+    line = _base_line(args, cfg, rays / (tb / 1e3) / 1e6, tb, "f32")
+    line["config"].update(scenes=len(specs), rays_per_step=rays,
+                          svo_scenes=sum(1 for s in specs if s["kind"] == "svo"),
+                          launch_config=best)
+    line.update({
+        "separate_launches_mrays_s": round(rays / (ts / 1e3) / 1e6, 3),
+        "persistent_without_graph_mrays_s": round(rays / (tp / 1e3) / 1e6, 3),
+        "speedup_vs_separate": round(ts / tb, 3),
+        "gpu_launches": args.steps, "clocks": clocks, "wall_s_timed_region": round(wall, 4),
+        "scene_build_s": round(t_scene, 2),
+        "roofline": None,
+        "e2e": None})
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -378,6 +689,12 @@ def main():
         return run_reference(args, cfg)
     if cfg["kind"] == "svo":
         return run_svo(args, cfg)
+    if cfg["kind"] == "brick":
+        return run_brick(args, cfg)
+    if cfg["kind"] == "train":
+        return run_train(args, cfg)
+    if cfg["kind"] == "batch":
+        return run_batch(args, cfg)
     raise SystemExit(f"unknown workload kind {cfg['kind']}")
 
 

@@ -322,6 +322,34 @@ yv_status yv_volume_sync_aprons(const yv_volume_device* vol, float* density,
                                 float* albedo, void* stream);
 
 /* ------------------------------------------------------------------------ */
+/* Batched persistent render (no reference code; nearest structure is the   */
+/* SPU tile loop, cell/spu/trace_spu.cpp:162-177)                           */
+/* ------------------------------------------------------------------------ */
+/* Up to 64 scenes+cameras of uneven depth and resolution - SVO first-hit
+ * frames and brick-volume composites - traced in ONE persistent launch whose
+ * warps pop 8x4-pixel tiles from a global ray queue (largest scenes first).
+ * Per-ray results are bit-identical to the per-scene launches. */
+typedef struct yv_batch yv_batch;
+yv_status yv_batch_create(yv_batch** out);
+void      yv_batch_destroy(yv_batch* b);
+yv_status yv_batch_clear(yv_batch* b);
+/* Adds the renderer's current scene, camera, light and resolution (a
+ * snapshot; the renderer must outlive the batch); output: device RGBA8. */
+yv_status yv_batch_add_svo(yv_batch* b, const yv_renderer* r, void* d_rgba);
+/* Adds one camera of a device volume; output: device RGBA float4. */
+yv_status yv_batch_add_volume(yv_batch* b, const yv_volume_device* vol,
+                              const yv_camera* cam, int32_t width,
+                              int32_t height, const yv_march_params* mp,
+                              float* d_rgba);
+yv_status yv_batch_set_launch_config(yv_batch* b, const yv_launch_config* cfg);
+/* One persistent launch for the whole batch on `stream`; use_graph != 0
+ * replays a captured CUDA graph (re-captured after the batch changes). */
+yv_status yv_batch_render(yv_batch* b, int32_t use_graph, void* stream);
+/* The same work as one plain launch per scene (the batch's baseline). */
+yv_status yv_batch_render_separate(yv_batch* b, void* stream);
+yv_status yv_batch_info(const yv_batch* b, uint32_t* n_items, uint64_t* rays);
+
+/* ------------------------------------------------------------------------ */
 /* Allocation-free frame (no counterpart in the reference)                  */
 /* ------------------------------------------------------------------------ */
 /* For callers that cannot call cudaMalloc: code running while a stream is

@@ -9,6 +9,7 @@
 #include <new>
 #include <string>
 
+#include "yv_batch.h"
 #include "yv_internal.h"
 #include "yv_kernels.h"
 
@@ -252,9 +253,9 @@ yv_status yv_get_device_scene_info(const yv_renderer* r, uint64_t* nodes, uint64
   return YV_OK;
 }
 
-static yv_status enqueue_frame(yv_renderer* r, const yv_frame_outputs* out, cudaStream_t s) {
-  if (!r->has_scene) return YV_ERR_NO_SCENE;
-  SvoFrameArgs a;
+// Scene and frame parameters of a renderer as the kernels take them
+// (outputs and counters left null).
+static void fill_frame_args(const yv_renderer* r, SvoFrameArgs& a) {
   std::memset(&a, 0, sizeof(a));
   std::memcpy(a.pos, r->pos, sizeof(a.pos));
   init_ray_dir(r->dir, r->up, r->fov, r->width, r->height, a.dir0, a.du, a.dv);
@@ -266,6 +267,25 @@ static yv_status enqueue_frame(yv_renderer* r, const yv_frame_outputs* out, cuda
   a.shadows = r->light.shadows ? 1 : 0;
   a.width = r->width;
   a.height = r->height;
+}
+
+}  // extern "C"
+
+namespace yv {
+bool renderer_view(const yv_renderer* r, yv_renderer_view* v) {
+  if (!r || !r->has_scene) return false;
+  v->sc = r->scene;
+  fill_frame_args(r, v->fa);
+  return true;
+}
+}  // namespace yv
+
+extern "C" {
+
+static yv_status enqueue_frame(yv_renderer* r, const yv_frame_outputs* out, cudaStream_t s) {
+  if (!r->has_scene) return YV_ERR_NO_SCENE;
+  SvoFrameArgs a;
+  fill_frame_args(r, a);
   a.rgba = static_cast<uint32_t*>(out->rgba);
   a.hit = static_cast<uint32_t*>(out->hit);
   a.hit_t = static_cast<float*>(out->hit_t);

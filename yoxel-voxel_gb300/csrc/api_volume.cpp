@@ -60,21 +60,21 @@ bool fill_args(const yv_volume_device* v, const yv_march_params* mp, int width, 
       !(mp->step_vox > 0.f) || !std::isfinite(mp->alpha_scale))
     return false;
   std::memset(a, 0, sizeof(*a));
-  a->grids = v->grids;
-  a->ngrids = v->ngrids;
-  a->levels = v->levels;
-  a->nb = 1 << (2 * v->levels);
-  a->density = v->density;
-  a->albedo = v->albedo;
-  a->nbricks = v->nbricks;
-  a->precision = v->precision;
+  a->v.grids = v->grids;
+  a->v.ngrids = v->ngrids;
+  a->v.levels = v->levels;
+  a->v.nb = 1 << (2 * v->levels);
+  a->v.density = v->density;
+  a->v.albedo = v->albedo;
+  a->v.nbricks = v->nbricks;
+  a->v.precision = v->precision;
   a->nbr_up = v->nbr_up;
   a->nbr_dn = v->nbr_dn;
-  a->S = (float)(8 * a->nb);
-  a->cell_size = 8.0f / a->S;
-  a->alpha_scale = mp->alpha_scale;
-  a->dt = mp->step_vox / a->S;
-  a->inv_dt = a->S / mp->step_vox;
+  a->v.S = (float)(8 * a->v.nb);
+  a->v.cell_size = 8.0f / a->v.S;
+  a->v.alpha_scale = mp->alpha_scale;
+  a->v.dt = mp->step_vox / a->v.S;
+  a->v.inv_dt = a->v.S / mp->step_vox;
   a->width = width;
   a->height = height;
   return true;

@@ -1,0 +1,273 @@
+// brick_march.cuh - device code of the brick-volume ray-march (ntree layout)
+// for sm_103a, shared by brick_kernels.cu and batch_kernels.cu.
+//
+// March (restating castRay / walkBrick / intersect of
+// reaction/trace/trace.cu:42-139 over the N=4 grid tree of volume_host.cpp):
+//  * clip the ray to the unit cube, t_enter = max(t_enter, 0);
+//  * DDA over brick cells; cell c spans [t_in, t_out) with t_in = the
+//    previous cell's t_out, so cells partition the ray;
+//  * in an occupied cell, samples sit at the global multiples t = k*dt
+//    (trace.cu:47), dt = step_vox lattice cells;
+//  * sample = software FP32 trilinear of density and albedo inside the brick
+//    (the 9^3 apron lattice keeps all 8 corners in the brick);
+//  * alpha = saturate(alpha_scale * density), front-to-back pre-multiplied
+//    accumulation C += (1-A)*alpha*albedo, A += (1-A)*alpha (trace.cu:58),
+//    stop once A > 0.99 (trace.cu:59).
+// Every float operation of the march is an explicit round-to-nearest
+// intrinsic so the forward and the backward kernels replay bit-identical
+// values (the adjoint relies on reaching the forward's exact final colour).
+//
+// Adjoint: the backward kernel re-marches each ray instead of storing
+// per-sample state.  With T = 1 - A before sample j and the forward output
+// (C, A) of the ray:
+//   d out_k / d alpha_j = T c_jk - (out_k - out_k after j) / (1 - alpha_j)
+//   d out_k / d c_jk    = T alpha_j            (c_A = 1)
+// Gradients for the 8 trilinear corners are coalesced in registers while
+// consecutive samples of a ray stay in the same trilinear cell, then flushed
+// with FP32 atomics (red.global.add.f32).
+#pragma once
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "yv_volume.h"
+
+namespace yv {
+namespace {
+
+constexpr int kL = 9;
+constexpr int kL3 = 729;
+constexpr uint32_t kEmpty = 0x80000000u;
+constexpr uint32_t kBrick = 0x40000000u;
+constexpr int kSmemGrids = 65;  // root + up to 64 level-1 grid nodes
+
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float ffma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float lerpf_(float a, float b, float t) { return ffma(t, fsub(b, a), a); }
+
+template <int P>
+struct Voxel;
+
+// precision 0: fp16 density, uchar4 albedo
+template <>
+struct Voxel<0> {
+  __device__ static __forceinline__ float den(const void* p, uint32_t i) {
+    return __half2float(__ushort_as_half(__ldg(static_cast<const unsigned short*>(p) + i)));
+  }
+  __device__ static __forceinline__ void alb(const void* p, uint32_t i, float* c) {
+    const uint32_t v = __ldg(static_cast<const unsigned int*>(p) + i);
+    const float s = 1.0f / 255.0f;
+    c[0] = fmul((float)(v & 0xFFu), s);
+    c[1] = fmul((float)((v >> 8) & 0xFFu), s);
+    c[2] = fmul((float)((v >> 16) & 0xFFu), s);
+  }
+};
+
+// precision 1: fp32 density, fp32 RGB albedo (learnable)
+template <>
+struct Voxel<1> {
+  __device__ static __forceinline__ float den(const void* p, uint32_t i) {
+    return __ldg(static_cast<const float*>(p) + i);
+  }
+  __device__ static __forceinline__ void alb(const void* p, uint32_t i, float* c) {
+    const float* q = static_cast<const float*>(p) + 3 * (size_t)i;
+    c[0] = __ldg(q);
+    c[1] = __ldg(q + 1);
+    c[2] = __ldg(q + 2);
+  }
+};
+
+struct SampleCtx {
+  uint32_t base;  // brick*729 + corner-000 lattice index
+  float fx, fy, fz;
+  float sigma, alpha;
+  float col[3];
+};
+
+// lx, ly, lz: brick-local lattice coordinates of the sample, in [0, 8].
+template <int P>
+__device__ __forceinline__ void eval_sample(const VolumeView& a, int b, float lx, float ly,
+                                            float lz, SampleCtx& s) {
+  float l[3] = {lx, ly, lz};
+  int i0[3];
+  float f[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    int k = __float2int_rd(l[i]);
+    k = k < 0 ? 0 : (k > 7 ? 7 : k);
+    float fi = fsub(l[i], (float)k);
+    fi = fi < 0.f ? 0.f : (fi > 1.f ? 1.f : fi);
+    i0[i] = k;
+    f[i] = fi;
+  }
+  s.fx = f[0];
+  s.fy = f[1];
+  s.fz = f[2];
+  s.base = (uint32_t)b * (uint32_t)kL3 + (uint32_t)((i0[2] * kL + i0[1]) * kL + i0[0]);
+  float d[8];
+  float c[8][3];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const uint32_t idx = s.base + (uint32_t)(((j >> 2) * kL + ((j >> 1) & 1)) * kL + (j & 1));
+    d[j] = Voxel<P>::den(a.density, idx);
+    Voxel<P>::alb(a.albedo, idx, c[j]);
+  }
+  // lerp along x, then y, then z (corner j: bit0 x, bit1 y, bit2 z)
+  float dx0 = lerpf_(d[0], d[1], f[0]), dx1 = lerpf_(d[2], d[3], f[0]);
+  float dx2 = lerpf_(d[4], d[5], f[0]), dx3 = lerpf_(d[6], d[7], f[0]);
+  s.sigma = lerpf_(lerpf_(dx0, dx1, f[1]), lerpf_(dx2, dx3, f[1]), f[2]);
+#pragma unroll
+  for (int ch = 0; ch < 3; ++ch) {
+    float x0 = lerpf_(c[0][ch], c[1][ch], f[0]), x1 = lerpf_(c[2][ch], c[3][ch], f[0]);
+    float x2 = lerpf_(c[4][ch], c[5][ch], f[0]), x3 = lerpf_(c[6][ch], c[7][ch], f[0]);
+    s.col[ch] = lerpf_(lerpf_(x0, x1, f[1]), lerpf_(x2, x3, f[1]), f[2]);
+  }
+  float al = fmul(s.sigma, a.alpha_scale);
+  s.alpha = al < 0.f ? 0.f : (al > 1.f ? 1.f : al);
+}
+
+// Tree descent for brick cell `cell` (ntree/ntree/nodes.h:56-99 offsets).
+// Top grid nodes come from shared memory.  Returns brick id, -1 if empty,
+// -2 if the pool is malformed.
+__device__ __forceinline__ int lookup(const VolumeView& a, const uint32_t* sg, uint32_t nsg,
+                                      const int* cell) {
+  uint32_t node = 0;
+  for (int lev = 0; lev < a.levels; ++lev) {
+    const int sh = 2 * (a.levels - 1 - lev);
+    const uint32_t c = (uint32_t)((((cell[2] >> sh) & 3) * 4 + ((cell[1] >> sh) & 3)) * 4 +
+                                  ((cell[0] >> sh) & 3));
+    if (node >= a.ngrids) return -2;
+    const uint32_t ref = node < nsg ? sg[node * 64 + c] : __ldg(a.grids + (size_t)node * 64 + c);
+    if (ref & kEmpty) return -1;
+    if (ref & kBrick) {
+      const uint32_t b = ref & 0x3FFFFFFFu;
+      return (lev == a.levels - 1 && b < a.nbricks) ? (int)b : -2;
+    }
+    if (lev == a.levels - 1) return -2;
+    node = ref;
+  }
+  return -1;
+}
+
+struct RayOut {
+  float c[3];
+  float a;
+  uint32_t samples;
+  uint32_t bricks;
+  bool bad;
+};
+
+// One ray; `Vis` is called per sample with (sample, T, C before).
+template <int P, class Vis>
+__device__ __forceinline__ void march(const VolumeView& a, const uint32_t* sg, uint32_t nsg,
+                                      const float* o, const float* d, Vis& vis, RayOut& r) {
+  r.c[0] = r.c[1] = r.c[2] = 0.f;
+  r.a = 0.f;
+  r.samples = 0;
+  r.bricks = 0;
+  r.bad = false;
+  float inv[3], t1[3], t2[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    inv[i] = __fdiv_rn(1.f, d[i]);
+    const float lo = fmul(fsub(0.f, o[i]), inv[i]);
+    const float hi = fmul(fsub(1.f, o[i]), inv[i]);
+    t1[i] = lo < hi ? lo : hi;
+    t2[i] = lo < hi ? hi : lo;
+  }
+  float t_enter = fmaxf(fmaxf(t1[0], t1[1]), t1[2]);
+  const float t_exit = fminf(fminf(t2[0], t2[1]), t2[2]);
+  if (t_enter < 0.f) t_enter = 0.f;
+  if (t_exit < 0.f || t_enter > t_exit) return;
+  const float h = a.cell_size;  // world size of a brick cell
+  int cell[3], step[3];
+  float Q[3], D[3];  // lattice-space origin and direction
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float q = __fdiv_rn(fadd(o[i], fmul(t_enter, d[i])), h);
+    int k = __float2int_rd(q);
+    k = k < 0 ? 0 : (k > a.nb - 1 ? a.nb - 1 : k);
+    cell[i] = k;
+    step[i] = d[i] > 0.f ? 1 : -1;
+    Q[i] = fmul(o[i], a.S);
+    D[i] = fmul(d[i], a.S);
+  }
+  float t_in = t_enter;
+  float A = 0.f, C0 = 0.f, C1 = 0.f, C2 = 0.f;
+  for (int guard = 0; guard < 4 * 4096; ++guard) {
+    float tx[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const float plane = fmul((float)(d[i] > 0.f ? cell[i] + 1 : cell[i]), h);
+      tx[i] = fmul(fsub(plane, o[i]), inv[i]);
+    }
+    int e = 0;
+    if (tx[1] < tx[e]) e = 1;
+    if (tx[2] < tx[e]) e = 2;
+    const float t_out = tx[e];
+    const int b = lookup(a, sg, nsg, cell);
+    if (b == -2) {
+      r.bad = true;
+      break;
+    }
+    if (b >= 0) {
+      ++r.bricks;
+      // Q - 8c is exact (8c is a multiple of ulp(Q)), so fma(t, D, Q - 8c)
+      // rounds the brick-local coordinate in [0, 8] once: the sample point
+      // is accurate to ulp(8) instead of ulp(|Q|).
+      const float L0 = fsub(Q[0], (float)(8 * cell[0]));
+      const float L1 = fsub(Q[1], (float)(8 * cell[1]));
+      const float L2 = fsub(Q[2], (float)(8 * cell[2]));
+      int k = __float2int_ru(fmul(t_in, a.inv_dt));
+      for (int it = 0; it < 1 << 16; ++it, ++k) {
+        const float t = fmul((float)k, a.dt);
+        if (!(t < t_out)) break;
+        SampleCtx s;
+        eval_sample<P>(a, b, ffma(t, D[0], L0), ffma(t, D[1], L1), ffma(t, D[2], L2), s);
+        const float T = fsub(1.f, A);
+        vis(s, T, A, C0, C1, C2);
+        const float w = fmul(T, s.alpha);
+        C0 = ffma(w, s.col[0], C0);
+        C1 = ffma(w, s.col[1], C1);
+        C2 = ffma(w, s.col[2], C2);
+        A = fadd(A, w);
+        ++r.samples;
+        if (A > 0.99f) goto done;
+      }
+    }
+    t_in = t_out;
+    cell[e] += step[e];
+    if (cell[e] < 0 || cell[e] >= a.nb) break;
+  }
+done:
+  r.c[0] = C0;
+  r.c[1] = C1;
+  r.c[2] = C2;
+  r.a = A;
+}
+
+struct NoVis {
+  __device__ __forceinline__ void operator()(const SampleCtx&, float, float, float, float,
+                                             float) {}
+};
+
+__device__ __forceinline__ void pixel_ray(const CamBasis& c, int x, int y, float* o, float* d) {
+  const float fx = (float)x, fy = (float)y;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    o[i] = c.pos[i];
+    d[i] = fadd(fadd(c.dir0[i], fmul(c.du[i], fx)), fmul(c.dv[i], fy));
+  }
+  const float len = __fsqrt_rn(fadd(fadd(fmul(d[0], d[0]), fmul(d[1], d[1])), fmul(d[2], d[2])));
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    d[i] = __fdiv_rn(d[i], len);
+    if (fabsf(d[i]) < 1e-5f) d[i] = copysignf(1e-5f, d[i]);
+  }
+}
+
+}  // namespace
+}  // namespace yv

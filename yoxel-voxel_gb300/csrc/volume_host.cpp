@@ -52,48 +52,60 @@ double lattice3(uint64_t seed, int oct, int64_t ix, int64_t iy, int64_t iz) {
 
 double smooth(double t) { return t * t * (3.0 - 2.0 * t); }
 
-double value_noise3(uint64_t seed, int oct, double x, double y, double z) {
-  double fx = std::floor(x), fy = std::floor(y), fz = std::floor(z);
-  int64_t ix = (int64_t)fx, iy = (int64_t)fy, iz = (int64_t)fz;
-  double sx = smooth(x - fx), sy = smooth(y - fy), sz = smooth(z - fz);
-  double v[2][2][2];
-  for (int a = 0; a < 2; ++a)
-    for (int b = 0; b < 2; ++b)
-      for (int c = 0; c < 2; ++c) v[a][b][c] = lattice3(seed, oct, ix + c, iy + b, iz + a);
-  double x00 = v[0][0][0] + (v[0][0][1] - v[0][0][0]) * sx;
-  double x01 = v[0][1][0] + (v[0][1][1] - v[0][1][0]) * sx;
-  double x10 = v[1][0][0] + (v[1][0][1] - v[1][0][0]) * sx;
-  double x11 = v[1][1][0] + (v[1][1][1] - v[1][1][0]) * sx;
-  double y0 = x00 + (x01 - x00) * sy, y1 = x10 + (x11 - x10) * sy;
-  return y0 + (y1 - y0) * sz;
-}
-
-// Upper bound of |value_noise3| over lattice cells of the noise grid that the
-// box [lo, hi] touches (the interpolant is a convex combination of corners).
-double noise_box_max(uint64_t seed, int oct, const double* lo, const double* hi) {
-  int64_t a[3], b[3];
-  for (int i = 0; i < 3; ++i) {
-    a[i] = (int64_t)std::floor(lo[i]);
-    b[i] = (int64_t)std::floor(hi[i]) + 1;
+// Lattice values of one noise octave over the scene, tabulated once (the
+// same lattice3 values the formula would hash on every lookup).
+struct LatticeTable {
+  int n = 0;  // entries per axis
+  std::vector<double> v;
+  void build(uint64_t seed, int oct, int n_) {
+    n = n_;
+    v.resize((size_t)n * n * n);
+    for (int z = 0; z < n; ++z)
+      for (int y = 0; y < n; ++y)
+        for (int x = 0; x < n; ++x)
+          v[((size_t)z * n + y) * n + x] = lattice3(seed, oct, x, y, z);
   }
-  double m = -1e30;
-  for (int64_t z = a[2]; z <= b[2]; ++z)
-    for (int64_t y = a[1]; y <= b[1]; ++y)
-      for (int64_t x = a[0]; x <= b[0]; ++x) m = std::max(m, lattice3(seed, oct, x, y, z));
-  return m;
-}
+  double at(int64_t x, int64_t y, int64_t z) const {
+    return v[((size_t)z * (size_t)n + (size_t)y) * (size_t)n + (size_t)x];
+  }
+  // value_noise3 from the table (x, y, z >= 0 inside the table)
+  double noise(double x, double y, double z) const {
+    double fx = std::floor(x), fy = std::floor(y), fz = std::floor(z);
+    int64_t ix = (int64_t)fx, iy = (int64_t)fy, iz = (int64_t)fz;
+    double sx = smooth(x - fx), sy = smooth(y - fy), sz = smooth(z - fz);
+    double x00 = at(ix, iy, iz) + (at(ix + 1, iy, iz) - at(ix, iy, iz)) * sx;
+    double x01 = at(ix, iy + 1, iz) + (at(ix + 1, iy + 1, iz) - at(ix, iy + 1, iz)) * sx;
+    double x10 = at(ix, iy, iz + 1) + (at(ix + 1, iy, iz + 1) - at(ix, iy, iz + 1)) * sx;
+    double x11 = at(ix, iy + 1, iz + 1) + (at(ix + 1, iy + 1, iz + 1) - at(ix, iy + 1, iz + 1)) * sx;
+    double y0 = x00 + (x01 - x00) * sy, y1 = x10 + (x11 - x10) * sy;
+    return y0 + (y1 - y0) * sz;
+  }
+  double box_max(const double* lo, const double* hi) const {
+    double m = -1e30;
+    for (int64_t z = (int64_t)std::floor(lo[2]); z <= (int64_t)std::floor(hi[2]) + 1; ++z)
+      for (int64_t y = (int64_t)std::floor(lo[1]); y <= (int64_t)std::floor(hi[1]) + 1; ++y)
+        for (int64_t x = (int64_t)std::floor(lo[0]); x <= (int64_t)std::floor(hi[0]) + 1; ++x)
+          m = std::max(m, at(x, y, z));
+    return m;
+  }
+};
 
 struct NoiseVolume {
   uint64_t seed;
   int S;
   double offset, amplitude;
   double wsum = 1.0 + 0.5 + 0.25 + 0.125;
+  LatticeTable oct[4], col[3];
+  void init() {
+    for (int o = 0; o < 4; ++o) oct[o].build(seed, o, 8 * (1 << o) + 2);
+    for (int c = 0; c < 3; ++c) col[c].build(seed ^ (0xA1BEull + (uint64_t)c * 977), 7 + c, 6);
+  }
   // density at lattice point p (integer lattice coordinates)
   double density(int x, int y, int z) const {
     double f = 8.0 / S, sum = 0.0, w = 1.0;
     for (int o = 0; o < 4; ++o) {
       double s = f * (double)(1 << o);
-      sum += w * value_noise3(seed, o, x * s, y * s, z * s);
+      sum += w * oct[o].noise(x * s, y * s, z * s);
       w *= 0.5;
     }
     double d = amplitude * (sum / wsum) - offset;
@@ -105,7 +117,7 @@ struct NoiseVolume {
       double s = f * (double)(1 << o);
       double lo[3] = {cx * kB * s, cy * kB * s, cz * kB * s};
       double hi[3] = {(cx * kB + kB) * s, (cy * kB + kB) * s, (cz * kB + kB) * s};
-      ub += w * noise_box_max(seed, o, lo, hi);
+      ub += w * oct[o].box_max(lo, hi);
       w *= 0.5;
     }
     return amplitude * (ub / wsum) - offset > 0.0;
@@ -113,7 +125,7 @@ struct NoiseVolume {
   void albedo(int x, int y, int z, uint8_t* rgb) const {
     double s = 4.0 / S;
     for (int c = 0; c < 3; ++c) {
-      double n = value_noise3(seed ^ (0xA1BEull + (uint64_t)c * 977), 7 + c, x * s, y * s, z * s);
+      double n = col[c].noise(x * s, y * s, z * s);
       double v = 140.0 + 110.0 * n;
       rgb[c] = (uint8_t)std::max(0.0, std::min(255.0, std::floor(v + 0.5)));
     }
@@ -211,6 +223,7 @@ yv_status yv_volume_gen_noise(yv_volume_host** out, int levels, float offset,
     v->nb = 1 << (2 * levels);
     v->S = v->nb * kB;
     NoiseVolume nv{seed, v->S, (double)offset, (double)amplitude};
+    nv.init();
     const int nb = v->nb;
     const size_t ncell = (size_t)nb * nb * nb;
     // candidate cells (bound test), then exact evaluation in parallel
@@ -220,6 +233,7 @@ yv_status yv_volume_gen_noise(yv_volume_host** out, int levels, float offset,
         for (int x = 0; x < nb; ++x)
           if (nv.maybe_nonzero(x, y, z)) cand.push_back((int32_t)(((size_t)z * nb + y) * nb + x));
     std::vector<float> cden(cand.size() * kL3);
+    std::vector<uint8_t> calb(cand.size() * kL3 * 3);
     std::vector<uint8_t> keep(cand.size(), 0);
     std::atomic<size_t> next{0};
     std::vector<std::thread> th;
@@ -240,6 +254,10 @@ yv_status yv_volume_gen_noise(yv_volume_host** out, int levels, float offset,
                 nz = nz || d > 0.f;
               }
           keep[i] = nz;
+          if (nz)
+            for (int k = 0; k < kL3; ++k)
+              nv.albedo(cx * kB + k % kL, cy * kB + (k / kL) % kL, cz * kB + k / (kL * kL),
+                        &calb[(i * kL3 + (size_t)k) * 3]);
         }
       });
     for (auto& t : th) t.join();
@@ -264,11 +282,7 @@ yv_status yv_volume_gen_noise(yv_volume_host** out, int levels, float offset,
       v->cell[b * 3 + 1] = cy;
       v->cell[b * 3 + 2] = cz;
       std::memcpy(&v->density[b * kL3], &cden[ci * kL3], kL3 * sizeof(float));
-      for (int z = 0; z < kL; ++z)
-        for (int y = 0; y < kL; ++y)
-          for (int x = 0; x < kL; ++x)
-            nv.albedo(cx * kB + x, cy * kB + y, cz * kB + z,
-                      &v->albedo[(b * kL3 + (size_t)((z * kL + y) * kL + x)) * 3]);
+      std::memcpy(&v->albedo[b * kL3 * 3], &calb[ci * kL3 * 3], kL3 * 3);
     }
     fill_neighbors(v);
     *out = v;

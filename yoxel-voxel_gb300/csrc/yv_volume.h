@@ -15,7 +15,8 @@ struct CamBasis {
   float dir0[3], du[3], dv[3];
 };
 
-struct VolumeArgs {
+// One volume as the march reads it.
+struct VolumeView {
   // tree + pool (device pointers)
   const uint32_t* grids;
   uint32_t ngrids;
@@ -25,13 +26,17 @@ struct VolumeArgs {
   const void* albedo;    // precision 0: uchar4, 1: fp32x3
   uint32_t nbricks;
   int precision;
-  const int32_t* nbr_up;  // nbricks*7
-  const int32_t* nbr_dn;  // nbricks*7
   // march
   float S;               // lattice cells per axis
   float cell_size;       // world size of a brick cell = 8/S
   float alpha_scale;
   float dt, inv_dt;      // world step and its inverse
+};
+
+struct VolumeArgs {
+  VolumeView v;
+  const int32_t* nbr_up;  // nbricks*7
+  const int32_t* nbr_dn;  // nbricks*7
   // cameras
   int ncams, width, height;
   CamBasis cam[kMaxVolumeCams];

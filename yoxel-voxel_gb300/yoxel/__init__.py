@@ -11,6 +11,8 @@ from .renderer import Renderer, CudaRenderer
 from .volume import (BrickVolume, VolumeGPU, render_volume, volume_backward, volume_march,
                      torch_desc, cameras, sphere_cameras)
 
-__all__ = ["SVOScene", "Renderer", "CudaRenderer", "YvError", "LIB_PATH",
+from .batch import Batch
+
+__all__ = ["SVOScene", "Renderer", "CudaRenderer", "YvError", "LIB_PATH", "Batch",
            "NODE_DTYPE", "ATTR_DTYPE", "BrickVolume", "VolumeGPU", "render_volume",
            "volume_backward", "volume_march", "torch_desc", "cameras", "sphere_cameras"]

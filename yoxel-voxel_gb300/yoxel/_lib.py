@@ -147,6 +147,16 @@ _SIGS = {
                                C.c_int32, C.c_int32, C.POINTER(MarchParams), P, P, P, P, P]),
     "yv_volume_fold_aprons": (S, [C.POINTER(VolumeDevice), P, P, P]),
     "yv_volume_sync_aprons": (S, [C.POINTER(VolumeDevice), P, P, P]),
+    "yv_batch_create": (S, [C.POINTER(P)]),
+    "yv_batch_destroy": (None, [P]),
+    "yv_batch_clear": (S, [P]),
+    "yv_batch_add_svo": (S, [P, P, P]),
+    "yv_batch_add_volume": (S, [P, C.POINTER(VolumeDevice), C.POINTER(Camera), C.c_int32,
+                                C.c_int32, C.POINTER(MarchParams), P]),
+    "yv_batch_set_launch_config": (S, [P, C.POINTER(LaunchConfig)]),
+    "yv_batch_render": (S, [P, C.c_int32, P]),
+    "yv_batch_render_separate": (S, [P, P]),
+    "yv_batch_info": (S, [P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint64)]),
     "yv_render_svo_noalloc": (S, [P, U32, U32, P, U32, C.POINTER(Camera), C.POINTER(Light),
                                   C.c_int32, C.c_int32, C.POINTER(FrameOutputs), P]),
 }
