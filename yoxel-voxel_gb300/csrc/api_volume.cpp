@@ -228,21 +228,35 @@ yv_status yv_volume_backward(const yv_volume_device* vol, const yv_camera* cams,
     return YV_ERR_INVALID_ARG;
   }
   const size_t px = (size_t)width * (size_t)height;
-  for (int c0 = 0; c0 < ncams; c0 += kMaxVolumeCams) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // Gradients accumulate in a packed (albedo rgb, density) float4 per
+  // lattice point - one 16-byte atomic per corner - taken from the
+  // stream-ordered pool and added into the caller's tensors at the end.
+  const size_t npts = (size_t)vol->nbricks * 729u;
+  float4* packed = nullptr;
+  cudaError_t e = cudaSuccess;
+  if (npts) {
+    e = cudaMallocAsync(reinterpret_cast<void**>(&packed), npts * sizeof(float4), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(packed, 0, npts * sizeof(float4), s);
+  }
+  for (int c0 = 0; c0 < ncams && e == cudaSuccess && npts; c0 += kMaxVolumeCams) {
     const int n = ncams - c0 < kMaxVolumeCams ? ncams - c0 : kMaxVolumeCams;
     set_cams(a, cams + c0, n);
     a->rgba_fwd = rgba + (size_t)c0 * px * 4;
     a->grad_rgba = grad_rgba + (size_t)c0 * px * 4;
     a->grad_density = grad_density;
     a->grad_albedo = grad_albedo;
-    cudaError_t e = launch_volume_backward(*a, static_cast<cudaStream_t>(stream));
-    if (e != cudaSuccess) {
-      delete a;
-      return fail(e, "volume backward launch");
-    }
+    a->grad_packed = packed;
+    e = launch_volume_backward(*a, s);
+  }
+  if (e == cudaSuccess && npts)
+    e = launch_unpack_grads(packed, (uint32_t)npts, grad_density, grad_albedo, s);
+  if (packed) {
+    cudaError_t ef = cudaFreeAsync(packed, s);
+    if (e == cudaSuccess) e = ef;
   }
   delete a;
-  return YV_OK;
+  return e == cudaSuccess ? YV_OK : fail(e, "volume backward");
 }
 
 yv_status yv_volume_fold_aprons(const yv_volume_device* vol, float* grad_density,

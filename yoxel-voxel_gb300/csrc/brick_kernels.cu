@@ -61,15 +61,15 @@ struct GradVis {
   uint32_t base;
   float gd[8];
   float ga[8][3];
+  // One 16-byte vector atomic per corner into the packed (albedo rgb,
+  // density) gradient of the lattice point.
   __device__ __forceinline__ void flush() {
     if (base == 0xFFFFFFFFu) return;
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const uint32_t idx = base + (uint32_t)(((j >> 2) * kL + ((j >> 1) & 1)) * kL + (j & 1));
-      if (gd[j] != 0.f) atomicAdd(a->grad_density + idx, gd[j]);
-#pragma unroll
-      for (int ch = 0; ch < 3; ++ch)
-        if (ga[j][ch] != 0.f) atomicAdd(a->grad_albedo + 3 * (size_t)idx + ch, ga[j][ch]);
+      if (gd[j] != 0.f || ga[j][0] != 0.f || ga[j][1] != 0.f || ga[j][2] != 0.f)
+        atomicAdd(a->grad_packed + idx, make_float4(ga[j][0], ga[j][1], ga[j][2], gd[j]));
       gd[j] = 0.f;
       ga[j][0] = ga[j][1] = ga[j][2] = 0.f;
     }
@@ -218,6 +218,25 @@ cudaError_t launch_apron_fold(const VolumeArgs& a, int channels, float* g, bool 
   const int blocks = 2 * device_sm_count_vol() * 8;
   if (gather) fold_gather_kernel<<<blocks, 256, 0, s>>>(a, channels, g);
   fold_scatter_kernel<<<blocks, 256, 0, s>>>(a, channels, g);
+  return cudaGetLastError();
+}
+
+__global__ void unpack_grads_kernel(const float4* __restrict__ p, uint32_t n, float* gd,
+                                    float* ga) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float4 v = p[i];
+    gd[i] += v.w;
+    ga[3 * (size_t)i] += v.x;
+    ga[3 * (size_t)i + 1] += v.y;
+    ga[3 * (size_t)i + 2] += v.z;
+  }
+}
+
+cudaError_t launch_unpack_grads(const float4* packed, uint32_t n, float* grad_density,
+                                float* grad_albedo, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  unpack_grads_kernel<<<2 * device_sm_count_vol() * 8, 256, 0, s>>>(packed, n, grad_density,
+                                                                     grad_albedo);
   return cudaGetLastError();
 }
 

@@ -204,10 +204,11 @@ __device__ __forceinline__ void march(const VolumeView& a, const uint32_t* sg, u
       const float plane = fmul((float)(d[i] > 0.f ? cell[i] + 1 : cell[i]), h);
       tx[i] = fmul(fsub(plane, o[i]), inv[i]);
     }
+    // exit axis = first argmin (selects, no dynamic register indexing)
     int e = 0;
-    if (tx[1] < tx[e]) e = 1;
-    if (tx[2] < tx[e]) e = 2;
-    const float t_out = tx[e];
+    float t_out = tx[0];
+    if (tx[1] < t_out) { e = 1; t_out = tx[1]; }
+    if (tx[2] < t_out) { e = 2; t_out = tx[2]; }
     const int b = lookup(a, sg, nsg, cell);
     if (b == -2) {
       r.bad = true;
@@ -239,8 +240,11 @@ __device__ __forceinline__ void march(const VolumeView& a, const uint32_t* sg, u
       }
     }
     t_in = t_out;
-    cell[e] += step[e];
-    if (cell[e] < 0 || cell[e] >= a.nb) break;
+    int ce;
+    if (e == 0) ce = (cell[0] += step[0]);
+    else if (e == 1) ce = (cell[1] += step[1]);
+    else ce = (cell[2] += step[2]);
+    if (ce < 0 || ce >= a.nb) break;
   }
 done:
   r.c[0] = C0;

@@ -48,11 +48,15 @@ struct VolumeArgs {
   const float* grad_rgba; // backward: dL/d rgba
   float* grad_density;    // backward outputs (pool layout)
   float* grad_albedo;
+  float4* grad_packed;    // backward scratch: (albedo rgb, density) per lattice point
   uint32_t* status;       // optional device status word
 };
 
 cudaError_t launch_volume_forward(const VolumeArgs& a, cudaStream_t s);
 cudaError_t launch_volume_backward(const VolumeArgs& a, cudaStream_t s);
+// grad_density += packed.w, grad_albedo += packed.xyz (n lattice points).
+cudaError_t launch_unpack_grads(const float4* packed, uint32_t n, float* grad_density,
+                                float* grad_albedo, cudaStream_t s);
 // gather=true: fold apron gradients into owners, then copy owners to aprons;
 // gather=false: copy owners to aprons only (parameter sync).
 cudaError_t launch_apron_fold(const VolumeArgs& a, int channels, float* g, bool gather,
