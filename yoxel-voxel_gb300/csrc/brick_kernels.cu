@@ -2,10 +2,16 @@
 // sm_103a: forward compositing over many cameras, the re-marching adjoint,
 // and apron maintenance.  Device helpers and the march are in
 // brick_march.cuh.
+#include <type_traits>
+
 #include "brick_march.cuh"
 
 namespace yv {
 namespace {
+
+// Adjoint variant: per-lane coalescing (GradVis) at 2 resident blocks/SM.
+constexpr bool kBackwardDirect = false;
+constexpr int kBackwardMinBlocks = 2;
 
 // tile mapping: warp w of the grid -> 8x4 pixel tile of one camera image
 __device__ __forceinline__ bool ray_of_thread(const VolumeArgs& a, uint32_t tile, int& cam,
@@ -52,8 +58,44 @@ __global__ void __launch_bounds__(256) volume_forward_kernel(VolumeArgs a) {
   if (bad && a.status) atomicOr(a.status, 4u);
 }
 
+// Gradient of one sample w.r.t. its alpha and colour (see the header):
+// returns d(sigma) (through saturate) and the colour gradient factor.
+struct SampleGrad {
+  float dsig;
+  float gc[3];
+};
+
+__device__ __forceinline__ SampleGrad sample_grad(const VolumeArgs* a, const float* g,
+                                                  const float* out, const SampleCtx& s,
+                                                  float T, float A, float C0, float C1,
+                                                  float C2) {
+  const float w = fmul(T, s.alpha);
+  const float om = fsub(1.f, s.alpha);
+  const float Cb[3] = {C0, C1, C2};
+  float dal = 0.f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float ck = k < 3 ? s.col[k] : 1.f;
+    const float before = k < 3 ? Cb[k] : A;
+    const float after = k < 3 ? ffma(w, ck, before) : fadd(A, w);
+    float term = fmul(T, ck);
+    if (om > 0.f) term = fsub(term, __fdiv_rn(fsub(out[k], after), om));
+    dal = ffma(g[k], term, dal);
+  }
+  const float sa = fmul(s.sigma, a->v.alpha_scale);
+  SampleGrad r;
+  // saturate'(s) = 1 on [0, 1): right derivative at 0 so that empty lattice
+  // points still receive gradient
+  r.dsig = (sa >= 0.f && sa < 1.f) ? fmul(dal, a->v.alpha_scale) : 0.f;
+  r.gc[0] = fmul(g[0], w);
+  r.gc[1] = fmul(g[1], w);
+  r.gc[2] = fmul(g[2], w);
+  return r;
+}
+
 // Per-lane coalescing of corner gradients while consecutive samples share
-// a trilinear cell; flushed with atomics.
+// a trilinear cell; flushed with one 16-byte vector atomic per corner into
+// the packed (albedo rgb, density) gradient of the lattice point.
 struct GradVis {
   const VolumeArgs* a;
   float g[4];    // dL/d(r,g,b,a) of this ray
@@ -61,15 +103,21 @@ struct GradVis {
   uint32_t base;
   float gd[8];
   float ga[8][3];
-  // One 16-byte vector atomic per corner into the packed (albedo rgb,
-  // density) gradient of the lattice point.
+  __device__ __forceinline__ void init() {
+    base = 0xFFFFFFFFu;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      gd[j] = 0.f;
+      ga[j][0] = ga[j][1] = ga[j][2] = 0.f;
+    }
+  }
   __device__ __forceinline__ void flush() {
     if (base == 0xFFFFFFFFu) return;
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-      const uint32_t idx = base + (uint32_t)(((j >> 2) * kL + ((j >> 1) & 1)) * kL + (j & 1));
       if (gd[j] != 0.f || ga[j][0] != 0.f || ga[j][1] != 0.f || ga[j][2] != 0.f)
-        atomicAdd(a->grad_packed + idx, make_float4(ga[j][0], ga[j][1], ga[j][2], gd[j]));
+        atomicAdd(a->grad_packed + base + corner_offset(j),
+                  make_float4(ga[j][0], ga[j][1], ga[j][2], gd[j]));
       gd[j] = 0.f;
       ga[j][0] = ga[j][1] = ga[j][2] = 0.f;
     }
@@ -80,39 +128,39 @@ struct GradVis {
       flush();
       base = s.base;
     }
-    const float w = fmul(T, s.alpha);
-    const float om = fsub(1.f, s.alpha);
-    const float Cb[3] = {C0, C1, C2};
-    float dal = 0.f;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const float ck = k < 3 ? s.col[k] : 1.f;
-      const float before = k < 3 ? Cb[k] : A;
-      const float after = k < 3 ? ffma(w, ck, before) : fadd(A, w);
-      float term = fmul(T, ck);
-      if (om > 0.f) term = fsub(term, __fdiv_rn(fsub(out[k], after), om));
-      dal = ffma(g[k], term, dal);
-    }
-    const float sa = fmul(s.sigma, a->v.alpha_scale);
-    // saturate'(s) = 1 on [0, 1): right derivative at 0 so that empty lattice
-    // points still receive gradient
-    const float dsig = (sa >= 0.f && sa < 1.f) ? fmul(dal, a->v.alpha_scale) : 0.f;
-    const float wx[2] = {fsub(1.f, s.fx), s.fx};
-    const float wy[2] = {fsub(1.f, s.fy), s.fy};
-    const float wz[2] = {fsub(1.f, s.fz), s.fz};
-    const float gc[3] = {fmul(g[0], w), fmul(g[1], w), fmul(g[2], w)};
+    const SampleGrad sg = sample_grad(a, g, out, s, T, A, C0, C1, C2);
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-      const float wj = fmul(fmul(wx[j & 1], wy[(j >> 1) & 1]), wz[j >> 2]);
-      gd[j] = ffma(wj, dsig, gd[j]);
+      gd[j] = ffma(s.w[j], sg.dsig, gd[j]);
 #pragma unroll
-      for (int ch = 0; ch < 3; ++ch) ga[j][ch] = ffma(wj, gc[ch], ga[j][ch]);
+      for (int ch = 0; ch < 3; ++ch) ga[j][ch] = ffma(s.w[j], sg.gc[ch], ga[j][ch]);
     }
   }
 };
 
-template <int P>
-__global__ void __launch_bounds__(256) volume_backward_kernel(VolumeArgs a) {
+// The same without coalescing: one vector atomic per corner and sample, no
+// register accumulators (fewer registers, more atomics).
+struct GradVisDirect {
+  const VolumeArgs* a;
+  float g[4];
+  float out[4];
+  __device__ __forceinline__ void init() {}
+  __device__ __forceinline__ void flush() {}
+  __device__ __forceinline__ void operator()(const SampleCtx& s, float T, float A, float C0,
+                                             float C1, float C2) {
+    const SampleGrad sg = sample_grad(a, g, out, s, T, A, C0, C1, C2);
+    if (sg.dsig == 0.f && sg.gc[0] == 0.f && sg.gc[1] == 0.f && sg.gc[2] == 0.f) return;
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      atomicAdd(a->grad_packed + s.base + corner_offset(j),
+                make_float4(fmul(s.w[j], sg.gc[0]), fmul(s.w[j], sg.gc[1]),
+                            fmul(s.w[j], sg.gc[2]), fmul(s.w[j], sg.dsig)));
+  }
+};
+
+// kDirect: GradVisDirect instead of GradVis; kMinBlocks: register budget.
+template <int P, bool kDirect, int kMinBlocks>
+__global__ void __launch_bounds__(256, kMinBlocks) volume_backward_kernel(VolumeArgs a) {
   __shared__ uint32_t sg[kSmemGrids * 64];
   const uint32_t nsg = stage_grids(a, sg);
   const uint32_t n_tiles = (uint32_t)a.ncams * (uint32_t)(((a.width + 7) >> 3) * ((a.height + 3) >> 2));
@@ -128,16 +176,11 @@ __global__ void __launch_bounds__(256) volume_backward_kernel(VolumeArgs a) {
     const float4 o4 = reinterpret_cast<const float4*>(a.rgba_fwd)[off];
     float o[3], d[3];
     pixel_ray(a.cam[cam], x, y, o, d);
-    GradVis gv;
+    typename std::conditional<kDirect, GradVisDirect, GradVis>::type gv;
     gv.a = &a;
     gv.g[0] = g4.x; gv.g[1] = g4.y; gv.g[2] = g4.z; gv.g[3] = g4.w;
     gv.out[0] = o4.x; gv.out[1] = o4.y; gv.out[2] = o4.z; gv.out[3] = o4.w;
-    gv.base = 0xFFFFFFFFu;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      gv.gd[j] = 0.f;
-      gv.ga[j][0] = gv.ga[j][1] = gv.ga[j][2] = 0.f;
-    }
+    gv.init();
     RayOut r;
     march<P>(a.v, sg, nsg, o, d, gv, r);
     gv.flush();
@@ -205,10 +248,9 @@ cudaError_t launch_volume_backward(const VolumeArgs& a, cudaStream_t s) {
   const uint32_t tiles = (uint32_t)a.ncams * (uint32_t)(((a.width + 7) >> 3) * ((a.height + 3) >> 2));
   const uint32_t blocks = (tiles + 7) / 8;
   if (blocks == 0) return cudaSuccess;
-  if (a.v.precision == 0)
-    volume_backward_kernel<0><<<blocks, 256, 0, s>>>(a);
-  else
-    volume_backward_kernel<1><<<blocks, 256, 0, s>>>(a);
+  // only fp32 (learnable) volumes have an adjoint
+  if (a.v.precision != 1) return cudaErrorInvalidValue;
+  volume_backward_kernel<1, kBackwardDirect, kBackwardMinBlocks><<<blocks, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 

@@ -51,24 +51,26 @@ __device__ __forceinline__ float lerpf_(float a, float b, float t) { return ffma
 template <int P>
 struct Voxel;
 
-// precision 0: fp16 density, uchar4 albedo
+// precision 0: fp16 density, uchar4 albedo (interpolated as raw 0..255
+// values and scaled once after interpolation)
 template <>
 struct Voxel<0> {
+  static constexpr float kAlbedoScale = 1.0f / 255.0f;
   __device__ static __forceinline__ float den(const void* p, uint32_t i) {
     return __half2float(__ushort_as_half(__ldg(static_cast<const unsigned short*>(p) + i)));
   }
   __device__ static __forceinline__ void alb(const void* p, uint32_t i, float* c) {
     const uint32_t v = __ldg(static_cast<const unsigned int*>(p) + i);
-    const float s = 1.0f / 255.0f;
-    c[0] = fmul((float)(v & 0xFFu), s);
-    c[1] = fmul((float)((v >> 8) & 0xFFu), s);
-    c[2] = fmul((float)((v >> 16) & 0xFFu), s);
+    c[0] = (float)(v & 0xFFu);
+    c[1] = (float)((v >> 8) & 0xFFu);
+    c[2] = (float)((v >> 16) & 0xFFu);
   }
 };
 
 // precision 1: fp32 density, fp32 RGB albedo (learnable)
 template <>
 struct Voxel<1> {
+  static constexpr float kAlbedoScale = 1.0f;
   __device__ static __forceinline__ float den(const void* p, uint32_t i) {
     return __ldg(static_cast<const float*>(p) + i);
   }
@@ -82,10 +84,15 @@ struct Voxel<1> {
 
 struct SampleCtx {
   uint32_t base;  // brick*729 + corner-000 lattice index
-  float fx, fy, fz;
+  float w[8];     // trilinear weights, corner j: bit0 +x, bit1 +y, bit2 +z
   float sigma, alpha;
   float col[3];
 };
+
+// Lattice offset of trilinear corner j inside a 9^3 brick.
+__device__ __forceinline__ uint32_t corner_offset(int j) {
+  return (uint32_t)(((j >> 2) * kL + ((j >> 1) & 1)) * kL + (j & 1));
+}
 
 // lx, ly, lz: brick-local lattice coordinates of the sample, in [0, 8].
 template <int P>
@@ -103,28 +110,33 @@ __device__ __forceinline__ void eval_sample(const VolumeView& a, int b, float lx
     i0[i] = k;
     f[i] = fi;
   }
-  s.fx = f[0];
-  s.fy = f[1];
-  s.fz = f[2];
   s.base = (uint32_t)b * (uint32_t)kL3 + (uint32_t)((i0[2] * kL + i0[1]) * kL + i0[0]);
-  float d[8];
-  float c[8][3];
+  const float gx = fsub(1.f, f[0]), gy = fsub(1.f, f[1]), gz = fsub(1.f, f[2]);
+  const float w00 = fmul(gx, gy), w10 = fmul(f[0], gy), w01 = fmul(gx, f[1]),
+              w11 = fmul(f[0], f[1]);
+  s.w[0] = fmul(w00, gz);
+  s.w[1] = fmul(w10, gz);
+  s.w[2] = fmul(w01, gz);
+  s.w[3] = fmul(w11, gz);
+  s.w[4] = fmul(w00, f[2]);
+  s.w[5] = fmul(w10, f[2]);
+  s.w[6] = fmul(w01, f[2]);
+  s.w[7] = fmul(w11, f[2]);
+  float sig = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f;
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
-    const uint32_t idx = s.base + (uint32_t)(((j >> 2) * kL + ((j >> 1) & 1)) * kL + (j & 1));
-    d[j] = Voxel<P>::den(a.density, idx);
-    Voxel<P>::alb(a.albedo, idx, c[j]);
+    const uint32_t idx = s.base + corner_offset(j);
+    float c[3];
+    Voxel<P>::alb(a.albedo, idx, c);
+    sig = ffma(s.w[j], Voxel<P>::den(a.density, idx), sig);
+    c0 = ffma(s.w[j], c[0], c0);
+    c1 = ffma(s.w[j], c[1], c1);
+    c2 = ffma(s.w[j], c[2], c2);
   }
-  // lerp along x, then y, then z (corner j: bit0 x, bit1 y, bit2 z)
-  float dx0 = lerpf_(d[0], d[1], f[0]), dx1 = lerpf_(d[2], d[3], f[0]);
-  float dx2 = lerpf_(d[4], d[5], f[0]), dx3 = lerpf_(d[6], d[7], f[0]);
-  s.sigma = lerpf_(lerpf_(dx0, dx1, f[1]), lerpf_(dx2, dx3, f[1]), f[2]);
-#pragma unroll
-  for (int ch = 0; ch < 3; ++ch) {
-    float x0 = lerpf_(c[0][ch], c[1][ch], f[0]), x1 = lerpf_(c[2][ch], c[3][ch], f[0]);
-    float x2 = lerpf_(c[4][ch], c[5][ch], f[0]), x3 = lerpf_(c[6][ch], c[7][ch], f[0]);
-    s.col[ch] = lerpf_(lerpf_(x0, x1, f[1]), lerpf_(x2, x3, f[1]), f[2]);
-  }
+  s.sigma = sig;
+  s.col[0] = fmul(c0, Voxel<P>::kAlbedoScale);
+  s.col[1] = fmul(c1, Voxel<P>::kAlbedoScale);
+  s.col[2] = fmul(c2, Voxel<P>::kAlbedoScale);
   float al = fmul(s.sigma, a.alpha_scale);
   s.alpha = al < 0.f ? 0.f : (al > 1.f ? 1.f : al);
 }
