@@ -33,6 +33,10 @@ for _p in (ROOT, PKG):
 
 METRIC = "Mrays/s on 1 GB300: plain vs persistent-batched, and fwd+bwd at stated error"
 UNIT = "Mrays/s"
+# brick pool formats (include/yv_c_api.h YV_PRECISION_*)
+POOL_FORMATS = {0: "fp16 density + RGBA8 albedo", 1: "fp32 density + fp32 RGB albedo",
+                2: "packed float4 (r, g, b, density)",
+                3: "packed 8 B (fp16 density, RGB8)"}
 LIGHT = (np.array([0.3, 0.5, 0.8]) / np.linalg.norm([0.3, 0.5, 0.8])).astype(np.float32)
 
 
@@ -55,17 +59,17 @@ CONFIGS = {
                           "floating cubes, 1920x1080 FP32 primary rays + 1 hard-shadow ray "
                           "per hit"),
     "cfg3": dict(kind="brick", levels=3, width=1024, height=1024, alpha_scale=1.0,
-                 step_vox=0.5,
+                 step_vox=0.5, precision=3,
                  workload="N=4 brick tree, 3 grid levels + 8^3 bricks = 512^3, fp16 density "
                           "(4-octave noise - 0.4, empty bricks culled, ~20% occupancy) + uint8 "
-                          "RGB albedo, 1024x1024 rays, 0.5-voxel steps, trilinear, "
+                          "RGB albedo packed 8 B per lattice point, 1024x1024 rays, 0.5-voxel steps, trilinear, "
                           "front-to-back, early exit at T<0.01"),
     "cfg4": dict(kind="train", levels=2, cams=64, width=256, height=256, alpha_scale=1.0,
                  step_vox=0.5,
                  workload="differentiable 128^3 brick volume (fp32 density + fp32 RGB albedo), "
                           "64 cameras on a sphere at 256x256, L2 loss to images of the volume "
                           "+ N(0,0.1) noise; forward + re-marching adjoint (value = fwd+bwd)"),
-    "cfg5": dict(kind="batch", n=32,
+    "cfg5": dict(kind="batch", n=32, precision=3,
                  workload="32 seeded scenes (cfg1-type SVO or cfg3-type fp16 bricks), depth "
                           "6..11, resolution 128^2..1024^2, one persistent launch from a global "
                           "ray queue replayed from a CUDA graph (value) vs 32 per-scene launches"),
@@ -431,7 +435,8 @@ def run_brick(args, cfg):
     t_scene = time.perf_counter()
     vol = yoxel.BrickVolume.noise(cfg["levels"], 0.4, 1.4, 1234)
     t_scene = time.perf_counter() - t_scene
-    gv = vol.upload(0)
+    prec = cfg["precision"] if args.precision is None else args.precision
+    gv = vol.upload(prec)
     desc = gv.desc()
     pos, view = W.camera()
     cam = [(pos, view, (0, 0, 1), 60.0)]
@@ -442,9 +447,11 @@ def run_brick(args, cfg):
     out = yoxel.render_volume(desc, cam, w, h, cfg["alpha_scale"], cfg["step_vox"],
                               samples=ns, bricks=nb)
     S, B = int(ns.to(torch.int64).sum()), int(nb.to(torch.int64).sum())
-    # 8 trilinear corners x (2 B fp16 density + 3 B RGB) per sample, 4 B per
-    # tree level per occupied brick entered, 16 B RGBA fp32 out
-    alg = 40 * S + 4 * cfg["levels"] * B + 16 * rays
+    # 8 trilinear corners x (density + RGB) per sample - 2 + 3 B for the fp16
+    # formats, 4 + 12 B for fp32 - 4 B per tree level per occupied brick
+    # entered, 16 B RGBA fp32 out
+    per_corner = 5 if prec in (0, 3) else 16
+    alg = 8 * per_corner * S + 4 * cfg["levels"] * B + 16 * rays
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     fn = lambda: yoxel.render_volume(desc, cam, w, h, cfg["alpha_scale"], cfg["step_vox"],
                                      out=out)
@@ -466,9 +473,11 @@ def run_brick(args, cfg):
     e2e_s = (time.perf_counter() - te) / args.steps
     peaks, kind = measured_peaks()
     achieved = alg / (mean_ms / 1e3) / 1e9
-    line = _base_line(args, cfg, rays / (mean_ms / 1e3) / 1e6, mean_ms, "f32 (fp16 storage)")
+    line = _base_line(args, cfg, rays / (mean_ms / 1e3) / 1e6, mean_ms,
+                      "f32 (fp16 storage)" if prec in (0, 3) else "f32")
     line["config"].update(volume_bricks=vol.nbricks, occupancy=round(vol.occupancy, 4),
-                          mean_samples_per_ray=round(S / rays, 2))
+                          mean_samples_per_ray=round(S / rays, 2),
+                          pool_format=POOL_FORMATS[prec])
     line.update({
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
@@ -481,7 +490,8 @@ def run_brick(args, cfg):
         "scene_build_s": round(t_scene, 2)})
     if not args.no_cpu_baseline:
         from oracle import pyoracle
-        den = vol.density.astype(np.float16).astype(np.float32)
+        den = vol.density.astype(np.float16 if prec in (0, 3) else np.float32)
+        den = den.astype(np.float32)
         alb = vol.albedo_u8.astype(np.float32) * np.float32(1.0 / 255.0)
         threads = os.cpu_count() or 1
         sw, sh = w // 4, h // 4
@@ -534,7 +544,10 @@ def run_train(args, cfg):
         loss.backward()
 
     fwd_out = torch.empty((cfg["cams"], h, w, 4), dtype=torch.float32, device="cuda")
-    desc = yoxel.torch_desc(tv, density.detach(), albedo.detach())
+    # forward-only and adjoint-only legs read the same packed float4 pool
+    # that volume_march builds each step
+    packed = yoxel.pack_volume(density.detach(), albedo.detach())
+    desc = yoxel.torch_desc(tv, packed=packed)
 
     def fwd():
         yoxel.render_volume(desc, cams, w, h, a_s, st, out=fwd_out)
@@ -581,7 +594,10 @@ def run_train(args, cfg):
                      "kernel": "volume_backward_kernel", "algorithmic_bytes_per_launch": alg_b},
         "gradient_check": "GPU adjoint vs FP64 adjoint / naive PyTorch marcher / FP64 central "
                           "differences: rel. error <= 1e-4 (tests/test_volume_gpu.py)",
-        "gpu_launches": args.steps * 3, "clocks": clocks, "wall_s_timed_region": round(wall, 4)})
+        # per fwd+bwd step: pack, forward, adjoint, unpack, 2 x (fold gather +
+        # scatter); the loss and its gradient are torch's own kernels
+        "gpu_launches": args.steps * (6 + 2 * -(-cfg["cams"] // 64)),
+        "clocks": clocks, "wall_s_timed_region": round(wall, 4)})
     host = torch.empty((), dtype=torch.float32, pin_memory=True)
     torch.cuda.synchronize()
     te = time.perf_counter()
@@ -630,7 +646,7 @@ def run_batch(args, cfg):
         else:
             v = yoxel.BrickVolume.noise(W.brick_levels_for_depth(sp["depth"]), 0.4, 1.4,
                                         sp["seed"])
-            gv = v.upload(0)
+            gv = v.upload(cfg["precision"] if args.precision is None else args.precision)
             out = torch.empty((res, res, 4), dtype=torch.float32, device="cuda")
             batch.add_volume(gv.desc(), (pos, view, (0, 0, 1), 60.0), res, res, out)
             keep += [gv, out]
@@ -676,6 +692,8 @@ def main():
     ap.add_argument("--impl", default="yoxel", choices=["yoxel", "reference"])
     ap.add_argument("--config", default="cfg2", choices=sorted(CONFIGS))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", type=int, default=None, choices=[0, 1, 2, 3],
+                    help="brick pool format for the brick workload (default: the config's)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -256,6 +256,10 @@ const int32_t*  yv_volume_neighbors(const yv_volume_host* v, int upper);
 
 #define YV_PRECISION_F16 0  /* fp16 density, uchar4 albedo (render only) */
 #define YV_PRECISION_F32 1  /* fp32 density, fp32 RGB albedo (learnable)  */
+/* Packed lattice points: the whole point in `albedo`, density == NULL.   */
+#define YV_PRECISION_F32_PACKED 2 /* float4 (r, g, b, density) (learnable) */
+#define YV_PRECISION_F16_PACKED 3 /* 8 B {fp16 density | r<<16 | g<<24, b},
+                                     RGB8 (render only)                     */
 
 /* Device view of a volume: all pointers are device pointers. */
 typedef struct yv_volume_device {
@@ -301,9 +305,9 @@ yv_status yv_volume_render(const yv_volume_device* vol, const yv_camera* cams,
                            const yv_march_params* mp, float* rgba,
                            uint32_t* samples, uint32_t* bricks, void* stream);
 
-/* Adjoint of yv_volume_render (fp32 volumes): re-marches every ray and
- * accumulates dL/ddensity and dL/dalbedo (pool layout, ADDED to the
- * buffers) from dL/drgba, given the forward output rgba. */
+/* Adjoint of yv_volume_render (fp32 volumes, plain or packed): re-marches
+ * every ray and accumulates dL/ddensity and dL/dalbedo (pool layout, ADDED
+ * to the buffers) from dL/drgba, given the forward output rgba. */
 yv_status yv_volume_backward(const yv_volume_device* vol,
                              const yv_camera* cams, int32_t ncams,
                              int32_t width, int32_t height,
@@ -320,6 +324,11 @@ yv_status yv_volume_fold_aprons(const yv_volume_device* vol,
 /* Copies owner values into the apron slots of fp32 density / albedo. */
 yv_status yv_volume_sync_aprons(const yv_volume_device* vol, float* density,
                                 float* albedo, void* stream);
+/* packed[i] = (albedo[3i], albedo[3i+1], albedo[3i+2], density[i]) for
+ * npoints lattice points (device pointers, packed 16-byte aligned): the
+ * YV_PRECISION_F32_PACKED pool of fp32 parameters, rebuilt per step. */
+yv_status yv_volume_pack(const float* density, const float* albedo,
+                         uint32_t npoints, float* packed, void* stream);
 
 /* ------------------------------------------------------------------------ */
 /* Batched persistent render (no reference code; nearest structure is the   */

@@ -27,7 +27,8 @@ def build_batch(yoxel_mod, torch):
         batch.add_svo(r, o)
         keep += [s, r]
         outs.append(("svo", r, o))
-    for i, (levels, prec, res) in enumerate([(1, 0, (72, 40)), (2, 1, (100, 100))]):
+    for i, (levels, prec, res) in enumerate([(1, 0, (72, 40)), (2, 1, (100, 100)),
+                                              (1, 3, (40, 56)), (2, 2, (64, 48))]):
         v = yoxel_mod.BrickVolume.noise(levels, 0.4, 1.4, 7 + i)
         g = v.upload(prec)
         pos, view = W.camera((0.3, 1.0, 0.4 + 0.2 * i))
@@ -43,7 +44,7 @@ def test_batch_matches_separate_launches_and_renderers(yoxel_mod):
     import torch
     batch, outs, keep = build_batch(yoxel_mod, torch)
     n, rays = batch.info()
-    assert n == 5 and rays > 0
+    assert n == 7 and rays > 0
     results = {}
     for mode in ("separate", "plain", "graph", "graph_again"):
         for _, _, o in outs:

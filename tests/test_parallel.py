@@ -1,0 +1,92 @@
+"""Multi-GPU host logic, exercised on CPU ranks (gloo, world size 2).
+
+The ray caster shards with no data-path collective (scene replicas, tile or
+scene partitions, a gather of frames at the end); training is data-parallel
+over cameras with one exchange step, a sum all-reduce of the gradients."""
+import os
+import socket
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import PKG, ROOT
+
+
+def test_partition_scenes_balances_and_covers():
+    from yoxel import parallel as P
+    costs = [100, 80, 60, 55, 40, 30, 20, 10, 5, 1]
+    parts = P.partition_scenes(costs, 3)
+    flat = sorted(i for p in parts for i in p)
+    assert flat == list(range(len(costs)))
+    loads = [sum(costs[i] for i in p) for p in parts]
+    assert max(loads) - min(loads) <= max(costs)
+    assert P.partition_scenes(costs, 3) == parts  # deterministic
+
+
+def test_partition_tiles_contiguous_and_balanced():
+    from yoxel import parallel as P
+    rng = np.random.default_rng(0)
+    c = rng.random(1000) * 10
+    parts = P.partition_tiles(c, 4)
+    assert parts[0][0] == 0 and parts[-1][1] == 1000
+    for (a, b), (a2, _) in zip(parts, parts[1:]):
+        assert b == a2 and a <= b
+    sums = [c[a:b].sum() for a, b in parts]
+    assert max(sums) - min(sums) <= 2 * c.max()
+    assert P.partition_tiles([], 3) == [(0, 0)] * 3
+
+
+def test_partition_cameras():
+    from yoxel import parallel as P
+    assert P.partition_cameras(64, 2) == [(0, 32), (32, 64)]
+    assert P.partition_cameras(5, 3) == [(0, 2), (2, 4), (4, 5)]
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _worker(rank, world, port, q):
+    sys.path[:0] = [ROOT, PKG]
+    import torch
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from yoxel import parallel as P
+    # data-parallel gradient: rank r holds the gradient of its camera shard
+    cams = P.partition_cameras(8, world)[rank]
+    g = torch.zeros(6, dtype=torch.float64)
+    for c in range(*cams):
+        g += torch.arange(6, dtype=torch.float64) * (c + 1)
+    P.sum_gradients([g])
+    # frame gather: every rank renders its tile band (here: a fake frame)
+    frame = torch.full((4,), float(rank), dtype=torch.float32)
+    frames = P.gather_to_root(frame, world, rank)
+    q.put((rank, g.tolist(), None if frames is None else [f.tolist() for f in frames]))
+    dist.destroy_process_group()
+
+
+def test_gloo_gradient_sum_and_frame_gather():
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = {}
+    for _ in range(2):
+        rank, g, frames = q.get(timeout=120)
+        res[rank] = (g, frames)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    full = (np.arange(6) * sum(range(1, 9))).tolist()
+    assert res[0][0] == full and res[1][0] == full
+    assert res[0][1] == [[0.0] * 4, [1.0] * 4] and res[1][1] is None

@@ -16,8 +16,10 @@ RTOL, ATOL = 1e-5, 1e-6
 
 
 def gpu_inputs(vol, precision):
-    """Oracle-side float copies of exactly the values the GPU reads."""
-    if precision == 0:
+    """Oracle-side float copies of exactly the values the GPU reads
+    (precisions 0 and 3 store fp16 density, all store 8-bit albedo scaled by
+    the fp32 constant 1/255)."""
+    if precision in (0, 3):
         den = vol.density.astype(np.float16).astype(np.float32)
         alb = vol.albedo_u8.astype(np.float32) * np.float32(1.0 / 255.0)
     else:
@@ -41,7 +43,7 @@ def compare_radiance(g, ref, ns_g, ns_ref):
     return int(real.sum()), int(tie.sum()), float((err / (np.abs(ref) + ATOL)).max())
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2, 3])
 def test_forward_matches_fp64_oracle(yoxel_mod, oracle, precision):
     import torch
     vol = yoxel_mod.BrickVolume.noise(2, 0.4, 1.4, 21)
@@ -101,11 +103,28 @@ def test_samples_and_bricks_counters(yoxel_mod, oracle):
     assert ns.sum() > 0
 
 
-def test_backward_matches_fp64_adjoint(yoxel_mod, oracle):
+def test_pack_volume_bit_exact(yoxel_mod):
     import torch
     vol = yoxel_mod.BrickVolume.noise(1, 0.4, 1.4, 3)
     tv = vol.to_torch()
-    desc = yoxel_mod.torch_desc(tv)
+    p = yoxel_mod.pack_volume(tv["density"], tv["albedo"])
+    torch.cuda.synchronize()
+    ref = np.concatenate([tv["albedo"].cpu().numpy().reshape(-1, 3),
+                          tv["density"].cpu().numpy().reshape(-1, 1)], axis=1)
+    assert p.shape == (vol.nbricks, 729, 4)
+    assert np.array_equal(p.cpu().numpy().reshape(-1, 4).view(np.uint32), ref.view(np.uint32))
+
+
+@pytest.mark.parametrize("packed", [False, True])
+def test_backward_matches_fp64_adjoint(yoxel_mod, oracle, packed):
+    import torch
+    vol = yoxel_mod.BrickVolume.noise(1, 0.4, 1.4, 3)
+    tv = vol.to_torch()
+    if packed:
+        pk = yoxel_mod.pack_volume(tv["density"], tv["albedo"])
+        desc = yoxel_mod.torch_desc(tv, packed=pk)
+    else:
+        desc = yoxel_mod.torch_desc(tv)
     w, h = 40, 32
     cams = [cam_at([1.6, 1.3, 1.1]), cam_at([-0.8, 0.3, 0.2], 45.0)]
     rgba = yoxel_mod.render_volume(desc, cams, w, h, alpha_scale=2.0)

@@ -152,8 +152,7 @@ yv_status yv_batch_add_svo(yv_batch* b, const yv_renderer* r, void* d_rgba) {
   if ((int)b->items.size() >= kMaxBatchItems) return YV_ERR_UNSUPPORTED;
   yv_renderer_view v;
   if (!renderer_view(r, &v)) return YV_ERR_NO_SCENE;
-  BatchItem it;
-  std::memset(&it, 0, sizeof(it));
+  BatchItem it{};
   it.kind = kBatchSvo;
   it.width = v.fa.width;
   it.height = v.fa.height;
@@ -172,12 +171,13 @@ yv_status yv_batch_add_volume(yv_batch* b, const yv_volume_device* vol, const yv
                               float* d_rgba) {
   if (!b || !vol || !cam || !mp || !d_rgba || width <= 0 || height <= 0 || !vol->grids ||
       vol->levels < 1 || vol->levels > 5 || !(mp->step_vox > 0.f) ||
-      !(cam->fov_deg > 0.f && cam->fov_deg < 180.f))
+      !(cam->fov_deg > 0.f && cam->fov_deg < 180.f) || vol->precision < YV_PRECISION_F16 ||
+      vol->precision > YV_PRECISION_F16_PACKED || (vol->nbricks && !vol->albedo) ||
+      (vol->nbricks && vol->precision < YV_PRECISION_F32_PACKED && !vol->density))
     return YV_ERR_INVALID_ARG;
   if ((int)b->items.size() >= kMaxBatchItems) return YV_ERR_UNSUPPORTED;
-  BatchItem it;
-  std::memset(&it, 0, sizeof(it));
-  it.kind = vol->precision == YV_PRECISION_F16 ? kBatchBrickF16 : kBatchBrickF32;
+  BatchItem it{};
+  it.kind = kBatchBrick;
   it.width = width;
   it.height = height;
   it.tiles_x = (uint32_t)((width + 7) / 8);

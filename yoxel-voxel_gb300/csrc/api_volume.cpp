@@ -57,8 +57,12 @@ uint16_t f32_to_f16(float f) {
 bool fill_args(const yv_volume_device* v, const yv_march_params* mp, int width, int height,
                VolumeArgs* a) {
   if (!v || !mp || !v->grids || v->levels < 1 || v->levels > 5 || width <= 0 || height <= 0 ||
-      !(mp->step_vox > 0.f) || !std::isfinite(mp->alpha_scale))
+      !(mp->step_vox > 0.f) || !std::isfinite(mp->alpha_scale) ||
+      v->precision < YV_PRECISION_F16 || v->precision > YV_PRECISION_F16_PACKED)
     return false;
+  // packed formats keep the whole lattice point in the albedo buffer
+  const bool packed = v->precision >= YV_PRECISION_F32_PACKED;
+  if (v->nbricks && (!v->albedo || (!packed && !v->density))) return false;
   std::memset(a, 0, sizeof(*a));
   a->v.grids = v->grids;
   a->v.ngrids = v->ngrids;
@@ -106,7 +110,7 @@ bool cams_ok(const yv_camera* c, int n) {
 extern "C" {
 
 yv_status yv_volume_upload(const yv_volume_host* v, int32_t precision, yv_volume_gpu** out) {
-  if (!v || !out || (precision != YV_PRECISION_F16 && precision != YV_PRECISION_F32))
+  if (!v || !out || precision < YV_PRECISION_F16 || precision > YV_PRECISION_F16_PACKED)
     return YV_ERR_INVALID_ARG;
   *out = nullptr;
   yv_volume_gpu* g = new (std::nothrow) yv_volume_gpu();
@@ -142,7 +146,7 @@ yv_status yv_volume_upload(const yv_volume_host* v, int32_t precision, yv_volume
       abuf[i * 4 + 2] = alb[i * 3 + 2];
       abuf[i * 4 + 3] = 255;
     }
-  } else {
+  } else if (precision == YV_PRECISION_F32) {
     dbytes = n * 4;
     abytes = n * 12;
     dbuf.resize(dbytes);
@@ -150,6 +154,27 @@ yv_status yv_volume_upload(const yv_volume_host* v, int32_t precision, yv_volume
     std::memcpy(dbuf.data(), den, dbytes);
     float* af = reinterpret_cast<float*>(abuf.data());
     for (size_t i = 0; i < n * 3; ++i) af[i] = (float)alb[i] * (1.0f / 255.0f);
+  } else if (precision == YV_PRECISION_F32_PACKED) {
+    // float4 (r, g, b, density) per lattice point; no separate density array
+    dbytes = 0;
+    abytes = n * 16;
+    abuf.resize(abytes);
+    float* af = reinterpret_cast<float*>(abuf.data());
+    for (size_t i = 0; i < n; ++i) {
+      for (int c = 0; c < 3; ++c) af[i * 4 + (size_t)c] = (float)alb[i * 3 + (size_t)c] * (1.0f / 255.0f);
+      af[i * 4 + 3] = den[i];
+    }
+  } else {
+    // 8 bytes per lattice point: {fp16 density | r << 16 | g << 24, b}
+    dbytes = 0;
+    abytes = n * 8;
+    abuf.resize(abytes);
+    uint32_t* au = reinterpret_cast<uint32_t*>(abuf.data());
+    for (size_t i = 0; i < n; ++i) {
+      au[i * 2] = (uint32_t)f32_to_f16(den[i]) | ((uint32_t)alb[i * 3] << 16) |
+                  ((uint32_t)alb[i * 3 + 1] << 24);
+      au[i * 2 + 1] = (uint32_t)alb[i * 3 + 2];
+    }
   }
   const void* src[5] = {grids, dbuf.data(), abuf.data(), yv_volume_neighbors(v, 1),
                         yv_volume_neighbors(v, 0)};
@@ -194,8 +219,7 @@ yv_status yv_volume_render(const yv_volume_device* vol, const yv_camera* cams, i
                            uint32_t* samples, uint32_t* bricks, void* stream) {
   VolumeArgs* a = new (std::nothrow) VolumeArgs;
   if (!a) return YV_ERR_OUT_OF_MEMORY;
-  if (!fill_args(vol, mp, width, height, a) || !cams_ok(cams, ncams) || !rgba ||
-      !vol->density || !vol->albedo) {
+  if (!fill_args(vol, mp, width, height, a) || !cams_ok(cams, ncams) || !rgba) {
     delete a;
     return YV_ERR_INVALID_ARG;
   }
@@ -223,7 +247,8 @@ yv_status yv_volume_backward(const yv_volume_device* vol, const yv_camera* cams,
   VolumeArgs* a = new (std::nothrow) VolumeArgs;
   if (!a) return YV_ERR_OUT_OF_MEMORY;
   if (!fill_args(vol, mp, width, height, a) || !cams_ok(cams, ncams) || !rgba || !grad_rgba ||
-      !grad_density || !grad_albedo || vol->precision != YV_PRECISION_F32) {
+      !grad_density || !grad_albedo ||
+      (vol->precision != YV_PRECISION_F32 && vol->precision != YV_PRECISION_F32_PACKED)) {
     delete a;
     return YV_ERR_INVALID_ARG;
   }
@@ -274,7 +299,9 @@ yv_status yv_volume_fold_aprons(const yv_volume_device* vol, float* grad_density
 
 yv_status yv_volume_sync_aprons(const yv_volume_device* vol, float* density, float* albedo,
                                 void* stream) {
-  if (!vol || !vol->nbr_up || vol->precision != YV_PRECISION_F32) return YV_ERR_INVALID_ARG;
+  if (!vol || !vol->nbr_up ||
+      (vol->precision != YV_PRECISION_F32 && vol->precision != YV_PRECISION_F32_PACKED))
+    return YV_ERR_INVALID_ARG;
   VolumeArgs a;
   yv_march_params mp = {1.f, 1.f};
   if (!fill_args(vol, &mp, 1, 1, &a)) return YV_ERR_INVALID_ARG;
@@ -283,6 +310,16 @@ yv_status yv_volume_sync_aprons(const yv_volume_device* vol, float* density, flo
   if (density) e = launch_apron_fold(a, 1, density, false, s);
   if (e == cudaSuccess && albedo) e = launch_apron_fold(a, 3, albedo, false, s);
   return e == cudaSuccess ? YV_OK : fail(e, "apron sync");
+}
+
+yv_status yv_volume_pack(const float* density, const float* albedo, uint32_t npoints,
+                         float* packed, void* stream) {
+  if (!npoints) return YV_OK;
+  if (!density || !albedo || !packed || (reinterpret_cast<uintptr_t>(packed) & 15u))
+    return YV_ERR_INVALID_ARG;
+  cudaError_t e = launch_pack_f32(density, albedo, npoints, reinterpret_cast<float4*>(packed),
+                                  static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? YV_OK : fail(e, "volume pack");
 }
 
 }  // extern "C"

@@ -73,10 +73,12 @@ __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
           pixel_ray(it.vcam, x, y, o, d);
           NoVis nv;
           RayOut r;
-          if (it.kind == kBatchBrickF16)
-            march<0>(it.vol, nullptr, 0u, o, d, nv, r);
-          else
-            march<1>(it.vol, nullptr, 0u, o, d, nv, r);
+          switch (it.vol.precision) {
+            case 0: march<0>(it.vol, nullptr, 0u, o, d, nv, r); break;
+            case 1: march<1>(it.vol, nullptr, 0u, o, d, nv, r); break;
+            case 2: march<2>(it.vol, nullptr, 0u, o, d, nv, r); break;
+            default: march<3>(it.vol, nullptr, 0u, o, d, nv, r); break;
+          }
           if (r.bad) err |= YV_DEV_ERR_POOL;
           reinterpret_cast<float4*>(it.frgba)[off] = make_float4(r.c[0], r.c[1], r.c[2], r.a);
         }

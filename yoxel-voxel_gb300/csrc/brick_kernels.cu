@@ -72,14 +72,15 @@ __device__ __forceinline__ SampleGrad sample_grad(const VolumeArgs* a, const flo
   const float w = fmul(T, s.alpha);
   const float om = fsub(1.f, s.alpha);
   const float Cb[3] = {C0, C1, C2};
+  // one correctly rounded reciprocal instead of four divisions
+  const float inv_om = om > 0.f ? __frcp_rn(om) : 0.f;
   float dal = 0.f;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const float ck = k < 3 ? s.col[k] : 1.f;
     const float before = k < 3 ? Cb[k] : A;
     const float after = k < 3 ? ffma(w, ck, before) : fadd(A, w);
-    float term = fmul(T, ck);
-    if (om > 0.f) term = fsub(term, __fdiv_rn(fsub(out[k], after), om));
+    const float term = fsub(fmul(T, ck), fmul(fsub(out[k], after), inv_om));
     dal = ffma(g[k], term, dal);
   }
   const float sa = fmul(s.sigma, a->v.alpha_scale);
@@ -237,10 +238,13 @@ cudaError_t launch_volume_forward(const VolumeArgs& a, cudaStream_t s) {
   const uint32_t tiles = (uint32_t)a.ncams * (uint32_t)(((a.width + 7) >> 3) * ((a.height + 3) >> 2));
   const uint32_t blocks = (tiles + 7) / 8;
   if (blocks == 0) return cudaSuccess;
-  if (a.v.precision == 0)
-    volume_forward_kernel<0><<<blocks, 256, 0, s>>>(a);
-  else
-    volume_forward_kernel<1><<<blocks, 256, 0, s>>>(a);
+  switch (a.v.precision) {
+    case 0: volume_forward_kernel<0><<<blocks, 256, 0, s>>>(a); break;
+    case 1: volume_forward_kernel<1><<<blocks, 256, 0, s>>>(a); break;
+    case 2: volume_forward_kernel<2><<<blocks, 256, 0, s>>>(a); break;
+    case 3: volume_forward_kernel<3><<<blocks, 256, 0, s>>>(a); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 
@@ -249,8 +253,12 @@ cudaError_t launch_volume_backward(const VolumeArgs& a, cudaStream_t s) {
   const uint32_t blocks = (tiles + 7) / 8;
   if (blocks == 0) return cudaSuccess;
   // only fp32 (learnable) volumes have an adjoint
-  if (a.v.precision != 1) return cudaErrorInvalidValue;
-  volume_backward_kernel<1, kBackwardDirect, kBackwardMinBlocks><<<blocks, 256, 0, s>>>(a);
+  if (a.v.precision == 1)
+    volume_backward_kernel<1, kBackwardDirect, kBackwardMinBlocks><<<blocks, 256, 0, s>>>(a);
+  else if (a.v.precision == 2)
+    volume_backward_kernel<2, kBackwardDirect, kBackwardMinBlocks><<<blocks, 256, 0, s>>>(a);
+  else
+    return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 
@@ -279,6 +287,19 @@ cudaError_t launch_unpack_grads(const float4* packed, uint32_t n, float* grad_de
   if (n == 0) return cudaSuccess;
   unpack_grads_kernel<<<2 * device_sm_count_vol() * 8, 256, 0, s>>>(packed, n, grad_density,
                                                                      grad_albedo);
+  return cudaGetLastError();
+}
+
+__global__ void pack_f32_kernel(const float* __restrict__ d, const float* __restrict__ c,
+                                uint32_t n, float4* __restrict__ out) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[i] = make_float4(c[3 * (size_t)i], c[3 * (size_t)i + 1], c[3 * (size_t)i + 2], d[i]);
+}
+
+cudaError_t launch_pack_f32(const float* density, const float* albedo, uint32_t n,
+                            float4* packed, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  pack_f32_kernel<<<2 * device_sm_count_vol() * 8, 256, 0, s>>>(density, albedo, n, packed);
   return cudaGetLastError();
 }
 

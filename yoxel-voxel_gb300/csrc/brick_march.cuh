@@ -51,34 +51,62 @@ __device__ __forceinline__ float lerpf_(float a, float b, float t) { return ffma
 template <int P>
 struct Voxel;
 
-// precision 0: fp16 density, uchar4 albedo (interpolated as raw 0..255
-// values and scaled once after interpolation)
+// Lattice formats (VolumeView::precision).  corner() loads one lattice
+// point: density and the three albedo channels (raw 0..255 for the uint8
+// formats, scaled once after interpolation by kAlbedoScale).
+//   0: fp16 density array + uchar4 albedo array (two loads)
+//   1: fp32 density array + fp32 RGB albedo array (learnable; four loads)
+//   2: packed float4 (r, g, b, density) (one 16-byte load)
+//   3: packed 8 bytes {fp16 density | r << 16 | g << 24, b} (one 8-byte load)
 template <>
 struct Voxel<0> {
   static constexpr float kAlbedoScale = 1.0f / 255.0f;
-  __device__ static __forceinline__ float den(const void* p, uint32_t i) {
-    return __half2float(__ushort_as_half(__ldg(static_cast<const unsigned short*>(p) + i)));
-  }
-  __device__ static __forceinline__ void alb(const void* p, uint32_t i, float* c) {
-    const uint32_t v = __ldg(static_cast<const unsigned int*>(p) + i);
+  __device__ static __forceinline__ void corner(const VolumeView& a, uint32_t i, float& d,
+                                                float* c) {
+    d = __half2float(__ushort_as_half(__ldg(static_cast<const unsigned short*>(a.density) + i)));
+    const uint32_t v = __ldg(static_cast<const unsigned int*>(a.albedo) + i);
     c[0] = (float)(v & 0xFFu);
     c[1] = (float)((v >> 8) & 0xFFu);
     c[2] = (float)((v >> 16) & 0xFFu);
   }
 };
 
-// precision 1: fp32 density, fp32 RGB albedo (learnable)
 template <>
 struct Voxel<1> {
   static constexpr float kAlbedoScale = 1.0f;
-  __device__ static __forceinline__ float den(const void* p, uint32_t i) {
-    return __ldg(static_cast<const float*>(p) + i);
-  }
-  __device__ static __forceinline__ void alb(const void* p, uint32_t i, float* c) {
-    const float* q = static_cast<const float*>(p) + 3 * (size_t)i;
+  __device__ static __forceinline__ void corner(const VolumeView& a, uint32_t i, float& d,
+                                                float* c) {
+    d = __ldg(static_cast<const float*>(a.density) + i);
+    const float* q = static_cast<const float*>(a.albedo) + 3 * (size_t)i;
     c[0] = __ldg(q);
     c[1] = __ldg(q + 1);
     c[2] = __ldg(q + 2);
+  }
+};
+
+template <>
+struct Voxel<2> {
+  static constexpr float kAlbedoScale = 1.0f;
+  __device__ static __forceinline__ void corner(const VolumeView& a, uint32_t i, float& d,
+                                                float* c) {
+    const float4 v = __ldg(static_cast<const float4*>(a.albedo) + i);
+    c[0] = v.x;
+    c[1] = v.y;
+    c[2] = v.z;
+    d = v.w;
+  }
+};
+
+template <>
+struct Voxel<3> {
+  static constexpr float kAlbedoScale = 1.0f / 255.0f;
+  __device__ static __forceinline__ void corner(const VolumeView& a, uint32_t i, float& d,
+                                                float* c) {
+    const uint2 v = __ldg(static_cast<const uint2*>(a.albedo) + i);
+    d = __half2float(__ushort_as_half((unsigned short)(v.x & 0xFFFFu)));
+    c[0] = (float)((v.x >> 16) & 0xFFu);
+    c[1] = (float)(v.x >> 24);
+    c[2] = (float)(v.y & 0xFFu);
   }
 };
 
@@ -125,10 +153,9 @@ __device__ __forceinline__ void eval_sample(const VolumeView& a, int b, float lx
   float sig = 0.f, c0 = 0.f, c1 = 0.f, c2 = 0.f;
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
-    const uint32_t idx = s.base + corner_offset(j);
-    float c[3];
-    Voxel<P>::alb(a.albedo, idx, c);
-    sig = ffma(s.w[j], Voxel<P>::den(a.density, idx), sig);
+    float dj, c[3];
+    Voxel<P>::corner(a, s.base + corner_offset(j), dj, c);
+    sig = ffma(s.w[j], dj, sig);
     c0 = ffma(s.w[j], c[0], c0);
     c1 = ffma(s.w[j], c[1], c1);
     c2 = ffma(s.w[j], c[2], c2);

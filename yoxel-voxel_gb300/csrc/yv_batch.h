@@ -13,7 +13,7 @@ namespace yv {
 
 constexpr int kMaxBatchItems = 64;
 
-enum BatchKind : int32_t { kBatchSvo = 0, kBatchBrickF16 = 1, kBatchBrickF32 = 2 };
+enum BatchKind : int32_t { kBatchSvo = 0, kBatchBrick = 1 };  // brick: any VolumeView precision
 
 // One scene + camera of a batch.  Ray ids [id_base, id_base + 32*tiles) map
 // to the item's 8x4 pixel tiles.

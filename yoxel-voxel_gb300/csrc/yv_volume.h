@@ -22,8 +22,9 @@ struct VolumeView {
   uint32_t ngrids;
   int levels;
   int nb;                // brick cells per axis = 4^levels
-  const void* density;   // precision 0: fp16, 1: fp32 (nbricks*729)
-  const void* albedo;    // precision 0: uchar4, 1: fp32x3
+  const void* density;   // precision 0: fp16, 1: fp32 (nbricks*729); 2, 3: unused
+  const void* albedo;    // precision 0: uchar4, 1: fp32x3, 2: float4 (r,g,b,density),
+                         // 3: uint2 {fp16 density | r<<16 | g<<24, b}
   uint32_t nbricks;
   int precision;
   // march
@@ -54,6 +55,9 @@ struct VolumeArgs {
 
 cudaError_t launch_volume_forward(const VolumeArgs& a, cudaStream_t s);
 cudaError_t launch_volume_backward(const VolumeArgs& a, cudaStream_t s);
+// packed[i] = (albedo rgb, density) of n lattice points (fp32 layouts).
+cudaError_t launch_pack_f32(const float* density, const float* albedo, uint32_t n,
+                            float4* packed, cudaStream_t s);
 // grad_density += packed.w, grad_albedo += packed.xyz (n lattice points).
 cudaError_t launch_unpack_grads(const float4* packed, uint32_t n, float* grad_density,
                                 float* grad_albedo, cudaStream_t s);

@@ -9,10 +9,11 @@ from ._lib import YvError, LIB_PATH
 from .svo import SVOScene, NODE_DTYPE, ATTR_DTYPE
 from .renderer import Renderer, CudaRenderer
 from .volume import (BrickVolume, VolumeGPU, render_volume, volume_backward, volume_march,
-                     torch_desc, cameras, sphere_cameras)
+                     torch_desc, pack_volume, cameras, sphere_cameras)
 
 from .batch import Batch
 
 __all__ = ["SVOScene", "Renderer", "CudaRenderer", "YvError", "LIB_PATH", "Batch",
            "NODE_DTYPE", "ATTR_DTYPE", "BrickVolume", "VolumeGPU", "render_volume",
-           "volume_backward", "volume_march", "torch_desc", "cameras", "sphere_cameras"]
+           "volume_backward", "volume_march", "torch_desc", "pack_volume", "cameras",
+           "sphere_cameras"]

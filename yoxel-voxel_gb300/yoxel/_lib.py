@@ -84,6 +84,8 @@ class MarchParams(C.Structure):
 
 YV_PRECISION_F16 = 0
 YV_PRECISION_F32 = 1
+YV_PRECISION_F32_PACKED = 2
+YV_PRECISION_F16_PACKED = 3
 
 F3 = C.c_float * 3
 P = C.c_void_p
@@ -147,6 +149,7 @@ _SIGS = {
                                C.c_int32, C.c_int32, C.POINTER(MarchParams), P, P, P, P, P]),
     "yv_volume_fold_aprons": (S, [C.POINTER(VolumeDevice), P, P, P]),
     "yv_volume_sync_aprons": (S, [C.POINTER(VolumeDevice), P, P, P]),
+    "yv_volume_pack": (S, [P, P, C.c_uint32, P, P]),
     "yv_batch_create": (S, [C.POINTER(P)]),
     "yv_batch_destroy": (None, [P]),
     "yv_batch_clear": (S, [P]),

@@ -1,0 +1,78 @@
+"""Multi-GPU host logic: partitioning and the training exchange step.
+
+Rays are independent, so rendering shards with no data-path collective:
+every GPU holds a replica of the scene and renders its share - whole scenes
+of a batch (largest-first greedy on a cost estimate) or bands of 8x4-pixel
+tiles of one frame (contiguous ranges of equal estimated cost) - and the
+frames are gathered to one rank at the end.  The differentiable volume is
+data-parallel over cameras with one exchange step per iteration: a sum
+all-reduce of the density / albedo gradient tensors.  torch.distributed
+(NCCL on GPUs, gloo on CPUs) carries the gather and the all-reduce.
+"""
+import numpy as np
+
+
+def partition_scenes(costs, world):
+    """Scene indices per rank: greedy longest-processing-time assignment of
+    `costs` (e.g. pixels x depth) to `world` ranks.  Deterministic."""
+    order = sorted(range(len(costs)), key=lambda i: (-float(costs[i]), i))
+    load = [0.0] * world
+    out = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        out[r].append(i)
+        load[r] += float(costs[i])
+    for lst in out:
+        lst.sort()
+    return out
+
+
+def partition_tiles(tile_costs, world):
+    """Contiguous [begin, end) tile ranges per rank with near-equal summed
+    cost (prefix-sum split); every tile is assigned exactly once."""
+    c = np.asarray(tile_costs, np.float64)
+    n = len(c)
+    if n == 0:
+        return [(0, 0)] * world
+    pref = np.concatenate([[0.0], np.cumsum(c)])
+    total = pref[-1]
+    bounds = [0]
+    for r in range(1, world):
+        target = total * r / world
+        k = int(np.searchsorted(pref, target, side="left"))
+        k = min(max(k, bounds[-1]), n)
+        bounds.append(k)
+    bounds.append(n)
+    return [(bounds[r], bounds[r + 1]) for r in range(world)]
+
+
+def partition_cameras(ncams, world):
+    """Contiguous camera ranges per rank (data parallelism over views)."""
+    base, extra = divmod(ncams, world)
+    out, start = [], 0
+    for r in range(world):
+        k = base + (1 if r < extra else 0)
+        out.append((start, start + k))
+        start += k
+    return out
+
+
+def sum_gradients(tensors, group=None):
+    """The exchange step of data-parallel training: in-place sum all-reduce."""
+    import torch.distributed as dist
+    for t in tensors:
+        dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+    return tensors
+
+
+def gather_to_root(tensor, world, rank, group=None):
+    """Gathers equally shaped per-rank tensors to rank 0 (list on rank 0,
+    None elsewhere)."""
+    import torch
+    import torch.distributed as dist
+    if rank == 0:
+        bufs = [torch.empty_like(tensor) for _ in range(world)]
+        dist.gather(tensor, gather_list=bufs, dst=0, group=group)
+        return bufs
+    dist.gather(tensor, dst=0, group=group)
+    return None

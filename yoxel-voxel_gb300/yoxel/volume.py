@@ -156,21 +156,43 @@ class VolumeGPU:
         return d
 
 
-def torch_desc(tv, density=None, albedo=None):
-    """VolumeDevice over torch tensors from BrickVolume.to_torch()."""
-    density = tv["density"] if density is None else density
-    albedo = tv["albedo"] if albedo is None else albedo
+def torch_desc(tv, density=None, albedo=None, packed=None):
+    """VolumeDevice over torch tensors from BrickVolume.to_torch(): fp32
+    density + albedo, or (packed given) the float4 (r, g, b, density) pool
+    that pack_volume() builds from them."""
     d = L.VolumeDevice()
     d.grids = tv["grids"].data_ptr()
     d.ngrids = tv["grids"].shape[0]
     d.levels = tv["levels"]
-    d.density = density.data_ptr()
-    d.albedo = albedo.data_ptr()
-    d.nbricks = density.shape[0]
-    d.precision = L.YV_PRECISION_F32
+    if packed is not None:
+        d.density = None
+        d.albedo = packed.data_ptr()
+        d.nbricks = packed.shape[0]
+        d.precision = L.YV_PRECISION_F32_PACKED
+    else:
+        density = tv["density"] if density is None else density
+        albedo = tv["albedo"] if albedo is None else albedo
+        d.density = density.data_ptr()
+        d.albedo = albedo.data_ptr()
+        d.nbricks = density.shape[0]
+        d.precision = L.YV_PRECISION_F32
     d.nbr_up = tv["nbr_up"].data_ptr()
     d.nbr_dn = tv["nbr_dn"].data_ptr()
     return d
+
+
+def pack_volume(density, albedo, out=None, stream=None):
+    """(nbricks, 729, 4) float32 CUDA tensor of (r, g, b, density) per lattice
+    point, from contiguous fp32 density (nbricks, 729) and albedo
+    (nbricks, 729, 3): one 16-byte load per trilinear corner in the march."""
+    torch = _torch()
+    nb = density.shape[0]
+    if out is None:
+        out = torch.empty((nb, 729, 4), dtype=torch.float32, device=density.device)
+    L.check(L.lib.yv_volume_pack(C.c_void_p(density.data_ptr()), C.c_void_p(albedo.data_ptr()),
+                                 nb * 729, C.c_void_p(out.data_ptr()), _stream(stream)),
+            "yv_volume_pack")
+    return out
 
 
 def cameras(cams):
@@ -236,26 +258,30 @@ def _make_function():
     torch = _torch()
 
     class VolumeMarch(torch.autograd.Function):
-        """rgba = march(density, albedo); backward re-marches each ray."""
+        """rgba = march(density, albedo); backward re-marches each ray.
+
+        The parameters are packed once per forward into the float4
+        (r, g, b, density) pool, which both passes read."""
 
         @staticmethod
         def forward(ctx, density, albedo, tv, cams, width, height, alpha_scale, step_vox):
             density = density.contiguous()
             albedo = albedo.contiguous()
-            desc = torch_desc(tv, density, albedo)
+            packed = pack_volume(density, albedo)
+            desc = torch_desc(tv, packed=packed)
             ca = cams if isinstance(cams, C.Array) else cameras(cams)
             rgba = render_volume(desc, ca, width, height, alpha_scale, step_vox)
-            ctx.save_for_backward(density, albedo, rgba)
-            ctx.meta = (tv, ca, width, height, alpha_scale, step_vox)
+            ctx.save_for_backward(packed, rgba)
+            ctx.meta = (tv, ca, width, height, alpha_scale, step_vox, density.shape, albedo.shape)
             return rgba
 
         @staticmethod
         def backward(ctx, grad_rgba):
-            density, albedo, rgba = ctx.saved_tensors
-            tv, ca, width, height, alpha_scale, step_vox = ctx.meta
-            gd = torch.zeros_like(density)
-            ga = torch.zeros_like(albedo)
-            desc = torch_desc(tv, density, albedo)
+            packed, rgba = ctx.saved_tensors
+            tv, ca, width, height, alpha_scale, step_vox, dshape, ashape = ctx.meta
+            gd = torch.zeros(dshape, dtype=torch.float32, device=packed.device)
+            ga = torch.zeros(ashape, dtype=torch.float32, device=packed.device)
+            desc = torch_desc(tv, packed=packed)
             volume_backward(desc, ca, width, height, rgba, grad_rgba.contiguous(), gd, ga,
                             alpha_scale, step_vox)
             return gd, ga, None, None, None, None, None, None
