@@ -46,14 +46,18 @@ __device__ __forceinline__ float max3f(float a, float b, float c) {
   float m = a > b ? a : b;  // max_vec_float3 order
   return m > c ? m : c;
 }
-__device__ __forceinline__ float min3f(float a, float b, float c) {
-  float m = a < b ? a : b;
-  return m < c ? m : c;
+// Minimum / maximum for the comparisons of the traversal (slab values are
+// never NaN; +0 and -0 compare equal, so the choice between them is moot).
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+  return fminf(fminf(a, b), c);
+}
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+  return fmaxf(fmaxf(a, b), c);
 }
 
 // FindFirstChild (cell/spu/trace_spu.cpp:48-68).
 __device__ __forceinline__ uint32_t ffc(Box& t) {
-  const float te = max3f(t.x1, t.y1, t.z1);
+  const float te = fmax3(t.x1, t.y1, t.z1);
   uint32_t ch = 0;
   float tm = __fmul_rn(0.5f, __fadd_rn(t.x1, t.x2));
   if (te > tm) { ch |= 1u; t.x1 = tm; } else { t.x2 = tm; }
@@ -125,13 +129,16 @@ __device__ __forceinline__ void fetch_node(const SvoDeviceScene& sc, const uint4
   }
 }
 
-// One stack frame: the node of a level, the child taken and that child's
-// slab box, exactly as RecTrace holds them in its activation record.
+// One stack frame: a level whose current child still has a next sibling
+// along the ray - the node, the child taken and that child's slab box,
+// exactly as RecTrace holds them in its activation record - and the level.
+// Levels whose current child is the last one the ray crosses are never
+// pushed: returning to them would only return further.
 struct __align__(16) Frame {
   uint32_t idch;  // node << 3 | ch
   float x1, y1, z1;
   float x2, y2, z2;
-  uint32_t pad;
+  uint32_t level;
 };
 
 enum : uint32_t { kIdle = 0, kPrimary = 1, kShadow = 2, kDone = 3 };
@@ -139,11 +146,12 @@ enum : int { kContinue = 0, kHit = 1, kMiss = 2 };
 
 // Traversal state of one lane.
 struct Trace {
-  uint32_t node, ch, df, steps, fetches;
+  uint32_t node, ch, df, steps, fetches, sp;
   int level;
   Box t;
   uint4 na, nb;
 };
+
 
 // SetupTrace (reaction/report/voxel.tex:312-326) + RecTrace entry test
 // (cell/ppu_renderer.cpp:20-21) + the root fetch.  False: the ray misses.
@@ -164,9 +172,9 @@ __device__ __forceinline__ bool begin_trace(const SvoDeviceScene& sc, const uint
   R.z1 = __fdiv_rn(__fsub_rn(0.f, pz), dz);
   R.z2 = __fdiv_rn(__fsub_rn(1.f, pz), dz);
   tr.fetches = 0;
-  if (!(max3f(R.x1, R.y1, R.z1) < min3f(R.x2, R.y2, R.z2))) return false;
+  if (!(fmax3(R.x1, R.y1, R.z1) < fmin3(R.x2, R.y2, R.z2))) return false;
   const uint32_t root = sc.root_word;
-  if ((root & (YV_DW_NULL | YV_DW_LEAF)) || min3f(R.x2, R.y2, R.z2) <= 0.f) return false;
+  if ((root & (YV_DW_NULL | YV_DW_LEAF)) || fmin3(R.x2, R.y2, R.z2) <= 0.f) return false;
   if (root >= sc.n_nodes) {
     err |= YV_DEV_ERR_POOL;
     return false;
@@ -174,6 +182,7 @@ __device__ __forceinline__ bool begin_trace(const SvoDeviceScene& sc, const uint
   tr.node = root;
   tr.df = df;
   tr.level = 0;
+  tr.sp = 0;
   tr.steps = 0;
   tr.fetches = 1;
   fetch_node<kRef>(sc, sm, nsm, root, tr.na, tr.nb);
@@ -182,9 +191,22 @@ __device__ __forceinline__ bool begin_trace(const SvoDeviceScene& sc, const uint
   return true;
 }
 
+// True when GoNext would find a next sibling (its exit axis, same tie
+// order, is not yet set in ch).
+__device__ __forceinline__ bool has_next(uint32_t ch, const Box& t) {
+  int e;
+  if (t.x2 > t.y2)
+    e = (t.y2 < t.z2) ? 1 : 2;
+  else
+    e = (t.x2 < t.z2) ? 0 : 2;
+  return !((ch >> e) & 1u);
+}
+
 // One step of RecTrace: test the current child (leaf -> hit, subtree ->
-// descend), else move to the next sibling, popping finished levels.
-template <bool kCull, bool kRef>
+// descend), else move to the next sibling, else return to the nearest
+// pushed level (whose next sibling then exists by construction).
+// kStack: frames of the per-lane stack.
+template <bool kCull, bool kRef, int kStack = YV_MAX_DEPTH>
 __device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint4* sm,
                                           uint32_t nsm, Frame* stk, Trace& tr, uint32_t& leaf,
                                           uint32_t& err) {
@@ -194,12 +216,13 @@ __device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint4*
   }
   const uint32_t c = tr.ch ^ tr.df;
   const uint32_t w = sel_child(tr.na, tr.nb, c);
+  const bool ahead = fmin3(tr.t.x2, tr.t.y2, tr.t.z2) > 0.f;
   if (w & YV_DW_LEAF) {
-    if (!kCull || min3f(tr.t.x2, tr.t.y2, tr.t.z2) > 0.f) {
+    if (!kCull || ahead) {
       leaf = w & 0x7FFFFFFFu;
       return kHit;
     }
-  } else if (!(w & YV_DW_NULL) && min3f(tr.t.x2, tr.t.y2, tr.t.z2) > 0.f) {
+  } else if (!(w & YV_DW_NULL) && ahead) {
     // descend: the recursive call of cell/ppu_renderer.cpp:34
     if (tr.level + 1 >= YV_MAX_DEPTH) {
       err |= YV_DEV_ERR_DEPTH;
@@ -209,12 +232,18 @@ __device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint4*
       err |= YV_DEV_ERR_POOL;
       return kMiss;
     }
-    Frame f;
-    f.idch = (tr.node << 3) | tr.ch;
-    f.x1 = tr.t.x1; f.y1 = tr.t.y1; f.z1 = tr.t.z1;
-    f.x2 = tr.t.x2; f.y2 = tr.t.y2; f.z2 = tr.t.z2;
-    f.pad = 0;
-    stk[tr.level] = f;
+    if (has_next(tr.ch, tr.t)) {
+      if (tr.sp >= (uint32_t)kStack) {
+        err |= YV_DEV_ERR_DEPTH;
+        return kMiss;
+      }
+      Frame f;
+      f.idch = (tr.node << 3) | tr.ch;
+      f.x1 = tr.t.x1; f.y1 = tr.t.y1; f.z1 = tr.t.z1;
+      f.x2 = tr.t.x2; f.y2 = tr.t.y2; f.z2 = tr.t.z2;
+      f.level = (uint32_t)tr.level;
+      stk[tr.sp++] = f;
+    }
     ++tr.level;
     tr.node = w;
     fetch_node<kRef>(sc, sm, nsm, w, tr.na, tr.nb);
@@ -223,20 +252,16 @@ __device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint4*
     return kContinue;
   }
   if (go_next(tr.ch, tr.t)) return kContinue;
-  // this level is exhausted: return to the parents until one has a next child
-  while (tr.level > 0) {
-    --tr.level;
-    const Frame f = stk[tr.level];
-    tr.ch = f.idch & 7u;
-    tr.t.x1 = f.x1; tr.t.y1 = f.y1; tr.t.z1 = f.z1;
-    tr.t.x2 = f.x2; tr.t.y2 = f.y2; tr.t.z2 = f.z2;
-    if (go_next(tr.ch, tr.t)) {
-      tr.node = f.idch >> 3;
-      fetch_node<kRef>(sc, sm, nsm, tr.node, tr.na, tr.nb);
-      return kContinue;
-    }
-  }
-  return kMiss;
+  if (tr.sp == 0) return kMiss;
+  const Frame f = stk[--tr.sp];
+  tr.ch = f.idch & 7u;
+  tr.node = f.idch >> 3;
+  tr.level = (int)f.level;
+  tr.t.x1 = f.x1; tr.t.y1 = f.y1; tr.t.z1 = f.z1;
+  tr.t.x2 = f.x2; tr.t.y2 = f.y2; tr.t.z2 = f.z2;
+  go_next(tr.ch, tr.t);
+  fetch_node<kRef>(sc, sm, nsm, tr.node, tr.na, tr.nb);
+  return kContinue;
 }
 
 // Per-pixel ray direction (cell/ppu_renderer.cpp:56) + AdjustDir (eps 1e-5).
