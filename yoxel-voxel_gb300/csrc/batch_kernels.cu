@@ -62,8 +62,8 @@ __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
         off = (uint32_t)y * (uint32_t)it.width + (uint32_t)x;
         if (it.kind == kBatchSvo) {
           pixel_dir(it.fa, x, y, dx, dy, dz);
-          if (begin_trace<false>(it.svo, nullptr, 0u, it.fa.pos[0], it.fa.pos[1], it.fa.pos[2],
-                                 dx, dy, dz, tr, err)) {
+          if (begin_trace(it.svo, it.fa.pos[0], it.fa.pos[1], it.fa.pos[2], dx, dy, dz, tr,
+                          err)) {
             mode = kPrimary;
           } else {
             write_pixel(it.fa, off, 0u, 0xFFFFFFFFu, 0.f, tr.fetches, 0u);
@@ -89,9 +89,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
 
     const BatchItem& it = items[item];
     uint32_t leaf = 0;
-    const int r = mode == kPrimary
-                      ? trace_step<false, false>(it.svo, nullptr, 0u, stk, tr, leaf, err)
-                      : trace_step<true, false>(it.svo, nullptr, 0u, stk, tr, leaf, err);
+    const int r = trace_step<false>(it.svo, nullptr, 0u, stk, tr, mode == kShadow, leaf, err);
     if (r == kContinue) continue;
     if (mode == kPrimary) {
       if (r == kMiss) {
@@ -123,8 +121,8 @@ __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
       const float half = __int_as_float((127 - (tr.level + 2)) << 23);
       const float d_off = ((tr.df >> e) & 1u) ? half : -half;
       o[e] = __fadd_rn(o[e], d_off);
-      if (begin_trace<false>(it.svo, nullptr, 0u, o[0], o[1], o[2], it.fa.light_ray[0],
-                             it.fa.light_ray[1], it.fa.light_ray[2], tr, err)) {
+      if (begin_trace(it.svo, o[0], o[1], o[2], it.fa.light_ray[0], it.fa.light_ray[1],
+                      it.fa.light_ray[2], tr, err)) {
         mode = kShadow;
       } else {
         write_pixel(it.fa, off, shade(attr, it.fa, false), hitw, ht, fp, tr.fetches);

@@ -36,7 +36,7 @@
 namespace yv {
 namespace {
 
-constexpr uint32_t kStepCap = 1u << 20;
+constexpr uint32_t kFetchCap = 1u << 20;
 
 struct Box {
   float x1, y1, z1, x2, y2, z2;
@@ -94,39 +94,23 @@ __device__ __forceinline__ bool go_next(uint32_t& ch, Box& t) {
   return true;
 }
 
-__device__ __forceinline__ uint32_t sel_child(const uint4& a, const uint4& b, uint32_t c) {
-  const uint4 v = (c & 4u) ? b : a;
-  const uint32_t lo = (c & 1u) ? v.y : v.x;
-  const uint32_t hi = (c & 1u) ? v.w : v.z;
-  return (c & 2u) ? hi : lo;
-}
-
-// Node fetch.  kRef = false: the library's 32-byte device records (two
-// 128-bit loads, top levels from shared memory).  kRef = true: the
-// reference's 40-byte VoxNode {flags, data, child[8]} read in place (five
-// 64-bit loads), its leaf / null flags folded into the same child words.
+// Child word c of node id, read where it lies at every step (the node's
+// sector stays in L1 while the ray is inside it, so the 8 words are not
+// held in registers).  kRef = false: the library's 32-byte device records
+// (top levels from shared memory).  kRef = true: the reference's 40-byte
+// VoxNode {flags, data, child[8]} read in place, its leaf / null flags
+// folded into the same word encoding.
 template <bool kRef>
-__device__ __forceinline__ void fetch_node(const SvoDeviceScene& sc, const uint4* sm,
-                                           uint32_t nsm, uint32_t id, uint4& a, uint4& b) {
+__device__ __forceinline__ uint32_t child_word(const SvoDeviceScene& sc, const uint32_t* sm,
+                                               uint32_t nsm, uint32_t id, uint32_t c) {
   if (kRef) {
-    const uint2* p = reinterpret_cast<const uint2*>(sc.nodes) + 5 * (size_t)id;
-    const uint2 q0 = __ldg(p), q1 = __ldg(p + 1), q2 = __ldg(p + 2), q3 = __ldg(p + 3),
-                q4 = __ldg(p + 4);
-    const uint32_t fl = q0.x;
-    uint32_t c[8] = {q1.x, q1.y, q2.x, q2.y, q3.x, q3.y, q4.x, q4.y};
-#pragma unroll
-    for (int i = 0; i < 8; ++i)
-      c[i] = ((fl >> i) & 1u) ? (YV_DW_LEAF | c[i]) : ((c[i] & 0x80000000u) ? YV_DW_NULL : c[i]);
-    a = make_uint4(c[0], c[1], c[2], c[3]);
-    b = make_uint4(c[4], c[5], c[6], c[7]);
-  } else if (id < nsm) {
-    a = sm[2 * id];
-    b = sm[2 * id + 1];
-  } else {
-    const uint4* p = sc.nodes + 2 * (size_t)id;
-    a = __ldg(p);
-    b = __ldg(p + 1);
+    const uint32_t* p = reinterpret_cast<const uint32_t*>(sc.nodes) + 10 * (size_t)id;
+    const uint32_t fl = __ldg(p);
+    const uint32_t cw = __ldg(p + 2 + c);
+    return ((fl >> c) & 1u) ? (YV_DW_LEAF | cw) : ((cw & 0x80000000u) ? YV_DW_NULL : cw);
   }
+  if (id < nsm) return sm[8 * id + c];
+  return __ldg(reinterpret_cast<const uint32_t*>(sc.nodes) + 8 * (size_t)id + c);
 }
 
 // One stack frame: a level whose current child still has a next sibling
@@ -146,18 +130,15 @@ enum : int { kContinue = 0, kHit = 1, kMiss = 2 };
 
 // Traversal state of one lane.
 struct Trace {
-  uint32_t node, ch, df, steps, fetches, sp;
+  uint32_t node, ch, df, fetches, sp;
   int level;
   Box t;
-  uint4 na, nb;
 };
 
 
 // SetupTrace (reaction/report/voxel.tex:312-326) + RecTrace entry test
 // (cell/ppu_renderer.cpp:20-21) + the root fetch.  False: the ray misses.
-template <bool kRef>
-__device__ __forceinline__ bool begin_trace(const SvoDeviceScene& sc, const uint4* sm,
-                                            uint32_t nsm, float px, float py, float pz,
+__device__ __forceinline__ bool begin_trace(const SvoDeviceScene& sc, float px, float py, float pz,
                                             float dx, float dy, float dz, Trace& tr,
                                             uint32_t& err) {
   uint32_t df = 0;
@@ -183,9 +164,7 @@ __device__ __forceinline__ bool begin_trace(const SvoDeviceScene& sc, const uint
   tr.df = df;
   tr.level = 0;
   tr.sp = 0;
-  tr.steps = 0;
   tr.fetches = 1;
-  fetch_node<kRef>(sc, sm, nsm, root, tr.na, tr.nb);
   tr.t = R;
   tr.ch = ffc(tr.t);
   return true;
@@ -205,25 +184,29 @@ __device__ __forceinline__ bool has_next(uint32_t ch, const Box& t) {
 // One step of RecTrace: test the current child (leaf -> hit, subtree ->
 // descend), else move to the next sibling, else return to the nearest
 // pushed level (whose next sibling then exists by construction).
-// kStack: frames of the per-lane stack.
-template <bool kCull, bool kRef, int kStack = YV_MAX_DEPTH>
-__device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint4* sm,
-                                          uint32_t nsm, Frame* stk, Trace& tr, uint32_t& leaf,
-                                          uint32_t& err) {
-  if (++tr.steps > kStepCap) {
-    err |= YV_DEV_ERR_ITER;
-    return kMiss;
-  }
-  const uint32_t c = tr.ch ^ tr.df;
-  const uint32_t w = sel_child(tr.na, tr.nb, c);
+// cull (shadow rays): leaves that lie wholly behind the origin do not count.
+// It is a run-time flag so that the primary and shadow rays of one warp run
+// the same instructions.  kStack: frames of the per-lane stack.
+// A ray stops with YV_DEV_ERR_ITER after kFetchCap node fetches; every other
+// step advances a sibling or pops a pushed level, so the steps of a ray are
+// bounded by a small multiple of its fetches.
+template <bool kRef, int kStack = YV_MAX_DEPTH>
+__device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint32_t* sm,
+                                          uint32_t nsm, Frame* stk, Trace& tr, bool cull,
+                                          uint32_t& leaf, uint32_t& err) {
+  const uint32_t w = child_word<kRef>(sc, sm, nsm, tr.node, tr.ch ^ tr.df);
   const bool ahead = fmin3(tr.t.x2, tr.t.y2, tr.t.z2) > 0.f;
   if (w & YV_DW_LEAF) {
-    if (!kCull || ahead) {
+    if (!cull || ahead) {
       leaf = w & 0x7FFFFFFFu;
       return kHit;
     }
   } else if (!(w & YV_DW_NULL) && ahead) {
     // descend: the recursive call of cell/ppu_renderer.cpp:34
+    if (++tr.fetches > kFetchCap) {
+      err |= YV_DEV_ERR_ITER;
+      return kMiss;
+    }
     if (tr.level + 1 >= YV_MAX_DEPTH) {
       err |= YV_DEV_ERR_DEPTH;
       return kMiss;
@@ -246,8 +229,6 @@ __device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint4*
     }
     ++tr.level;
     tr.node = w;
-    fetch_node<kRef>(sc, sm, nsm, w, tr.na, tr.nb);
-    ++tr.fetches;
     tr.ch = ffc(tr.t);
     return kContinue;
   }
@@ -260,7 +241,6 @@ __device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint4*
   tr.t.x1 = f.x1; tr.t.y1 = f.y1; tr.t.z1 = f.z1;
   tr.t.x2 = f.x2; tr.t.y2 = f.y2; tr.t.z2 = f.z2;
   go_next(tr.ch, tr.t);
-  fetch_node<kRef>(sc, sm, nsm, tr.node, tr.na, tr.nb);
   return kContinue;
 }
 
@@ -327,6 +307,7 @@ __global__ void __launch_bounds__(256, kMinBlocks)
   extern __shared__ uint4 smem[];
   for (uint32_t i = threadIdx.x; i < 2 * nsm; i += blockDim.x) smem[i] = __ldg(sc.nodes + i);
   __syncthreads();
+  const uint32_t* smw = reinterpret_cast<const uint32_t*>(smem);
 
   Frame stk[YV_MAX_DEPTH];
   const uint32_t lane = threadIdx.x & 31u;
@@ -345,8 +326,7 @@ __global__ void __launch_bounds__(256, kMinBlocks)
   for (;;) {
     // ---- refill idle lanes from the global ray counter ----
     const uint32_t idle = __ballot_sync(0xFFFFFFFFu, mode == kIdle);
-    const uint32_t busy = __ballot_sync(0xFFFFFFFFu, mode == kPrimary || mode == kShadow);
-    if (idle && (__popc(idle) >= (int)refill_min || busy == 0)) {
+    if (idle) {
       const uint32_t leader = (uint32_t)__ffs(idle) - 1u;
       uint32_t base = 0;
       if (lane == leader) base = atomicAdd(&a.counters[0], (uint32_t)__popc(idle));
@@ -362,7 +342,7 @@ __global__ void __launch_bounds__(256, kMinBlocks)
           if (x < a.width && y < a.height) {
             off = (uint32_t)y * (uint32_t)a.width + (uint32_t)x;
             pixel_dir(a, x, y, dx, dy, dz);
-            if (begin_trace<kRef>(sc, smem, nsm, a.pos[0], a.pos[1], a.pos[2], dx, dy, dz, tr, err)) {
+            if (begin_trace(sc, a.pos[0], a.pos[1], a.pos[2], dx, dy, dz, tr, err)) {
               mode = kPrimary;
             } else {
               write_pixel(a, off, 0u, 0xFFFFFFFFu, 0.f, tr.fetches, 0u);
@@ -372,60 +352,60 @@ __global__ void __launch_bounds__(256, kMinBlocks)
       }
     }
     if (__all_sync(0xFFFFFFFFu, mode == kDone)) break;
-    if (mode != kPrimary && mode != kShadow) continue;
 
-    // ---- one traversal step ----
-    uint32_t leaf = 0;
-    const int r = mode == kPrimary
-                      ? trace_step<false, kRef>(sc, smem, nsm, stk, tr, leaf, err)
-                      : trace_step<true, kRef>(sc, smem, nsm, stk, tr, leaf, err);
-    if (r == kContinue) continue;
-    if (mode == kPrimary) {
-      if (r == kMiss) {
-        write_pixel(a, off, 0u, 0xFFFFFFFFu, 0.f, tr.fetches, 0u);
-        mode = kIdle;
-        continue;
+    // ---- trace until refill_min lanes (or all) are free ----
+    for (;;) {
+      if (mode == kPrimary || mode == kShadow) {
+        uint32_t leaf = 0;
+        const int r = trace_step<kRef>(sc, smw, nsm, stk, tr, mode == kShadow, leaf, err);
+        if (r != kContinue) {
+          if (mode == kShadow) {
+            // end of a shadow ray
+            const bool sh = r == kHit;
+            my_shadowed += sh ? 1u : 0u;
+            write_pixel(a, off, shade(attr, a, sh), hitw, ht, fp, tr.fetches);
+            mode = kIdle;
+          } else if (r == kMiss) {
+            write_pixel(a, off, 0u, 0xFFFFFFFFu, 0.f, tr.fetches, 0u);
+            mode = kIdle;
+          } else {
+            ++my_hits;
+            hitw = ((kRef ? tr.node : __ldg(sc.orig_id + tr.node)) << 3) | (tr.ch ^ tr.df);
+            ht = max3f(tr.t.x1, tr.t.y1, tr.t.z1);
+            fp = tr.fetches;
+            attr = make_uint2(0u, 0u);
+            if (leaf < sc.n_attrs)
+              attr = __ldg(sc.attrs + leaf);
+            else
+              err |= YV_DEV_ERR_POOL;
+            mode = kIdle;
+            if (a.shadows) {
+              // shadow ray: the hit point moved half a leaf out through the entry face
+              float o[3];
+              o[0] = __fadd_rn(a.pos[0], __fmul_rn(dx, ht));
+              o[1] = __fadd_rn(a.pos[1], __fmul_rn(dy, ht));
+              o[2] = __fadd_rn(a.pos[2], __fmul_rn(dz, ht));
+              int e = 0;
+              float m = tr.t.x1;
+              if (tr.t.y1 > m) { e = 1; m = tr.t.y1; }
+              if (tr.t.z1 > m) e = 2;
+              const float half = __int_as_float((127 - (tr.level + 2)) << 23);
+              const float d_off = ((tr.df >> e) & 1u) ? half : -half;
+              o[e] = __fadd_rn(o[e], d_off);
+              if (begin_trace(sc, o[0], o[1], o[2], a.light_ray[0], a.light_ray[1],
+                              a.light_ray[2], tr, err))
+                mode = kShadow;
+              else
+                write_pixel(a, off, shade(attr, a, false), hitw, ht, fp, tr.fetches);
+            } else {
+              write_pixel(a, off, shade(attr, a, false), hitw, ht, fp, 0u);
+            }
+          }
+        }
       }
-      ++my_hits;
-      hitw = ((kRef ? tr.node : __ldg(sc.orig_id + tr.node)) << 3) | (tr.ch ^ tr.df);
-      ht = max3f(tr.t.x1, tr.t.y1, tr.t.z1);
-      fp = tr.fetches;
-      attr = make_uint2(0u, 0u);
-      if (leaf < sc.n_attrs)
-        attr = __ldg(sc.attrs + leaf);
-      else
-        err |= YV_DEV_ERR_POOL;
-      if (!a.shadows) {
-        write_pixel(a, off, shade(attr, a, false), hitw, ht, fp, 0u);
-        mode = kIdle;
-        continue;
-      }
-      // shadow ray: the hit point moved half a leaf out through the entry face
-      float o[3];
-      o[0] = __fadd_rn(a.pos[0], __fmul_rn(dx, ht));
-      o[1] = __fadd_rn(a.pos[1], __fmul_rn(dy, ht));
-      o[2] = __fadd_rn(a.pos[2], __fmul_rn(dz, ht));
-      int e = 0;
-      float m = tr.t.x1;
-      if (tr.t.y1 > m) { e = 1; m = tr.t.y1; }
-      if (tr.t.z1 > m) e = 2;
-      const float half = __int_as_float((127 - (tr.level + 2)) << 23);
-      const float d_off = ((tr.df >> e) & 1u) ? half : -half;
-      o[e] = __fadd_rn(o[e], d_off);
-      if (begin_trace<kRef>(sc, smem, nsm, o[0], o[1], o[2], a.light_ray[0], a.light_ray[1],
-                      a.light_ray[2], tr, err)) {
-        mode = kShadow;
-      } else {
-        write_pixel(a, off, shade(attr, a, false), hitw, ht, fp, tr.fetches);
-        mode = kIdle;
-      }
-      continue;
+      const uint32_t free_lanes = __ballot_sync(0xFFFFFFFFu, mode == kIdle || mode == kDone);
+      if (free_lanes == 0xFFFFFFFFu || __popc(free_lanes) >= (int)refill_min) break;
     }
-    // end of a shadow ray
-    const bool sh = r == kHit;
-    my_shadowed += sh ? 1u : 0u;
-    write_pixel(a, off, shade(attr, a, sh), hitw, ht, fp, tr.fetches);
-    mode = kIdle;
   }
 
   // block totals of the counters, one atomic per block and counter
