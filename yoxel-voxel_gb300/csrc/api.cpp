@@ -8,6 +8,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "yv_batch.h"
 #include "yv_internal.h"
@@ -29,7 +30,7 @@ struct yv_renderer {
   // device scene
   uint32_t* d_words = nullptr;
   uint32_t* d_orig = nullptr;
-  yv_leaf_attr* d_attrs = nullptr;
+  uint4* d_attrs = nullptr;  // shading records, 16 B per leaf
   SvoDeviceScene scene;
   bool has_scene = false;
   uint64_t scene_bytes = 0;
@@ -147,17 +148,36 @@ yv_status yv_set_scene_svo(yv_renderer* r, const yv_vox_node* nodes,
             "upload ids");
   }
   if (nattrs) {
-    YV_CUDA(cudaMalloc(&r->d_attrs, (size_t)nattrs * 8u), "cudaMalloc(attrs)");
-    YV_CUDA(cudaMemcpy(r->d_attrs, attrs, (size_t)nattrs * 8u, cudaMemcpyHostToDevice),
+    // Per leaf: RGBA8 + the unit normal, normalised here once with the
+    // same FP32 operations the shading of every hit would repeat.
+    std::vector<uint32_t> rec((size_t)nattrs * 4u);
+    for (uint32_t i = 0; i < nattrs; ++i) {
+      const yv_leaf_attr& at = attrs[i];
+      const float nx = (float)at.nx, ny = (float)at.ny, nz = (float)at.nz;
+      const float len2 = nx * nx + ny * ny + nz * nz;
+      float u[3] = {0.f, 0.f, 0.f};
+      if (len2 > 0.f) {
+        const float len = std::sqrt(len2);
+        u[0] = nx / len;
+        u[1] = ny / len;
+        u[2] = nz / len;
+      }
+      uint32_t* q = &rec[(size_t)i * 4u];
+      q[0] = (uint32_t)at.r | ((uint32_t)at.g << 8) | ((uint32_t)at.b << 16) |
+             ((uint32_t)at.a << 24);
+      std::memcpy(q + 1, u, 12);
+    }
+    YV_CUDA(cudaMalloc(&r->d_attrs, (size_t)nattrs * 16u), "cudaMalloc(attrs)");
+    YV_CUDA(cudaMemcpy(r->d_attrs, rec.data(), (size_t)nattrs * 16u, cudaMemcpyHostToDevice),
             "upload attrs");
   }
   r->scene.nodes = reinterpret_cast<const uint4*>(r->d_words);
   r->scene.orig_id = r->d_orig;
-  r->scene.attrs = reinterpret_cast<const uint2*>(r->d_attrs);
+  r->scene.attrs = r->d_attrs;
   r->scene.n_nodes = (uint32_t)nn;
   r->scene.n_attrs = nattrs;
   r->scene.root_word = dl.root_word;
-  r->scene_bytes = (uint64_t)nn * 36u + (uint64_t)nattrs * 8u;
+  r->scene_bytes = (uint64_t)nn * 36u + (uint64_t)nattrs * 16u;
   r->has_scene = true;
   return YV_OK;
 }

@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
   float dx = 0.f, dy = 0.f, dz = 0.f;
   uint32_t hitw = 0xFFFFFFFFu, fp = 0;
   float ht = 0.f;
-  uint2 attr = make_uint2(0u, 0u);
+  uint4 attr = make_uint4(0u, 0u, 0u, 0u);
 
   for (;;) {
     const uint32_t busy = __ballot_sync(0xFFFFFFFFu, mode == kPrimary || mode == kShadow);
@@ -100,9 +100,9 @@ __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
       hitw = (__ldg(it.svo.orig_id + tr.node) << 3) | (tr.ch ^ tr.df);
       ht = max3f(tr.t.x1, tr.t.y1, tr.t.z1);
       fp = tr.fetches;
-      attr = make_uint2(0u, 0u);
+      attr = make_uint4(0u, 0u, 0u, 0u);
       if (leaf < it.svo.n_attrs)
-        attr = __ldg(it.svo.attrs + leaf);
+        attr = load_shading<false>(it.svo, leaf);
       else
         err |= YV_DEV_ERR_POOL;
       if (!it.fa.shadows) {

@@ -60,8 +60,8 @@ cudaError_t launch_svo_frame(const SvoDeviceScene& sc, const SvoFrameArgs& a,
   uint32_t refill = (uint32_t)(cfg.tile_rays <= 0 ? 32 : cfg.tile_rays);
   if (refill > 32) refill = 32;
   // register budget: blocks_per_sm 2 (up to 128 regs), 3 (80), 4 (64);
-  // 0 = default 4
-  const int mb = cfg.blocks_per_sm <= 0 ? 4 : (cfg.blocks_per_sm > 4 ? 4 : cfg.blocks_per_sm);
+  // 0 = default 3 (fastest on the 2048^3 and 256^3 frames)
+  const int mb = cfg.blocks_per_sm <= 0 ? 3 : (cfg.blocks_per_sm > 4 ? 4 : cfg.blocks_per_sm);
   cudaError_t e;
   if (mb <= 2)
     e = launch_with<2>(sc, a, bt, nsm, refill, 0, stream);

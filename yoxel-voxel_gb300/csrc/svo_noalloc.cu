@@ -85,7 +85,7 @@ extern "C" yv_status yv_render_svo_noalloc(const yv_vox_node* nodes, uint32_t co
   SvoDeviceScene sc;
   sc.nodes = reinterpret_cast<const uint4*>(nodes);  // read as 40-byte VoxNode records
   sc.orig_id = nullptr;
-  sc.attrs = reinterpret_cast<const uint2*>(attrs);
+  sc.attrs = attrs;
   sc.n_nodes = count;
   sc.n_attrs = nattrs;
   sc.root_word = (root & 0x80000000u) ? YV_DW_NULL : root;

@@ -68,16 +68,15 @@ __device__ __forceinline__ uint32_t ffc(Box& t) {
   return ch;
 }
 
-// GoNext (cell/spu/trace_spu.cpp:70-93), argmin tie order of :75-78.
-__device__ __forceinline__ bool go_next(uint32_t& ch, Box& t) {
-  int e;
-  if (t.x2 > t.y2)
-    e = (t.y2 < t.z2) ? 1 : 2;
-  else
-    e = (t.x2 < t.z2) ? 0 : 2;
-  const uint32_t mask = 1u << e;
-  if (ch & mask) return false;
-  ch ^= mask;
+// GoNext (cell/spu/trace_spu.cpp:70-93) in two parts: the exit axis (the
+// argmin tie order of :75-78) and the move into the sibling across it.
+__device__ __forceinline__ int exit_axis(const Box& t) {
+  if (t.x2 > t.y2) return (t.y2 < t.z2) ? 1 : 2;
+  return (t.x2 < t.z2) ? 0 : 2;
+}
+
+__device__ __forceinline__ void advance(uint32_t& ch, Box& t, int e) {
+  ch ^= 1u << e;
   if (e == 0) {
     const float dt = __fsub_rn(t.x2, t.x1);
     t.x1 = t.x2;
@@ -91,7 +90,6 @@ __device__ __forceinline__ bool go_next(uint32_t& ch, Box& t) {
     t.z1 = t.z2;
     t.z2 = __fadd_rn(t.z2, dt);
   }
-  return true;
 }
 
 // Child word c of node id, read where it lies at every step (the node's
@@ -170,27 +168,17 @@ __device__ __forceinline__ bool begin_trace(const SvoDeviceScene& sc, float px, 
   return true;
 }
 
-// True when GoNext would find a next sibling (its exit axis, same tie
-// order, is not yet set in ch).
-__device__ __forceinline__ bool has_next(uint32_t ch, const Box& t) {
-  int e;
-  if (t.x2 > t.y2)
-    e = (t.y2 < t.z2) ? 1 : 2;
-  else
-    e = (t.x2 < t.z2) ? 0 : 2;
-  return !((ch >> e) & 1u);
-}
-
 // One step of RecTrace: test the current child (leaf -> hit, subtree ->
-// descend), else move to the next sibling, else return to the nearest
-// pushed level (whose next sibling then exists by construction).
-// cull (shadow rays): leaves that lie wholly behind the origin do not count.
-// It is a run-time flag so that the primary and shadow rays of one warp run
-// the same instructions.  kStack: frames of the per-lane stack.
-// A ray stops with YV_DEV_ERR_ITER after kFetchCap node fetches; every other
-// step advances a sibling or pops a pushed level, so the steps of a ray are
-// bounded by a small multiple of its fetches.
-template <bool kRef, int kStack = YV_MAX_DEPTH>
+// descend), else move to the next sibling, first returning to the nearest
+// pushed level when this one is exhausted (that level's next sibling exists
+// by construction, so both cases share the move).
+// kRef (caller-supplied VoxNode pool): child refs are range-checked, depth
+// is capped at YV_MAX_DEPTH levels and a ray stops with YV_DEV_ERR_ITER after
+// kFetchCap fetches.  The library's own layout is validated acyclic, in
+// range and at most YV_MAX_DEPTH levels deep when it is built, so it needs
+// none of these.  In both cases a push happens at level < YV_MAX_DEPTH - 1,
+// so at most YV_MAX_DEPTH - 1 frames are ever held.
+template <bool kRef>
 __device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint32_t* sm,
                                           uint32_t nsm, Frame* stk, Trace& tr, bool cull,
                                           uint32_t& leaf, uint32_t& err) {
@@ -203,23 +191,22 @@ __device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint32
     }
   } else if (!(w & YV_DW_NULL) && ahead) {
     // descend: the recursive call of cell/ppu_renderer.cpp:34
-    if (++tr.fetches > kFetchCap) {
-      err |= YV_DEV_ERR_ITER;
-      return kMiss;
-    }
-    if (tr.level + 1 >= YV_MAX_DEPTH) {
-      err |= YV_DEV_ERR_DEPTH;
-      return kMiss;
-    }
-    if (w >= sc.n_nodes) {
-      err |= YV_DEV_ERR_POOL;
-      return kMiss;
-    }
-    if (has_next(tr.ch, tr.t)) {
-      if (tr.sp >= (uint32_t)kStack) {
+    if (kRef) {
+      if (tr.fetches >= kFetchCap) {
+        err |= YV_DEV_ERR_ITER;
+        return kMiss;
+      }
+      if (tr.level + 1 >= YV_MAX_DEPTH) {
         err |= YV_DEV_ERR_DEPTH;
         return kMiss;
       }
+      if (w >= sc.n_nodes) {
+        err |= YV_DEV_ERR_POOL;
+        return kMiss;
+      }
+    }
+    ++tr.fetches;
+    if (!((tr.ch >> exit_axis(tr.t)) & 1u)) {
       Frame f;
       f.idch = (tr.node << 3) | tr.ch;
       f.x1 = tr.t.x1; f.y1 = tr.t.y1; f.z1 = tr.t.z1;
@@ -232,15 +219,18 @@ __device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint32
     tr.ch = ffc(tr.t);
     return kContinue;
   }
-  if (go_next(tr.ch, tr.t)) return kContinue;
-  if (tr.sp == 0) return kMiss;
-  const Frame f = stk[--tr.sp];
-  tr.ch = f.idch & 7u;
-  tr.node = f.idch >> 3;
-  tr.level = (int)f.level;
-  tr.t.x1 = f.x1; tr.t.y1 = f.y1; tr.t.z1 = f.z1;
-  tr.t.x2 = f.x2; tr.t.y2 = f.y2; tr.t.z2 = f.z2;
-  go_next(tr.ch, tr.t);
+  int e = exit_axis(tr.t);
+  if ((tr.ch >> e) & 1u) {
+    if (tr.sp == 0) return kMiss;
+    const Frame f = stk[--tr.sp];
+    tr.ch = f.idch & 7u;
+    tr.node = f.idch >> 3;
+    tr.level = (int)f.level;
+    tr.t.x1 = f.x1; tr.t.y1 = f.y1; tr.t.z1 = f.z1;
+    tr.t.x2 = f.x2; tr.t.y2 = f.y2; tr.t.z2 = f.z2;
+    e = exit_axis(tr.t);
+  }
+  advance(tr.ch, tr.t, e);
   return kContinue;
 }
 
@@ -262,20 +252,37 @@ __device__ __forceinline__ void pixel_dir(const SvoFrameArgs& a, int x, int y, f
   if (fabsf(dz) < eps) dz = copysignf(eps, dz);
 }
 
-// Lambert: ambient + diffuse*max(0, n.L) (ambient only in shadow).
-__device__ __forceinline__ uint32_t shade(uint2 at, const SvoFrameArgs& a, bool shadowed) {
+// Shading record of a leaf: x = RGBA8, y/z/w = the unit normal in FP32
+// (int8 normal / its length, each a round-to-nearest operation; zero for a
+// zero normal).  The library's layout stores these records (normalised once
+// on the host); a caller's 8-byte yv_leaf_attr is normalised here.
+__device__ __forceinline__ uint4 shading_record(uint2 at) {
   const float nx = (float)(int8_t)(at.y & 0xFFu);
   const float ny = (float)(int8_t)((at.y >> 8) & 0xFFu);
   const float nz = (float)(int8_t)((at.y >> 16) & 0xFFu);
   const float len2 =
       __fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)), __fmul_rn(nz, nz));
-  float ndl = 0.f;
+  float ux = 0.f, uy = 0.f, uz = 0.f;
   if (len2 > 0.f) {
     const float len = __fsqrt_rn(len2);
-    const float ux = __fdiv_rn(nx, len), uy = __fdiv_rn(ny, len), uz = __fdiv_rn(nz, len);
-    ndl = __fadd_rn(__fadd_rn(__fmul_rn(ux, a.light[0]), __fmul_rn(uy, a.light[1])),
-                    __fmul_rn(uz, a.light[2]));
+    ux = __fdiv_rn(nx, len);
+    uy = __fdiv_rn(ny, len);
+    uz = __fdiv_rn(nz, len);
   }
+  return make_uint4(at.x, __float_as_uint(ux), __float_as_uint(uy), __float_as_uint(uz));
+}
+
+template <bool kRef>
+__device__ __forceinline__ uint4 load_shading(const SvoDeviceScene& sc, uint32_t leaf) {
+  if (kRef) return shading_record(__ldg(static_cast<const uint2*>(sc.attrs) + leaf));
+  return __ldg(static_cast<const uint4*>(sc.attrs) + leaf);
+}
+
+// Lambert: ambient + diffuse*max(0, n.L) (ambient only in shadow).
+__device__ __forceinline__ uint32_t shade(uint4 at, const SvoFrameArgs& a, bool shadowed) {
+  const float ndl = __fadd_rn(__fadd_rn(__fmul_rn(__uint_as_float(at.y), a.light[0]),
+                                        __fmul_rn(__uint_as_float(at.z), a.light[1])),
+                              __fmul_rn(__uint_as_float(at.w), a.light[2]));
   const float dif = ndl > 0.f ? ndl : 0.f;
   const float inten = shadowed ? a.ambient : __fadd_rn(a.ambient, __fmul_rn(a.diffuse, dif));
   uint32_t out = 0xFF000000u;
@@ -321,7 +328,7 @@ __global__ void __launch_bounds__(256, kMinBlocks)
   float dx = 0.f, dy = 0.f, dz = 0.f;
   uint32_t hitw = 0xFFFFFFFFu, fp = 0;
   float ht = 0.f;
-  uint2 attr = make_uint2(0u, 0u);
+  uint4 attr = make_uint4(0u, 0u, 0u, 0u);
 
   for (;;) {
     // ---- refill idle lanes from the global ray counter ----
@@ -373,9 +380,9 @@ __global__ void __launch_bounds__(256, kMinBlocks)
             hitw = ((kRef ? tr.node : __ldg(sc.orig_id + tr.node)) << 3) | (tr.ch ^ tr.df);
             ht = max3f(tr.t.x1, tr.t.y1, tr.t.z1);
             fp = tr.fetches;
-            attr = make_uint2(0u, 0u);
+            attr = make_uint4(0u, 0u, 0u, 0u);
             if (leaf < sc.n_attrs)
-              attr = __ldg(sc.attrs + leaf);
+              attr = load_shading<kRef>(sc, leaf);
             else
               err |= YV_DEV_ERR_POOL;
             mode = kIdle;

@@ -12,7 +12,9 @@ namespace yv {
 struct SvoDeviceScene {
   const uint4* nodes = nullptr;       // 2 x uint4 (8 child words) per node
   const uint32_t* orig_id = nullptr;  // device index -> caller node id
-  const uint2* attrs = nullptr;       // yv_leaf_attr, 8 bytes each
+  // library layout: 16-byte shading records {RGBA8, unit normal xyz fp32};
+  // caller VoxNode pools: the caller's yv_leaf_attr (8 bytes)
+  const void* attrs = nullptr;
   uint32_t n_nodes = 0;
   uint32_t n_attrs = 0;
   uint32_t root_word = 0x40000000u;
