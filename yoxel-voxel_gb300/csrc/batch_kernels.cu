@@ -89,7 +89,8 @@ __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
 
     const BatchItem& it = items[item];
     uint32_t leaf = 0;
-    const int r = trace_step<false>(it.svo, nullptr, 0u, stk, tr, mode == kShadow, leaf, err);
+    const int r =
+        trace_step<false, 0>(it.svo, nullptr, 0u, stk, nullptr, tr, mode == kShadow, leaf, err);
     if (r == kContinue) continue;
     if (mode == kPrimary) {
       if (r == kMiss) {

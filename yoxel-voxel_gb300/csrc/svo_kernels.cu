@@ -17,11 +17,14 @@ int device_sm_count() {
   return cached[dev];
 }
 
+// Frames of the per-lane shared-memory stack ring.
+constexpr int kSvoRing = 4;
+
 template <int kMinBlocks>
 static cudaError_t launch_with(const SvoDeviceScene& sc, const SvoFrameArgs& a, int bt,
                                uint32_t nsm, uint32_t refill, int per_sm, cudaStream_t stream) {
-  auto kern = svo_frame_kernel<kMinBlocks, false>;
-  const size_t smem = (size_t)nsm * 32u;
+  auto kern = svo_frame_kernel<kMinBlocks, false, kSvoRing>;
+  const size_t smem = (size_t)nsm * 32u + (size_t)(bt / 32) * kSvoRing * 1024u;
   if (smem > 48u * 1024u) {
     static bool opted_in[64] = {false};
     int dev = 0;

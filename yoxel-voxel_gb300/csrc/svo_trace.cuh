@@ -128,10 +128,59 @@ enum : int { kContinue = 0, kHit = 1, kMiss = 2 };
 
 // Traversal state of one lane.
 struct Trace {
-  uint32_t node, ch, df, fetches, sp;
+  uint32_t node, ch, df, fetches;
+  uint32_t sp;  // frames held
+  uint32_t lo;  // with a shared-memory ring: frames below lo are in local memory
   int level;
   Box t;
 };
+
+// Per-lane frame stack.  kRing = 0: every frame in a local-memory array.
+// kRing > 0 (a power of two): the newest kRing frames in a shared-memory
+// ring, one 16-byte column per lane (lane-contiguous, so a warp's stores and
+// loads are conflict-free and move only the active lanes' bytes); a push
+// into a full ring first moves the oldest frame to the local array.
+template <int kRing>
+__device__ __forceinline__ void push_frame(Frame* stk, uint4* ring, Trace& tr, const Frame& f) {
+  if (kRing == 0) {
+    stk[tr.sp++] = f;
+    return;
+  }
+  if (tr.sp - tr.lo == (uint32_t)kRing) {
+    const uint32_t s = tr.lo & (uint32_t)(kRing - 1);
+    const uint4 q0 = ring[(2 * s) * 32], q1 = ring[(2 * s + 1) * 32];
+    Frame g;
+    g.idch = q0.x;
+    g.x1 = __uint_as_float(q0.y); g.y1 = __uint_as_float(q0.z); g.z1 = __uint_as_float(q0.w);
+    g.x2 = __uint_as_float(q1.x); g.y2 = __uint_as_float(q1.y); g.z2 = __uint_as_float(q1.z);
+    g.level = q1.w;
+    stk[tr.lo++] = g;
+  }
+  const uint32_t s = tr.sp & (uint32_t)(kRing - 1);
+  ring[(2 * s) * 32] =
+      make_uint4(f.idch, __float_as_uint(f.x1), __float_as_uint(f.y1), __float_as_uint(f.z1));
+  ring[(2 * s + 1) * 32] =
+      make_uint4(__float_as_uint(f.x2), __float_as_uint(f.y2), __float_as_uint(f.z2), f.level);
+  ++tr.sp;
+}
+
+template <int kRing>
+__device__ __forceinline__ Frame pop_frame(const Frame* stk, const uint4* ring, Trace& tr) {
+  --tr.sp;
+  if (kRing == 0) return stk[tr.sp];
+  if (tr.sp < tr.lo) {
+    tr.lo = tr.sp;
+    return stk[tr.sp];
+  }
+  const uint32_t s = tr.sp & (uint32_t)(kRing - 1);
+  const uint4 q0 = ring[(2 * s) * 32], q1 = ring[(2 * s + 1) * 32];
+  Frame g;
+  g.idch = q0.x;
+  g.x1 = __uint_as_float(q0.y); g.y1 = __uint_as_float(q0.z); g.z1 = __uint_as_float(q0.w);
+  g.x2 = __uint_as_float(q1.x); g.y2 = __uint_as_float(q1.y); g.z2 = __uint_as_float(q1.z);
+  g.level = q1.w;
+  return g;
+}
 
 
 // SetupTrace (reaction/report/voxel.tex:312-326) + RecTrace entry test
@@ -162,6 +211,7 @@ __device__ __forceinline__ bool begin_trace(const SvoDeviceScene& sc, float px, 
   tr.df = df;
   tr.level = 0;
   tr.sp = 0;
+  tr.lo = 0;
   tr.fetches = 1;
   tr.t = R;
   tr.ch = ffc(tr.t);
@@ -178,12 +228,16 @@ __device__ __forceinline__ bool begin_trace(const SvoDeviceScene& sc, float px, 
 // range and at most YV_MAX_DEPTH levels deep when it is built, so it needs
 // none of these.  In both cases a push happens at level < YV_MAX_DEPTH - 1,
 // so at most YV_MAX_DEPTH - 1 frames are ever held.
-template <bool kRef>
+template <bool kRef, int kRing>
 __device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint32_t* sm,
-                                          uint32_t nsm, Frame* stk, Trace& tr, bool cull,
-                                          uint32_t& leaf, uint32_t& err) {
+                                          uint32_t nsm, Frame* stk, uint4* ring, Trace& tr,
+                                          bool cull, uint32_t& leaf, uint32_t& err) {
   const uint32_t w = child_word<kRef>(sc, sm, nsm, tr.node, tr.ch ^ tr.df);
   const bool ahead = fmin3(tr.t.x2, tr.t.y2, tr.t.z2) > 0.f;
+  // exit axis of the current child and whether it is the last one along
+  // the ray in this node (needed by both the descent and the sibling move)
+  int e = exit_axis(tr.t);
+  const bool last = (tr.ch >> e) & 1u;
   if (w & YV_DW_LEAF) {
     if (!cull || ahead) {
       leaf = w & 0x7FFFFFFFu;
@@ -206,23 +260,22 @@ __device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint32
       }
     }
     ++tr.fetches;
-    if (!((tr.ch >> exit_axis(tr.t)) & 1u)) {
+    if (!last) {
       Frame f;
       f.idch = (tr.node << 3) | tr.ch;
       f.x1 = tr.t.x1; f.y1 = tr.t.y1; f.z1 = tr.t.z1;
       f.x2 = tr.t.x2; f.y2 = tr.t.y2; f.z2 = tr.t.z2;
       f.level = (uint32_t)tr.level;
-      stk[tr.sp++] = f;
+      push_frame<kRing>(stk, ring, tr, f);
     }
     ++tr.level;
     tr.node = w;
     tr.ch = ffc(tr.t);
     return kContinue;
   }
-  int e = exit_axis(tr.t);
-  if ((tr.ch >> e) & 1u) {
+  if (last) {
     if (tr.sp == 0) return kMiss;
-    const Frame f = stk[--tr.sp];
+    const Frame f = pop_frame<kRing>(stk, ring, tr);
     tr.ch = f.idch & 7u;
     tr.node = f.idch >> 3;
     tr.level = (int)f.level;
@@ -308,13 +361,16 @@ __device__ __forceinline__ void write_pixel(const SvoFrameArgs& a, uint32_t off,
 // sized for (the occupancy / register-spill trade-off is autotuned).
 // kRef: the node pool is the reference VoxNode layout (hit ids are then the
 // pool's own node indices); otherwise the library's device layout.
-template <int kMinBlocks, bool kRef>
+// kRing: frames of the per-lane shared-memory ring (0: local memory only);
+// dynamic shared memory = 32 B x nsm staged nodes + 1 KB x kRing per warp.
+template <int kMinBlocks, bool kRef, int kRing>
 __global__ void __launch_bounds__(256, kMinBlocks)
     svo_frame_kernel(SvoDeviceScene sc, SvoFrameArgs a, uint32_t nsm, uint32_t refill_min) {
   extern __shared__ uint4 smem[];
   for (uint32_t i = threadIdx.x; i < 2 * nsm; i += blockDim.x) smem[i] = __ldg(sc.nodes + i);
   __syncthreads();
   const uint32_t* smw = reinterpret_cast<const uint32_t*>(smem);
+  uint4* ring = smem + 2 * nsm + (threadIdx.x >> 5) * (2 * kRing * 32) + (threadIdx.x & 31u);
 
   Frame stk[YV_MAX_DEPTH];
   const uint32_t lane = threadIdx.x & 31u;
@@ -360,11 +416,12 @@ __global__ void __launch_bounds__(256, kMinBlocks)
     }
     if (__all_sync(0xFFFFFFFFu, mode == kDone)) break;
 
-    // ---- trace until refill_min lanes (or all) are free ----
-    for (;;) {
+    // ---- trace until refill_min lanes (or all) are free; two steps per vote ----
+    auto step = [&]() {
       if (mode == kPrimary || mode == kShadow) {
         uint32_t leaf = 0;
-        const int r = trace_step<kRef>(sc, smw, nsm, stk, tr, mode == kShadow, leaf, err);
+        const int r =
+            trace_step<kRef, kRing>(sc, smw, nsm, stk, ring, tr, mode == kShadow, leaf, err);
         if (r != kContinue) {
           if (mode == kShadow) {
             // end of a shadow ray
@@ -410,6 +467,10 @@ __global__ void __launch_bounds__(256, kMinBlocks)
           }
         }
       }
+    };
+    for (;;) {
+      step();
+      step();
       const uint32_t free_lanes = __ballot_sync(0xFFFFFFFFu, mode == kIdle || mode == kDone);
       if (free_lanes == 0xFFFFFFFFu || __popc(free_lanes) >= (int)refill_min) break;
     }
