@@ -37,6 +37,8 @@ namespace yv {
 namespace {
 
 constexpr uint32_t kFetchCap = 1u << 20;
+// traversal steps between two warp votes (refill / end-of-ray handling)
+constexpr int kStepsPerVote = 8;
 
 struct Box {
   float x1, y1, z1, x2, y2, z2;
@@ -76,20 +78,18 @@ __device__ __forceinline__ int exit_axis(const Box& t) {
 }
 
 __device__ __forceinline__ void advance(uint32_t& ch, Box& t, int e) {
+  // branch-free: the lanes of a warp cross different axes
   ch ^= 1u << e;
-  if (e == 0) {
-    const float dt = __fsub_rn(t.x2, t.x1);
-    t.x1 = t.x2;
-    t.x2 = __fadd_rn(t.x2, dt);
-  } else if (e == 1) {
-    const float dt = __fsub_rn(t.y2, t.y1);
-    t.y1 = t.y2;
-    t.y2 = __fadd_rn(t.y2, dt);
-  } else {
-    const float dt = __fsub_rn(t.z2, t.z1);
-    t.z1 = t.z2;
-    t.z2 = __fadd_rn(t.z2, dt);
-  }
+  const bool ex = e == 0, ey = e == 1, ez = e == 2;
+  const float a1 = ex ? t.x1 : (ey ? t.y1 : t.z1);
+  const float a2 = ex ? t.x2 : (ey ? t.y2 : t.z2);
+  const float n2 = __fadd_rn(a2, __fsub_rn(a2, a1));
+  t.x1 = ex ? a2 : t.x1;
+  t.x2 = ex ? n2 : t.x2;
+  t.y1 = ey ? a2 : t.y1;
+  t.y2 = ey ? n2 : t.y2;
+  t.z1 = ez ? a2 : t.z1;
+  t.z2 = ez ? n2 : t.z2;
 }
 
 // Child word c of node id, read where it lies at every step (the node's
@@ -416,61 +416,60 @@ __global__ void __launch_bounds__(256, kMinBlocks)
     }
     if (__all_sync(0xFFFFFFFFu, mode == kDone)) break;
 
-    // ---- trace until refill_min lanes (or all) are free; two steps per vote ----
-    auto step = [&]() {
-      if (mode == kPrimary || mode == kShadow) {
-        uint32_t leaf = 0;
-        const int r =
-            trace_step<kRef, kRing>(sc, smw, nsm, stk, ring, tr, mode == kShadow, leaf, err);
-        if (r != kContinue) {
-          if (mode == kShadow) {
-            // end of a shadow ray
-            const bool sh = r == kHit;
-            my_shadowed += sh ? 1u : 0u;
-            write_pixel(a, off, shade(attr, a, sh), hitw, ht, fp, tr.fetches);
-            mode = kIdle;
-          } else if (r == kMiss) {
-            write_pixel(a, off, 0u, 0xFFFFFFFFu, 0.f, tr.fetches, 0u);
-            mode = kIdle;
-          } else {
-            ++my_hits;
-            hitw = ((kRef ? tr.node : __ldg(sc.orig_id + tr.node)) << 3) | (tr.ch ^ tr.df);
-            ht = max3f(tr.t.x1, tr.t.y1, tr.t.z1);
-            fp = tr.fetches;
-            attr = make_uint4(0u, 0u, 0u, 0u);
-            if (leaf < sc.n_attrs)
-              attr = load_shading<kRef>(sc, leaf);
+    // ---- trace until refill_min lanes (or all) are free: up to kStepsPerVote
+    // steps per warp vote, the end of a ray handled once after them (a lane
+    // whose ray ended idles for the rest of the group) ----
+    for (;;) {
+      int r = kContinue;
+      uint32_t leaf = 0;
+#pragma unroll
+      for (int k = 0; k < kStepsPerVote; ++k)
+        if ((mode == kPrimary || mode == kShadow) && r == kContinue)
+          r = trace_step<kRef, kRing>(sc, smw, nsm, stk, ring, tr, mode == kShadow, leaf, err);
+      if (r != kContinue) {
+        if (mode == kShadow) {
+          // end of a shadow ray
+          const bool sh = r == kHit;
+          my_shadowed += sh ? 1u : 0u;
+          write_pixel(a, off, shade(attr, a, sh), hitw, ht, fp, tr.fetches);
+          mode = kIdle;
+        } else if (r == kMiss) {
+          write_pixel(a, off, 0u, 0xFFFFFFFFu, 0.f, tr.fetches, 0u);
+          mode = kIdle;
+        } else {
+          ++my_hits;
+          hitw = ((kRef ? tr.node : __ldg(sc.orig_id + tr.node)) << 3) | (tr.ch ^ tr.df);
+          ht = max3f(tr.t.x1, tr.t.y1, tr.t.z1);
+          fp = tr.fetches;
+          attr = make_uint4(0u, 0u, 0u, 0u);
+          if (leaf < sc.n_attrs)
+            attr = load_shading<kRef>(sc, leaf);
+          else
+            err |= YV_DEV_ERR_POOL;
+          mode = kIdle;
+          if (a.shadows) {
+            // shadow ray: the hit point moved half a leaf out through the entry face
+            float o[3];
+            o[0] = __fadd_rn(a.pos[0], __fmul_rn(dx, ht));
+            o[1] = __fadd_rn(a.pos[1], __fmul_rn(dy, ht));
+            o[2] = __fadd_rn(a.pos[2], __fmul_rn(dz, ht));
+            int e = 0;
+            float m = tr.t.x1;
+            if (tr.t.y1 > m) { e = 1; m = tr.t.y1; }
+            if (tr.t.z1 > m) e = 2;
+            const float half = __int_as_float((127 - (tr.level + 2)) << 23);
+            const float d_off = ((tr.df >> e) & 1u) ? half : -half;
+            o[e] = __fadd_rn(o[e], d_off);
+            if (begin_trace(sc, o[0], o[1], o[2], a.light_ray[0], a.light_ray[1],
+                            a.light_ray[2], tr, err))
+              mode = kShadow;
             else
-              err |= YV_DEV_ERR_POOL;
-            mode = kIdle;
-            if (a.shadows) {
-              // shadow ray: the hit point moved half a leaf out through the entry face
-              float o[3];
-              o[0] = __fadd_rn(a.pos[0], __fmul_rn(dx, ht));
-              o[1] = __fadd_rn(a.pos[1], __fmul_rn(dy, ht));
-              o[2] = __fadd_rn(a.pos[2], __fmul_rn(dz, ht));
-              int e = 0;
-              float m = tr.t.x1;
-              if (tr.t.y1 > m) { e = 1; m = tr.t.y1; }
-              if (tr.t.z1 > m) e = 2;
-              const float half = __int_as_float((127 - (tr.level + 2)) << 23);
-              const float d_off = ((tr.df >> e) & 1u) ? half : -half;
-              o[e] = __fadd_rn(o[e], d_off);
-              if (begin_trace(sc, o[0], o[1], o[2], a.light_ray[0], a.light_ray[1],
-                              a.light_ray[2], tr, err))
-                mode = kShadow;
-              else
-                write_pixel(a, off, shade(attr, a, false), hitw, ht, fp, tr.fetches);
-            } else {
-              write_pixel(a, off, shade(attr, a, false), hitw, ht, fp, 0u);
-            }
+              write_pixel(a, off, shade(attr, a, false), hitw, ht, fp, tr.fetches);
+          } else {
+            write_pixel(a, off, shade(attr, a, false), hitw, ht, fp, 0u);
           }
         }
       }
-    };
-    for (;;) {
-      step();
-      step();
       const uint32_t free_lanes = __ballot_sync(0xFFFFFFFFu, mode == kIdle || mode == kDone);
       if (free_lanes == 0xFFFFFFFFu || __popc(free_lanes) >= (int)refill_min) break;
     }
