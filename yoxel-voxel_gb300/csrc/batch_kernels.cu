@@ -21,9 +21,14 @@
 namespace yv {
 namespace {
 
+// Dynamic shared memory: the per-lane frame ring of the SVO traversal,
+// 1 KB x kBatchRing per warp.
+constexpr int kBatchRing = 4;
+
 template <int kMinBlocks>
 __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
   __shared__ BatchItem items[kMaxBatchItems];
+  extern __shared__ uint4 ring_smem[];
   {
     const uint32_t words = (uint32_t)(b.nitems * (int)sizeof(BatchItem) / 4);
     const uint32_t* src = reinterpret_cast<const uint32_t*>(b.items);
@@ -33,6 +38,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
   __syncthreads();
 
   Frame stk[YV_MAX_DEPTH];
+  uint4* ring = ring_smem + (threadIdx.x >> 5) * (2 * kBatchRing * 32) + (threadIdx.x & 31u);
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t err = 0;
   uint32_t mode = kIdle, off = 0;
@@ -85,19 +91,24 @@ __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
       }
       continue;
     }
-    if (mode != kPrimary && mode != kShadow) continue;
 
+    // up to kStepsPerVote traversal steps, then the end of a ray once
     const BatchItem& it = items[item];
+    int r = kContinue;
     uint32_t leaf = 0;
-    const int r =
-        trace_step<false, 0>(it.svo, nullptr, 0u, stk, nullptr, tr, mode == kShadow, leaf, err);
+#pragma unroll
+    for (int k = 0; k < kStepsPerVote; ++k)
+      if ((mode == kPrimary || mode == kShadow) && r == kContinue)
+        r = trace_step<false, kBatchRing>(it.svo, nullptr, 0u, stk, ring, tr, mode == kShadow,
+                                          leaf, err);
     if (r == kContinue) continue;
-    if (mode == kPrimary) {
-      if (r == kMiss) {
-        write_pixel(it.fa, off, 0u, 0xFFFFFFFFu, 0.f, tr.fetches, 0u);
-        mode = kIdle;
-        continue;
-      }
+    if (mode == kShadow) {
+      write_pixel(it.fa, off, shade(attr, it.fa, r == kHit), hitw, ht, fp, tr.fetches);
+      mode = kIdle;
+    } else if (r == kMiss) {
+      write_pixel(it.fa, off, 0u, 0xFFFFFFFFu, 0.f, tr.fetches, 0u);
+      mode = kIdle;
+    } else {
       hitw = (__ldg(it.svo.orig_id + tr.node) << 3) | (tr.ch ^ tr.df);
       ht = max3f(tr.t.x1, tr.t.y1, tr.t.z1);
       fp = tr.fetches;
@@ -106,33 +117,28 @@ __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
         attr = load_shading<false>(it.svo, leaf);
       else
         err |= YV_DEV_ERR_POOL;
+      mode = kIdle;
       if (!it.fa.shadows) {
         write_pixel(it.fa, off, shade(attr, it.fa, false), hitw, ht, fp, 0u);
-        mode = kIdle;
-        continue;
-      }
-      float o[3];
-      o[0] = __fadd_rn(it.fa.pos[0], __fmul_rn(dx, ht));
-      o[1] = __fadd_rn(it.fa.pos[1], __fmul_rn(dy, ht));
-      o[2] = __fadd_rn(it.fa.pos[2], __fmul_rn(dz, ht));
-      int e = 0;
-      float m = tr.t.x1;
-      if (tr.t.y1 > m) { e = 1; m = tr.t.y1; }
-      if (tr.t.z1 > m) e = 2;
-      const float half = __int_as_float((127 - (tr.level + 2)) << 23);
-      const float d_off = ((tr.df >> e) & 1u) ? half : -half;
-      o[e] = __fadd_rn(o[e], d_off);
-      if (begin_trace(it.svo, o[0], o[1], o[2], it.fa.light_ray[0], it.fa.light_ray[1],
-                      it.fa.light_ray[2], tr, err)) {
-        mode = kShadow;
       } else {
-        write_pixel(it.fa, off, shade(attr, it.fa, false), hitw, ht, fp, tr.fetches);
-        mode = kIdle;
+        float o[3];
+        o[0] = __fadd_rn(it.fa.pos[0], __fmul_rn(dx, ht));
+        o[1] = __fadd_rn(it.fa.pos[1], __fmul_rn(dy, ht));
+        o[2] = __fadd_rn(it.fa.pos[2], __fmul_rn(dz, ht));
+        int e = 0;
+        float m = tr.t.x1;
+        if (tr.t.y1 > m) { e = 1; m = tr.t.y1; }
+        if (tr.t.z1 > m) e = 2;
+        const float half = __int_as_float((127 - (tr.level + 2)) << 23);
+        const float d_off = ((tr.df >> e) & 1u) ? half : -half;
+        o[e] = __fadd_rn(o[e], d_off);
+        if (begin_trace(it.svo, o[0], o[1], o[2], it.fa.light_ray[0], it.fa.light_ray[1],
+                        it.fa.light_ray[2], tr, err))
+          mode = kShadow;
+        else
+          write_pixel(it.fa, off, shade(attr, it.fa, false), hitw, ht, fp, tr.fetches);
       }
-      continue;
     }
-    write_pixel(it.fa, off, shade(attr, it.fa, r == kHit), hitw, ht, fp, tr.fetches);
-    mode = kIdle;
   }
   if (err) atomicOr(&b.counters[1], err);
 }
@@ -140,13 +146,26 @@ __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
 template <int kMinBlocks>
 cudaError_t launch_batch_with(const BatchLaunch& b, int bt, cudaStream_t s) {
   auto kern = batch_kernel<kMinBlocks>;
+  const size_t smem = (size_t)(bt / 32) * kBatchRing * 1024u;
+  static bool opted_in[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) dev = 0;
+  cudaError_t e = cudaSuccess;
+  if (!opted_in[dev]) {
+    // the item table is static shared memory; the ring is dynamic
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             8 * kBatchRing * 1024);
+    if (e != cudaSuccess) return e;
+    opted_in[dev] = true;
+  }
   int resident = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, bt, 0);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, bt, smem);
   if (e != cudaSuccess) return e;
   if (resident <= 0) return cudaErrorInvalidConfiguration;
   e = cudaMemsetAsync(b.counters, 0, 2 * sizeof(uint32_t), s);
   if (e != cudaSuccess) return e;
-  kern<<<device_sm_count() * resident, bt, 0, s>>>(b);
+  kern<<<device_sm_count() * resident, bt, smem, s>>>(b);
   return cudaGetLastError();
 }
 
