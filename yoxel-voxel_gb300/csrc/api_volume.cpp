@@ -29,16 +29,18 @@ yv_status fail(cudaError_t e, const char* what) {
   return e == cudaErrorMemoryAllocation ? YV_ERR_OUT_OF_MEMORY : YV_ERR_CUDA;
 }
 
-// IEEE binary32 -> binary16, round to nearest even (host side, own code).
+// IEEE binary32 -> binary16, round to nearest even, saturating at +-65504
+// (the fp16 lattice formats hold finite values only; the device decodes
+// them with exact bit arithmetic that assumes a finite half).  NaN -> 0.
 uint16_t f32_to_f16(float f) {
   uint32_t x;
   std::memcpy(&x, &f, 4);
   const uint32_t sign = (x >> 16) & 0x8000u;
   const int32_t exp = (int32_t)((x >> 23) & 0xFFu);
   uint32_t man = x & 0x7FFFFFu;
-  if (exp == 0xFF) return (uint16_t)(sign | 0x7C00u | (man ? 0x200u : 0u));
+  if (exp == 0xFF) return man ? (uint16_t)0 : (uint16_t)(sign | 0x7BFFu);
   int32_t e = exp - 127 + 15;
-  if (e >= 0x1F) return (uint16_t)(sign | 0x7C00u);
+  if (e >= 0x1F) return (uint16_t)(sign | 0x7BFFu);
   if (e <= 0) {
     if (e < -10) return (uint16_t)sign;
     man |= 0x800000u;
@@ -51,6 +53,7 @@ uint16_t f32_to_f16(float f) {
   uint32_t h = ((uint32_t)e << 10) | (man >> 13);
   const uint32_t rem = man & 0x1FFFu;
   if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) ++h;
+  if (h >= 0x7C00u) h = 0x7BFFu;
   return (uint16_t)(sign | h);
 }
 
