@@ -24,7 +24,7 @@
 //   d out_k / d c_jk    = T alpha_j            (c_A = 1)
 // Gradients for the 8 trilinear corners are coalesced in registers while
 // consecutive samples of a ray stay in the same trilinear cell, then flushed
-// with FP32 atomics (red.global.add.f32).
+// with one 16-byte FP32 vector atomic per corner (brick_kernels.cu).
 #pragma once
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
