@@ -149,6 +149,21 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+def cpu_model():
+    """Host CPU name from /proc/cpuinfo (x86 "model name", Arm "CPU part"),
+    or the platform string."""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                k, _, v = line.partition(":")
+                if k.strip() in ("model name", "CPU part"):
+                    return v.strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
 def profile_traffic(name):
     """DRAM bytes per launch recorded from an ncu capture in profiles/<name>.md
     (line `traffic_bytes_per_launch: N`), or None."""
@@ -387,11 +402,14 @@ def run_svo(args, cfg):
         sw, sh = w // 4, h // 4
         v, s, rr = cpu_svo(cfg, scene, sw, sh, threads, min_seconds=10.0, max_runs=50)
         v1, s1, rr1 = cpu_svo(cfg, scene, w // 16, h // 16, 1)
+        v4, s4, rr4 = cpu_svo(cfg, scene, w // 8, h // 8, 4)
         line["cpu_baseline"] = {
             "value": round(v, 4), "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{sw}x{sh} frame of the same scene and camera ({rr} rays incl. shadow "
                       f"rays), repeated for >=10 s; FP32 C restatement of cell/ppu_renderer.cpp",
-            "single_thread_value": round(v1, 4)}
+            "single_thread_value": round(v1, 4),
+            "four_thread_value": round(v4, 4),
+            "cpu_model": cpu_model()}
     print(json.dumps(line), flush=True)
     if pg is not None:
         pg.destroy_process_group()
@@ -627,6 +645,8 @@ def run_batch(args, cfg):
     keep = []
     t_scene = time.perf_counter()
     rays = 0
+    alg = 0      # algorithmic bytes of one batch (SVO: 40 B/fetch + 8 B/pixel + 8 B/hit;
+    outs = []    # bricks: 8 corners x format bytes per sample + refs + 16 B/pixel)
     for sp in specs:
         res = sp["res"]
         pos, view = W.camera(sp["cam_dir"])
@@ -641,16 +661,30 @@ def run_batch(args, cfg):
             r.SetLight(LIGHT, 0.15, 0.85, False)
             out = torch.empty((res, res), dtype=torch.int32, device="cuda")
             batch.add_svo(r, out)
+            # algorithmic bytes of this scene from its own counters (one render)
+            o = r.render_outputs()
+            alg += (40 * int(o["fetches"].to(torch.int64).sum()) + 8 * res * res +
+                    8 * int(o["stats"]["hits"]))
             keep += [r, out]
-            del s
+            outs.append(out)
+            del s, o
         else:
             v = yoxel.BrickVolume.noise(W.brick_levels_for_depth(sp["depth"]), 0.4, 1.4,
                                         sp["seed"])
-            gv = v.upload(cfg["precision"] if args.precision is None else args.precision)
+            prec = cfg["precision"] if args.precision is None else args.precision
+            gv = v.upload(prec)
             out = torch.empty((res, res, 4), dtype=torch.float32, device="cuda")
-            batch.add_volume(gv.desc(), (pos, view, (0, 0, 1), 60.0), res, res, out)
+            cam = (pos, view, (0, 0, 1), 60.0)
+            batch.add_volume(gv.desc(), cam, res, res, out)
+            ns = torch.zeros((1, res, res), dtype=torch.int32, device="cuda")
+            nb = torch.zeros((1, res, res), dtype=torch.int32, device="cuda")
+            yoxel.render_volume(gv.desc(), [cam], res, res, samples=ns, bricks=nb)
+            per_corner = 5 if prec in (0, 3) else 16
+            alg += (8 * per_corner * int(ns.to(torch.int64).sum()) +
+                    4 * v.levels * int(nb.to(torch.int64).sum()) + 16 * res * res)
             keep += [gv, out]
-            del v
+            outs.append(out)
+            del v, ns, nb
         rays += res * res
     t_scene = time.perf_counter() - t_scene
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -669,6 +703,20 @@ def run_batch(args, cfg):
                            lambda: flush.fill_(1))
     clocks = sampler.stop()
     tb, ts, tp = (sum(x) / len(x) for x in (ms_b, ms_s, ms_p))
+    # end to end: the graph replay plus the device-to-host copy of every
+    # frame of the batch into pinned memory, synchronous per step
+    hosts = [torch.empty(o.shape, dtype=o.dtype, pin_memory=True) for o in outs]
+    d2h = sum(o.numel() * o.element_size() for o in outs)
+    torch.cuda.synchronize()
+    te = time.perf_counter()
+    for _ in range(args.steps):
+        batch.render(graph=True)
+        for hst, o in zip(hosts, outs):
+            hst.copy_(o, non_blocking=True)
+        torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - te) / args.steps
+    peaks, kind = measured_peaks()
+    achieved = alg / (tb / 1e3) / 1e9
     line = _base_line(args, cfg, rays / (tb / 1e3) / 1e6, tb, "f32")
     line["config"].update(scenes=len(specs), rays_per_step=rays,
                           svo_scenes=sum(1 for s in specs if s["kind"] == "svo"),
@@ -679,8 +727,14 @@ def run_batch(args, cfg):
         "speedup_vs_separate": round(ts / tb, 3),
         "gpu_launches": args.steps, "clocks": clocks, "wall_s_timed_region": round(wall, 4),
         "scene_build_s": round(t_scene, 2),
-        "roofline": None,
-        "e2e": None})
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
+                     "traffic": None, "peak_source": kind, "kernel": "batch_kernel",
+                     "algorithmic_bytes_per_launch": alg},
+        "e2e": {"value": round(rays / e2e_s / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": d2h,
+                "path": "yoxel.Batch.render (CUDA graph replay) + copy of all frames into "
+                        "pinned host memory; scenes and cameras resident on the device"}})
     print(json.dumps(line), flush=True)
 
 
