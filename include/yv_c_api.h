@@ -117,6 +117,20 @@ const yv_leaf_attr* yv_svo_attrs(const yv_svo_host* svo);
 /* Tree depth (levels of nodes below the root that carry leaves); 0 if empty. */
 int                yv_svo_depth(const yv_svo_host* svo);
 
+/* GPU build of the canonical SVO from a dense density grid: the iso/raw
+ * source form of DynamicSVO::BuildRange (ore/src/main.cpp:37-129,
+ * demo/Demo.cpp:82-114).  density: DEVICE float array of (2^depth)^3
+ * values, x fastest (index x + G*(y + G*z)); rgb: DEVICE uint8 RGB per voxel
+ * or NULL (white).  Voxel solid iff density > iso; surface voxel = solid
+ * with a 6-neighbour outside the grid or not solid (a leaf); regions without
+ * surface voxels are EmptyNode / FullNode; nodes and leaves breadth-first.
+ * Leaf normal = quantised normalize (double) of the central difference
+ * (d(x-1)-d(x+1), ...) with coordinates clamped to the grid.  1 <= depth
+ * <= 11.  Runs on `stream`, then copies the pool into a new host container. */
+yv_status yv_svo_build_dense(const float* density, const uint8_t* rgb,
+                             int32_t depth, float iso, void* stream,
+                             yv_svo_host** out);
+
 /* Host-side validation: child indices in range, leaf VoxData < nattrs,
  * depth <= 16, no cycles.  YV_OK or YV_ERR_BAD_POOL. */
 yv_status yv_svo_validate(const yv_vox_node* nodes, uint32_t count,
@@ -181,6 +195,12 @@ yv_status yv_set_scene_svo(yv_renderer* r, const yv_vox_node* nodes,
                            const yv_leaf_attr* attrs, uint32_t nattrs);
 yv_status yv_set_scene_host(yv_renderer* r, const yv_svo_host* svo);
 yv_status yv_load_scene_vox(yv_renderer* r, const char* path);
+/* The same GPU build (yv_svo_build_dense) straight into the renderer's
+ * device layout: no host copy of the pool.  Node ids are the breadth-first
+ * ids of yv_svo_build_dense. */
+yv_status yv_set_scene_dense(yv_renderer* r, const float* density,
+                             const uint8_t* rgb, int32_t depth, float iso,
+                             void* stream);
 
 /* Camera: ISVORenderer::SetViewPos/SetViewDir/SetViewUp/SetResolution/
  * GetResolution/SetFOV (cell/svorenderer.h:12-21).  Defaults follow

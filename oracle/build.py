@@ -1,6 +1,7 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
-Compiles oracle/yv_oracle.c into oracle/liboracle.so with gcc.  The oracle
+Compiles oracle/yv_oracle.c and oracle/yv_oracle_build.c into
+oracle/liboracle.so with gcc.  The oracle
 is the checker for the CUDA path and the timed CPU baseline; the product
 library never links or loads it.  -ffp-contract=off keeps one IEEE rounding
 per written float operation (no fused multiply-add), which is what makes
@@ -11,9 +12,9 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SRC = os.path.join(HERE, "yv_oracle.c")
+SRCS = [os.path.join(HERE, "yv_oracle.c"), os.path.join(HERE, "yv_oracle_build.c")]
 OUT = os.path.join(HERE, "liboracle.so")
-DEPS = [SRC, os.path.join(HERE, "yv_oracle_impl.h"), os.path.join(HERE, "yv_oracle.h")]
+DEPS = SRCS + [os.path.join(HERE, "yv_oracle_impl.h"), os.path.join(HERE, "yv_oracle.h")]
 
 
 def build(force=False, verbose=False):
@@ -24,7 +25,7 @@ def build(force=False, verbose=False):
             return OUT
     cmd = ["gcc", "-std=c11", "-O3", "-ffp-contract=off", "-fno-fast-math",
            "-fPIC", "-shared", "-pthread", "-Wall", "-Wno-unused-function",
-           SRC, "-o", OUT + ".tmp", "-lm"]
+           *SRCS, "-o", OUT + ".tmp", "-lm"]
     if verbose:
         print(" ".join(cmd))
     subprocess.run(cmd, check=True)

@@ -48,6 +48,7 @@ def load_library(build_if_missing=True):
                                             P, P, P]),
         "orc_brick_render_mt_f32": (I, [I, P, U, P, P, U, I, P, P, P, P, I, I, F, F, P, P, P]),
         "orc_brick_backward_f64": (I, [P, U, P, P, U, I, P, P, P, P, I, I, D, D, P, P, P]),
+        "orc_svo_build_dense": (I, [P, P, I, F, P, U, P, U, P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -288,3 +289,28 @@ def brick_render_f64_f32ray(grids, density, albedo, levels, pos, dir_, up, fov, 
     if st != 0:
         raise RuntimeError(f"oracle brick render failed: {st}")
     return rgba.reshape(height, width, 4), ns.reshape(height, width), nb.reshape(height, width)
+
+
+def svo_build_dense(density, depth, iso=0.0, rgb=None):
+    """CPU build of the canonical SVO from a dense (2^depth)^3 float32 grid
+    (x fastest).  Returns (nodes uint32 (n, 10), attrs uint8 (m, 8), root)."""
+    G = 1 << depth
+    d = np.ascontiguousarray(density, dtype=np.float32).reshape(-1)
+    assert d.size == G ** 3
+    c = None if rgb is None else np.ascontiguousarray(rgb, dtype=np.uint8).reshape(-1)
+    assert c is None or c.size == 3 * G ** 3
+    L = lib()
+    nn, na, root = C.c_uint32(0), C.c_uint32(0), C.c_uint32(0)
+    cap_n, cap_a = 1 << 16, 1 << 16
+    while True:
+        nodes = np.zeros((cap_n, 10), np.uint32)
+        attrs = np.zeros((cap_a, 8), np.uint8)
+        st = L.orc_svo_build_dense(d.ctypes.data, None if c is None else c.ctypes.data, depth,
+                                   float(iso), nodes.ctypes.data, cap_n, attrs.ctypes.data,
+                                   cap_a, C.byref(nn), C.byref(na), C.byref(root))
+        if st == 1:
+            cap_n, cap_a = max(nn.value, 1), max(na.value, 1)
+            continue
+        if st != 0:
+            raise RuntimeError(f"orc_svo_build_dense: {st}")
+        return nodes[:nn.value].copy(), attrs[:na.value].copy(), root.value

@@ -133,6 +133,17 @@ int orc_brick_backward_f64(const uint32_t* grids, uint32_t ngrids,
                            const double* grad_rgba, double* grad_density,
                            double* grad_albedo);
 
+/* SVO build from a dense density grid (yv_oracle_build.c): 2^depth grid,
+ * solid = density > iso, canonical breadth-first pool (nodes: 10 uint32 per
+ * VoxNode, attrs: 8 bytes per leaf).  Returns 0; 1 if node_cap / attr_cap
+ * are too small (n_nodes / n_attrs then hold the sizes needed); 2 bad
+ * arguments; 3 out of memory.  An empty (full) grid gives root EmptyNode
+ * (FullNode) and no nodes. */
+int orc_svo_build_dense(const float* density, const uint8_t* rgb, int depth, float iso,
+                        uint32_t* nodes, uint32_t node_cap, uint8_t* attrs,
+                        uint32_t attr_cap, uint32_t* n_nodes, uint32_t* n_attrs,
+                        uint32_t* root);
+
 #ifdef __cplusplus
 }
 #endif

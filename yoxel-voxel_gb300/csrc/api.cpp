@@ -69,6 +69,40 @@ static void free_scene(yv_renderer* r) {
   r->scene_bytes = 0;
 }
 
+namespace yv {
+
+// Installs device buffers built on the GPU (renderer layout: 32-byte child
+// records, id map, 16-byte shading records) as the renderer's scene; the
+// renderer owns them from here on, also on failure.
+yv_status renderer_adopt_scene(yv_renderer* r, uint32_t* d_words, uint32_t* d_orig,
+                               void* d_attrs, uint32_t nn, uint32_t na, uint32_t root_word,
+                               int depth) {
+  cudaError_t e = cudaSetDevice(r->device);
+  if (e != cudaSuccess) {
+    cudaFree(d_words);
+    cudaFree(d_orig);
+    cudaFree(d_attrs);
+    return cuda_fail(e, "cudaSetDevice");
+  }
+  if (r->frame_pending) cudaStreamSynchronize(r->last_stream);
+  free_scene(r);
+  r->d_words = d_words;
+  r->d_orig = d_orig;
+  r->d_attrs = static_cast<uint4*>(d_attrs);
+  r->scene.nodes = reinterpret_cast<const uint4*>(d_words);
+  r->scene.orig_id = d_orig;
+  r->scene.attrs = d_attrs;
+  r->scene.n_nodes = nn;
+  r->scene.n_attrs = na;
+  r->scene.root_word = root_word;
+  r->scene_bytes = (uint64_t)nn * 36u + (uint64_t)na * 16u;
+  r->has_scene = true;
+  (void)depth;
+  return YV_OK;
+}
+
+}  // namespace yv
+
 extern "C" {
 
 const char* yv_status_string(yv_status s) {

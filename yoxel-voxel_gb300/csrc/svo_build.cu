@@ -1,0 +1,558 @@
+// svo_build.cu - GPU build of the canonical sparse voxel octree from a
+// dense density grid: the iso/raw-source form of DynamicSVO::BuildRange
+// (the GROW pass driven by a voxel source, ore/src/main.cpp:37-129,
+// demo/Demo.cpp:82-114; the DynamicSVO source is not in the reference
+// snapshot), with the surface-voxel rule of scene_gen.py:32-66 and the
+// VoxNode layout of reaction/report/main.tex:36-56.
+//
+// Rules (identical to the host generators' canonical form):
+//   voxel v of the 2^depth grid is solid iff density[v] > iso; a solid voxel
+//   with a 6-neighbour outside the grid or not solid is a surface voxel (a
+//   leaf); a cube region without surface voxels is EmptyNode (no solid
+//   voxel) or FullNode; nodes are numbered breadth-first from the root
+//   (id 0), children in child order c = x | y<<1 | z<<2, leaves in the same
+//   order.  Leaf: RGB of the voxel (white without an rgb grid), A = 255,
+//   normal = quantised normalize of the central difference (d(x-1) -
+//   d(x+1), ...) with coordinates clamped to the grid, in double precision.
+//
+// GB300 design, level-synchronous with no recursion and no host loop over
+// regions:
+//   1. one thread per 2^3-voxel bottom region classifies its 8 voxels
+//      (empty / full / leaf, 2 bits each) and the region;
+//   2. one pass per level folds 8 child classes into the parent class
+//      (EMPTY if all 8 EMPTY, FULL if all 8 FULL, else a node);
+//   3. top-down, the breadth-first node list of level k+1 is the
+//      stable expansion of level k's list (an exclusive scan of the per-node
+//      counts of node children gives every node its first child id), and the
+//      same scan over leaf children numbers the attributes;
+//   4. one pass per level writes the VoxNodes, one pass the leaf attributes.
+// Depth <= 11 (a 2048^3 grid: 8.6 G voxels, 34 GB of float density).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "yv_internal.h"
+#include "yv_kernels.h"
+
+namespace yv {
+namespace {
+
+enum : uint8_t { kClsEmpty = 0, kClsFull = 1, kClsNode = 2 };
+// voxel child codes of a bottom region (2 bits each)
+enum : uint32_t { kVoxEmpty = 0, kVoxFull = 1, kVoxLeaf = 2 };
+
+constexpr int kScanBlock = 1024;  // elements per block of the scan (256 x 4)
+
+struct Grid {
+  const float* d;
+  const uint8_t* rgb;
+  int G;
+  float iso;
+};
+
+__device__ __forceinline__ size_t vidx(int G, int x, int y, int z) {
+  return (size_t)x + (size_t)G * ((size_t)y + (size_t)G * (size_t)z);
+}
+
+__device__ __forceinline__ bool solid(const Grid& g, int x, int y, int z) {
+  if (x < 0 || y < 0 || z < 0 || x >= g.G || y >= g.G || z >= g.G) return false;
+  return __ldg(g.d + vidx(g.G, x, y, z)) > g.iso;
+}
+
+__device__ __forceinline__ float dens_clamped(const Grid& g, int x, int y, int z) {
+  x = x < 0 ? 0 : (x >= g.G ? g.G - 1 : x);
+  y = y < 0 ? 0 : (y >= g.G ? g.G - 1 : y);
+  z = z < 0 ? 0 : (z >= g.G ? g.G - 1 : z);
+  return __ldg(g.d + vidx(g.G, x, y, z));
+}
+
+// Pass 1: bottom regions (2^3 voxels).  codes: 2 bits per voxel child.
+__global__ void classify_bottom_kernel(Grid g, uint32_t n, uint8_t* cls, uint16_t* codes) {
+  const uint64_t total = (uint64_t)n * n * n;
+  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < total;
+       r += (uint64_t)gridDim.x * blockDim.x) {
+    const int rx = (int)(r % n), ry = (int)((r / n) % n), rz = (int)(r / ((uint64_t)n * n));
+    uint32_t code = 0;
+    int n_empty = 0, n_full = 0;
+#pragma unroll
+    for (int ch = 0; ch < 8; ++ch) {
+      const int x = 2 * rx + (ch & 1), y = 2 * ry + ((ch >> 1) & 1), z = 2 * rz + (ch >> 2);
+      uint32_t c;
+      if (!solid(g, x, y, z)) {
+        c = kVoxEmpty;
+        ++n_empty;
+      } else if (!solid(g, x + 1, y, z) || !solid(g, x - 1, y, z) || !solid(g, x, y + 1, z) ||
+                 !solid(g, x, y - 1, z) || !solid(g, x, y, z + 1) || !solid(g, x, y, z - 1)) {
+        c = kVoxLeaf;
+      } else {
+        c = kVoxFull;
+        ++n_full;
+      }
+      code |= c << (2 * ch);
+    }
+    cls[r] = n_empty == 8 ? kClsEmpty : (n_full == 8 ? kClsFull : kClsNode);
+    codes[r] = (uint16_t)code;
+  }
+}
+
+// Pass 2: class of each region of level k (n per axis) from its 8 children
+// at level k+1 (2n per axis).
+__global__ void fold_level_kernel(const uint8_t* child, uint32_t n, uint8_t* cls) {
+  const uint64_t total = (uint64_t)n * n * n;
+  const uint64_t m = 2ull * n;
+  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < total;
+       r += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t rx = r % n, ry = (r / n) % n, rz = r / ((uint64_t)n * n);
+    int n_empty = 0, n_full = 0;
+#pragma unroll
+    for (int ch = 0; ch < 8; ++ch) {
+      const uint64_t c = (2 * rx + (ch & 1)) + m * ((2 * ry + ((ch >> 1) & 1)) +
+                                                    m * (2 * rz + (ch >> 2)));
+      const uint8_t k = child[c];
+      n_empty += k == kClsEmpty;
+      n_full += k == kClsFull;
+    }
+    cls[r] = n_empty == 8 ? kClsEmpty : (n_full == 8 ? kClsFull : kClsNode);
+  }
+}
+
+__device__ __forceinline__ uint64_t child_region(uint64_t r, uint32_t n, int ch) {
+  const uint64_t m = 2ull * n;
+  const uint64_t rx = r % n, ry = (r / n) % n, rz = r / ((uint64_t)n * n);
+  return (2 * rx + (ch & 1)) + m * ((2 * ry + ((ch >> 1) & 1)) + m * (2 * rz + (ch >> 2)));
+}
+
+// Mask of node children (level < bottom) or leaf children (bottom level).
+__device__ __forceinline__ uint32_t node_mask(const uint8_t* child_cls, uint64_t r, uint32_t n) {
+  uint32_t mask = 0;
+#pragma unroll
+  for (int ch = 0; ch < 8; ++ch)
+    if (child_cls[child_region(r, n, ch)] == kClsNode) mask |= 1u << ch;
+  return mask;
+}
+__device__ __forceinline__ uint32_t leaf_mask(uint16_t code) {
+  uint32_t mask = 0;
+#pragma unroll
+  for (int ch = 0; ch < 8; ++ch)
+    if (((code >> (2 * ch)) & 3u) == kVoxLeaf) mask |= 1u << ch;
+  return mask;
+}
+
+// Pass 3a: per node of a level list, the number of node children (or of
+// leaf children at the bottom level).
+__global__ void count_kernel(const uint64_t* list, uint32_t m, const uint8_t* child_cls,
+                             const uint16_t* codes, uint32_t n, uint32_t* counts) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    const uint64_t r = list[i];
+    counts[i] = (uint32_t)__popc(codes ? leaf_mask(codes[r]) : node_mask(child_cls, r, n));
+  }
+}
+
+// Pass 3b: the next level's list, in breadth-first order.
+__global__ void expand_kernel(const uint64_t* list, uint32_t m, const uint8_t* child_cls,
+                              uint32_t n, const uint32_t* offsets, uint64_t* next) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    const uint64_t r = list[i];
+    uint32_t o = offsets[i];
+#pragma unroll
+    for (int ch = 0; ch < 8; ++ch) {
+      const uint64_t c = child_region(r, n, ch);
+      if (child_cls[c] == kClsNode) next[o++] = c;
+    }
+  }
+}
+
+__device__ __forceinline__ uint32_t null_word(uint32_t cls_or_code_full) {
+  return cls_or_code_full ? YV_FULL_NODE : YV_EMPTY_NODE;
+}
+
+// Pass 4a: VoxNodes of one level above the bottom.
+__global__ void emit_nodes_kernel(const uint64_t* list, uint32_t m, const uint8_t* child_cls,
+                                  uint32_t n, const uint32_t* offsets, uint32_t child_base,
+                                  uint32_t node_base, yv_vox_node* out) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    const uint64_t r = list[i];
+    yv_vox_node v;
+    v.flags = 0;
+    v.data = 0;
+    uint32_t next = child_base + offsets[i];
+#pragma unroll
+    for (int ch = 0; ch < 8; ++ch) {
+      const uint8_t k = child_cls[child_region(r, n, ch)];
+      if (k == kClsNode) {
+        v.child[ch] = next++;
+      } else {
+        v.child[ch] = null_word(k == kClsFull);
+        v.flags |= 1u << (8 + ch);
+      }
+    }
+    out[node_base + i] = v;
+  }
+}
+
+__device__ __forceinline__ int8_t quant_n(double v) {
+  double q = floor(__dadd_rn(__dmul_rn(127.0, v), 0.5));
+  if (q > 127.0) q = 127.0;
+  if (q < -127.0) q = -127.0;
+  return (int8_t)(int)q;
+}
+
+// Pass 4b: bottom-level VoxNodes and their leaf attributes.
+__global__ void emit_bottom_kernel(Grid g, const uint64_t* list, uint32_t m, const uint16_t* codes,
+                                   uint32_t n, const uint32_t* offsets, uint32_t node_base,
+                                   yv_vox_node* out, yv_leaf_attr* attrs) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    const uint64_t r = list[i];
+    const int rx = (int)(r % n), ry = (int)((r / n) % n), rz = (int)(r / ((uint64_t)n * n));
+    const uint32_t code = codes[r];
+    yv_vox_node v;
+    v.flags = 0;
+    v.data = 0;
+    uint32_t next = offsets[i];
+    for (int ch = 0; ch < 8; ++ch) {
+      const uint32_t c = (code >> (2 * ch)) & 3u;
+      if (c != kVoxLeaf) {
+        v.child[ch] = null_word(c == kVoxFull);
+        v.flags |= 1u << (8 + ch);
+        continue;
+      }
+      const int x = 2 * rx + (ch & 1), y = 2 * ry + ((ch >> 1) & 1), z = 2 * rz + (ch >> 2);
+      yv_leaf_attr a;
+      if (g.rgb) {
+        const size_t o = 3 * vidx(g.G, x, y, z);
+        a.r = g.rgb[o];
+        a.g = g.rgb[o + 1];
+        a.b = g.rgb[o + 2];
+      } else {
+        a.r = a.g = a.b = 255;
+      }
+      a.a = 255;
+      const float fx = __fsub_rn(dens_clamped(g, x - 1, y, z), dens_clamped(g, x + 1, y, z));
+      const float fy = __fsub_rn(dens_clamped(g, x, y - 1, z), dens_clamped(g, x, y + 1, z));
+      const float fz = __fsub_rn(dens_clamped(g, x, y, z - 1), dens_clamped(g, x, y, z + 1));
+      double nx = fx, ny = fy, nz = fz;
+      const double len = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(nx, nx), __dmul_rn(ny, ny)),
+                                              __dmul_rn(nz, nz)));
+      if (len > 0) {
+        nx = __ddiv_rn(nx, len);
+        ny = __ddiv_rn(ny, len);
+        nz = __ddiv_rn(nz, len);
+      } else {
+        nx = ny = nz = 0;
+      }
+      a.nx = quant_n(nx);
+      a.ny = quant_n(ny);
+      a.nz = quant_n(nz);
+      a.nw = 0;
+      attrs[next] = a;
+      v.child[ch] = next++;
+      v.flags |= 1u << ch;
+    }
+    out[node_base + i] = v;
+  }
+}
+
+// Renderer layout: 32-byte child-word records, identity id map, 16-byte
+// shading records (RGBA8 + unit normal, the FP32 normalisation of the
+// upload path).
+__global__ void device_layout_kernel(const yv_vox_node* nodes, uint32_t nn, uint32_t* words,
+                                     uint32_t* orig) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += gridDim.x * blockDim.x) {
+    const yv_vox_node v = nodes[i];
+#pragma unroll
+    for (int ch = 0; ch < 8; ++ch) {
+      const uint32_t w = v.child[ch];
+      words[8 * (size_t)i + ch] = ((v.flags >> ch) & 1u) ? (YV_DW_LEAF | w)
+                                  : (w & 0x80000000u)     ? YV_DW_NULL
+                                                          : w;
+    }
+    orig[i] = i;
+  }
+}
+
+__global__ void shading_kernel(const yv_leaf_attr* attrs, uint32_t na, uint4* rec) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < na; i += gridDim.x * blockDim.x) {
+    const yv_leaf_attr a = attrs[i];
+    const float nx = (float)a.nx, ny = (float)a.ny, nz = (float)a.nz;
+    const float len2 =
+        __fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)), __fmul_rn(nz, nz));
+    float u[3] = {0.f, 0.f, 0.f};
+    if (len2 > 0.f) {
+      const float len = __fsqrt_rn(len2);
+      u[0] = __fdiv_rn(nx, len);
+      u[1] = __fdiv_rn(ny, len);
+      u[2] = __fdiv_rn(nz, len);
+    }
+    rec[i] = make_uint4((uint32_t)a.r | ((uint32_t)a.g << 8) | ((uint32_t)a.b << 16) |
+                            ((uint32_t)a.a << 24),
+                        __float_as_uint(u[0]), __float_as_uint(u[1]), __float_as_uint(u[2]));
+  }
+}
+
+// ---- exclusive scan of uint32 counts (blocks of 1024, recursive sums) ----
+__global__ void scan_block_kernel(const uint32_t* in, uint32_t* out, uint32_t* sums, uint32_t n) {
+  __shared__ uint32_t warp_tot[8];
+  const uint32_t base = blockIdx.x * kScanBlock + threadIdx.x * 4;
+  uint32_t v[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) v[k] = base + k < n ? in[base + k] : 0u;
+  const uint32_t t = v[0] + v[1] + v[2] + v[3];
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t inc = t;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+    if (lane >= (uint32_t)o) inc += u;
+  }
+  if (lane == 31) warp_tot[warp] = inc;
+  __syncthreads();
+  uint32_t wbase = 0;
+  for (uint32_t w = 0; w < warp; ++w) wbase += warp_tot[w];
+  uint32_t run = wbase + inc - t;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (base + k < n) out[base + k] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == blockDim.x - 1) {
+    uint32_t tot = 0;
+    for (int w = 0; w < 8; ++w) tot += warp_tot[w];
+    sums[blockIdx.x] = tot;
+  }
+}
+
+__global__ void scan_add_kernel(uint32_t* out, const uint32_t* offs, uint32_t n) {
+  const uint32_t i = blockIdx.x * kScanBlock + threadIdx.x * 4;
+  const uint32_t add = offs[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    if (i + k < n) out[i + k] += add;
+}
+
+// Device buffers released on scope exit (stream-ordered).
+struct DevBuf {
+  void* p = nullptr;
+  cudaStream_t s = nullptr;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  cudaError_t alloc(size_t bytes, cudaStream_t st) {
+    s = st;
+    return cudaMallocAsync(&p, bytes ? bytes : 16, st);
+  }
+  ~DevBuf() {
+    if (p) cudaFreeAsync(p, s);
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+int grid_for(uint64_t work) {
+  const uint64_t b = (work + 255) / 256;
+  const uint64_t cap = (uint64_t)device_sm_count() * 16;
+  return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+// out[i] = sum of in[0..i), *total = sum of all.
+cudaError_t exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* total,
+                           cudaStream_t s) {
+  if (n == 0) {
+    *total = 0;
+    return cudaSuccess;
+  }
+  const uint32_t blocks = (n + kScanBlock - 1) / kScanBlock;
+  DevBuf sums, offs;
+  cudaError_t e = sums.alloc((size_t)blocks * 4, s);
+  if (e == cudaSuccess) e = offs.alloc((size_t)blocks * 4, s);
+  if (e != cudaSuccess) return e;
+  scan_block_kernel<<<blocks, 256, 0, s>>>(in, out, sums.as<uint32_t>(), n);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (blocks > 1) {
+    e = exclusive_scan(sums.as<uint32_t>(), offs.as<uint32_t>(), blocks, total, s);
+    if (e != cudaSuccess) return e;
+    scan_add_kernel<<<blocks, 256, 0, s>>>(out, offs.as<uint32_t>(), n);
+    return cudaGetLastError();
+  }
+  // one block: its sum is the total
+  e = cudaMemcpyAsync(total, sums.as<uint32_t>(), 4, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e;
+}
+
+struct BuildResult {
+  DevBuf nodes;  // yv_vox_node[nn]
+  DevBuf attrs;  // yv_leaf_attr[na]
+  uint32_t nn = 0, na = 0, root = YV_EMPTY_NODE;
+};
+
+yv_status build_fail(cudaError_t e, const char* what) {
+  set_last_error(std::string("dense SVO build: ") + what + ": " + cudaGetErrorString(e));
+  cudaGetLastError();
+  return e == cudaErrorMemoryAllocation ? YV_ERR_OUT_OF_MEMORY : YV_ERR_CUDA;
+}
+
+yv_status build_dense(const float* density, const uint8_t* rgb, int depth, float iso,
+                      cudaStream_t s, BuildResult& res) {
+  if (!density || depth < 1 || depth > 11 || std::isnan(iso)) return YV_ERR_INVALID_ARG;
+  const int G = 1 << depth;
+  const Grid g{density, rgb, G, iso};
+  // class arrays of every level, codes of the bottom regions
+  std::vector<DevBuf> cls((size_t)depth);
+  DevBuf codes;
+  cudaError_t e;
+  for (int k = 0; k < depth; ++k) {
+    const uint64_t n = 1ull << k;
+    if ((e = cls[(size_t)k].alloc(n * n * n, s)) != cudaSuccess) return build_fail(e, "alloc");
+  }
+  const uint32_t nb = (uint32_t)(G / 2);
+  const uint64_t nb3 = (uint64_t)nb * nb * nb;
+  if ((e = codes.alloc(nb3 * 2, s)) != cudaSuccess) return build_fail(e, "alloc");
+  classify_bottom_kernel<<<grid_for(nb3), 256, 0, s>>>(g, nb, cls[(size_t)depth - 1].as<uint8_t>(),
+                                                       codes.as<uint16_t>());
+  for (int k = depth - 2; k >= 0; --k) {
+    const uint32_t n = 1u << k;
+    fold_level_kernel<<<grid_for((uint64_t)n * n * n), 256, 0, s>>>(
+        cls[(size_t)k + 1].as<uint8_t>(), n, cls[(size_t)k].as<uint8_t>());
+  }
+  if ((e = cudaGetLastError()) != cudaSuccess) return build_fail(e, "classify");
+  uint8_t root_cls = 0;
+  if ((e = cudaMemcpyAsync(&root_cls, cls[0].as<uint8_t>(), 1, cudaMemcpyDeviceToHost, s)) !=
+          cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return build_fail(e, "root class");
+  if (root_cls != kClsNode) {
+    res.root = root_cls == kClsFull ? YV_FULL_NODE : YV_EMPTY_NODE;
+    return YV_OK;
+  }
+  // breadth-first lists, level by level
+  std::vector<DevBuf> list((size_t)depth), offs((size_t)depth);
+  std::vector<uint32_t> m((size_t)depth, 0), base((size_t)depth + 1, 0);
+  if ((e = list[0].alloc(8, s)) != cudaSuccess) return build_fail(e, "alloc");
+  if ((e = cudaMemsetAsync(list[0].p, 0, 8, s)) != cudaSuccess) return build_fail(e, "list");
+  m[0] = 1;
+  uint32_t n_attrs = 0;
+  for (int k = 0; k < depth; ++k) {
+    const bool bottom = k == depth - 1;
+    const uint32_t n = 1u << k;
+    DevBuf counts;
+    if ((e = counts.alloc((size_t)m[(size_t)k] * 4, s)) != cudaSuccess ||
+        (e = offs[(size_t)k].alloc((size_t)m[(size_t)k] * 4, s)) != cudaSuccess)
+      return build_fail(e, "alloc");
+    // (a node region holds a surface voxel, so every level below the root
+    // has nodes; an empty list would only skip its kernels)
+    if (m[(size_t)k])
+      count_kernel<<<grid_for(m[(size_t)k]), 256, 0, s>>>(
+        list[(size_t)k].as<uint64_t>(), m[(size_t)k],
+        bottom ? nullptr : cls[(size_t)k + 1].as<uint8_t>(), bottom ? codes.as<uint16_t>() : nullptr,
+        n, counts.as<uint32_t>());
+    uint32_t total = 0;
+    if ((e = cudaGetLastError()) != cudaSuccess ||
+        (e = exclusive_scan(counts.as<uint32_t>(), offs[(size_t)k].as<uint32_t>(), m[(size_t)k],
+                            &total, s)) != cudaSuccess)
+      return build_fail(e, "scan");
+    base[(size_t)k + 1] = base[(size_t)k] + m[(size_t)k];
+    if ((uint64_t)base[(size_t)k + 1] > YV_MAX_DEVICE_NODES) {
+      set_last_error("dense SVO build: more than 2^29 nodes");
+      return YV_ERR_UNSUPPORTED;
+    }
+    if (bottom) {
+      n_attrs = total;
+      break;
+    }
+    m[(size_t)k + 1] = total;
+    if ((e = list[(size_t)k + 1].alloc((size_t)total * 8, s)) != cudaSuccess)
+      return build_fail(e, "alloc");
+    expand_kernel<<<grid_for(m[(size_t)k]), 256, 0, s>>>(
+        list[(size_t)k].as<uint64_t>(), m[(size_t)k], cls[(size_t)k + 1].as<uint8_t>(), n,
+        offs[(size_t)k].as<uint32_t>(), list[(size_t)k + 1].as<uint64_t>());
+    if ((e = cudaGetLastError()) != cudaSuccess) return build_fail(e, "expand");
+  }
+  res.nn = base[(size_t)depth];
+  res.na = n_attrs;
+  res.root = 0;
+  if ((e = res.nodes.alloc((size_t)res.nn * sizeof(yv_vox_node), s)) != cudaSuccess ||
+      (e = res.attrs.alloc((size_t)res.na * sizeof(yv_leaf_attr), s)) != cudaSuccess)
+    return build_fail(e, "alloc");
+  for (int k = 0; k < depth - 1; ++k)
+    emit_nodes_kernel<<<grid_for(m[(size_t)k]), 256, 0, s>>>(
+        list[(size_t)k].as<uint64_t>(), m[(size_t)k], cls[(size_t)k + 1].as<uint8_t>(),
+        1u << k, offs[(size_t)k].as<uint32_t>(), base[(size_t)k + 1], base[(size_t)k],
+        res.nodes.as<yv_vox_node>());
+  const int kb = depth - 1;
+  emit_bottom_kernel<<<grid_for(m[(size_t)kb]), 256, 0, s>>>(
+      g, list[(size_t)kb].as<uint64_t>(), m[(size_t)kb], codes.as<uint16_t>(), 1u << kb,
+      offs[(size_t)kb].as<uint32_t>(), base[(size_t)kb], res.nodes.as<yv_vox_node>(),
+      res.attrs.as<yv_leaf_attr>());
+  if ((e = cudaGetLastError()) != cudaSuccess) return build_fail(e, "emit");
+  return YV_OK;
+}
+
+}  // namespace
+}  // namespace yv
+
+using namespace yv;
+
+extern "C" {
+
+yv_status yv_svo_build_dense(const float* density, const uint8_t* rgb, int32_t depth, float iso,
+                             void* stream, yv_svo_host** out) {
+  if (!out) return YV_ERR_INVALID_ARG;
+  *out = nullptr;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  BuildResult res;
+  yv_status st = build_dense(density, rgb, depth, iso, s, res);
+  if (st != YV_OK) return st;
+  std::vector<yv_vox_node> nodes(res.nn);
+  std::vector<yv_leaf_attr> attrs(res.na);
+  cudaError_t e = cudaSuccess;
+  if (res.nn)
+    e = cudaMemcpyAsync(nodes.data(), res.nodes.p, (size_t)res.nn * sizeof(yv_vox_node),
+                        cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && res.na)
+    e = cudaMemcpyAsync(attrs.data(), res.attrs.p, (size_t)res.na * sizeof(yv_leaf_attr),
+                        cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return build_fail(e, "download");
+  return yv_svo_from_arrays(out, nodes.data(), res.nn, res.root, attrs.data(), res.na);
+}
+
+yv_status yv_set_scene_dense(yv_renderer* r, const float* density, const uint8_t* rgb,
+                             int32_t depth, float iso, void* stream) {
+  if (!r) return YV_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  BuildResult res;
+  yv_status st = build_dense(density, rgb, depth, iso, s, res);
+  if (st != YV_OK) return st;
+  // renderer layout: owned by the renderer once adopted
+  uint32_t *words = nullptr, *orig = nullptr;
+  uint4* rec = nullptr;
+  cudaError_t e = cudaMalloc(&words, (size_t)(res.nn ? res.nn : 1) * 32u);
+  if (e == cudaSuccess) e = cudaMalloc(&orig, (size_t)(res.nn ? res.nn : 1) * 4u);
+  if (e == cudaSuccess) e = cudaMalloc(&rec, (size_t)(res.na ? res.na : 1) * 16u);
+  if (e == cudaSuccess && res.nn) {
+    device_layout_kernel<<<grid_for(res.nn), 256, 0, s>>>(res.nodes.as<yv_vox_node>(), res.nn,
+                                                          words, orig);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && res.na) {
+    shading_kernel<<<grid_for(res.na), 256, 0, s>>>(res.attrs.as<yv_leaf_attr>(), res.na, rec);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    cudaFree(words);
+    cudaFree(orig);
+    cudaFree(rec);
+    return build_fail(e, "device layout");
+  }
+  const uint32_t root_word = (res.root & 0x80000000u) ? YV_DW_NULL : 0u;
+  return renderer_adopt_scene(r, words, orig, rec, res.nn, res.na, root_word, depth);
+}
+
+}  // extern "C"

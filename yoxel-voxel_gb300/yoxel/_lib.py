@@ -110,11 +110,13 @@ _SIGS = {
     "yv_svo_attrs": (P, [P]),
     "yv_svo_depth": (I32, [P]),
     "yv_svo_validate": (S, [P, U32, U32, U32]),
+    "yv_svo_build_dense": (S, [P, P, C.c_int32, C.c_float, P, C.POINTER(P)]),
     "yv_renderer_create": (S, [C.POINTER(P)]),
     "yv_renderer_destroy": (None, [P]),
     "yv_set_scene_svo": (S, [P, P, U32, U32, P, U32]),
     "yv_set_scene_host": (S, [P, P]),
     "yv_load_scene_vox": (S, [P, C.c_char_p]),
+    "yv_set_scene_dense": (S, [P, P, P, C.c_int32, C.c_float, P]),
     "yv_set_view_pos": (S, [P, F3]),
     "yv_set_view_dir": (S, [P, F3]),
     "yv_set_view_up": (S, [P, F3]),

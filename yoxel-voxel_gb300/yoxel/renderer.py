@@ -60,6 +60,17 @@ class Renderer:
         L.check(L.lib.yv_set_scene_host(self._h, scene.handle), "SetScene")
         self._scene = scene
 
+    def SetSceneDense(self, density, depth, iso=0.0, rgb=None, stream=None):
+        """Builds the scene on the GPU from a dense CUDA float32 grid (see
+        SVOScene.build_dense) straight into the renderer's device layout."""
+        from .svo import _check_dense
+        _check_dense(density, depth, rgb)
+        L.check(L.lib.yv_set_scene_dense(self._h, C.c_void_p(density.data_ptr()),
+                                         None if rgb is None else C.c_void_p(rgb.data_ptr()),
+                                         depth, float(iso), _stream_ptr(stream)),
+                "SetSceneDense")
+        self._scene = None
+
     def SetSceneArrays(self, nodes, root, attrs):
         from .svo import ATTR_DTYPE, NODE_DTYPE
         nodes = np.ascontiguousarray(nodes, dtype=NODE_DTYPE)

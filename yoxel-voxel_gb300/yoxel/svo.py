@@ -54,6 +54,20 @@ class SVOScene:
         return cls(h.value)
 
     @classmethod
+    def build_dense(cls, density, depth, iso=0.0, rgb=None, stream=None):
+        """GPU build from a dense CUDA float32 grid of (2^depth)^3 values
+        (x fastest, e.g. a (G, G, G) tensor indexed [z, y, x]); rgb: CUDA
+        uint8 (G, G, G, 3) or None (white).  Solid = density > iso; surface
+        voxels become leaves; the canonical pool is copied to the host."""
+        _check_dense(density, depth, rgb)
+        h = C.c_void_p()
+        L.check(L.lib.yv_svo_build_dense(C.c_void_p(density.data_ptr()),
+                                         None if rgb is None else C.c_void_p(rgb.data_ptr()),
+                                         depth, float(iso), _stream(stream), C.byref(h)),
+                "yv_svo_build_dense")
+        return cls(h.value)
+
+    @classmethod
     def load(cls, path):
         """SVOData::Load of a .vox file."""
         h = C.c_void_p()
@@ -120,3 +134,20 @@ class SVOScene:
 
     def nbytes(self):
         return self.node_count * 40 + self.attr_count * 8
+
+
+def _check_dense(density, depth, rgb):
+    G = 1 << int(depth)
+    if not (density.is_cuda and density.is_contiguous() and str(density.dtype) == "torch.float32"
+            and density.numel() == G ** 3):
+        raise ValueError(f"density must be a contiguous CUDA float32 tensor of {G}^3 values")
+    if rgb is not None and not (rgb.is_cuda and rgb.is_contiguous() and
+                                str(rgb.dtype) == "torch.uint8" and rgb.numel() == 3 * G ** 3):
+        raise ValueError(f"rgb must be a contiguous CUDA uint8 tensor of {G}^3 x 3 values")
+
+
+def _stream(stream):
+    if stream is None:
+        import torch
+        stream = torch.cuda.current_stream()
+    return C.c_void_p(stream.cuda_stream)
