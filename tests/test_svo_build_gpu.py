@@ -92,7 +92,8 @@ def test_renderer_scene_built_on_gpu(yoxel_mod, oracle):
                             np.array([0, 0, 1], np.float32), 60.0, w, h, LIGHT, 0.15, 0.85, True)
     hit = got["hit"].cpu().numpy().view(np.uint32).reshape(-1)
     rgba = got["rgba"].cpu().numpy().view(np.uint32).reshape(-1)
-    assert np.array_equal(hit, ref["hit"]) and np.array_equal(rgba, ref["rgba"])
+    assert np.array_equal(hit, ref["hit"].reshape(-1))
+    assert np.array_equal(rgba, ref["rgba"].reshape(-1))
     assert (hit != 0xFFFFFFFF).sum() > 100
     # the same pool uploaded from the host renders the same frame
     r2 = yoxel_mod.Renderer()
