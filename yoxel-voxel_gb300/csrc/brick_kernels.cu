@@ -60,15 +60,14 @@ __global__ void __launch_bounds__(256) volume_forward_kernel(VolumeArgs a) {
 // Gradient of one sample w.r.t. its alpha (see the header), contracted with
 // dL/d(rgba) = g of the ray up front:
 //   sum_k g_k d out_k / d alpha = T (g.c) - (g.out - g.C_after) / (1 - alpha)
-// with c_A = 1, C_after = C_before + T alpha c, and g.out a per-ray constant
-// (gout).  Returns d(sigma) through saturate.  The colour gradient of the
-// sample is g_k T alpha: g is constant along the ray, so only T alpha needs
-// accumulating per corner.
-__device__ __forceinline__ float sample_dsigma(const VolumeArgs* a, const float* g, float gout,
-                                               const SampleCtx& s, float T, float w, float A,
-                                               float C0, float C1, float C2) {
-  const float gc = ffma(g[2], s.col[2], ffma(g[1], s.col[1], ffma(g[0], s.col[0], g[3])));
-  const float gb = ffma(g[3], A, ffma(g[2], C2, ffma(g[1], C1, fmul(g[0], C0))));
+// with c_A = 1, C_after = C_before + T alpha c, g.out a per-ray constant
+// (gout) and gb = g.C_before tracked along the ray (so the replay need not
+// composite the colour).  Returns d(sigma) through saturate.  The colour
+// gradient of the sample is g_k T alpha: g is constant along the ray, so
+// only T alpha needs accumulating per corner.
+__device__ __forceinline__ float sample_dsigma(const VolumeArgs* a, float gc, float gout,
+                                               float gb, const SampleCtx& s, float T,
+                                               float w) {
   const float ga = ffma(w, gc, gb);
   const float om = fsub(1.f, s.alpha);
   // the gradient bar is 1e-4 relative: the hardware reciprocal suffices
@@ -91,10 +90,14 @@ struct GradVis {
   const VolumeArgs* a;
   float g[4];   // dL/d(r,g,b,a) of this ray
   float gout;   // g . (forward output of this ray)
+  float gb;     // g . (r, g, b, A) composited before the current sample
   uint32_t base;
   float gd[8];  // density
   float gw[8];  // colour weight
-  __device__ __forceinline__ void init() { base = 0xFFFFFFFFu; }
+  __device__ __forceinline__ void init() {
+    base = 0xFFFFFFFFu;
+    gb = 0.f;
+  }
   __device__ __forceinline__ void flush() {
     if (base == 0xFFFFFFFFu) return;
 #pragma unroll
@@ -102,10 +105,11 @@ struct GradVis {
       atomicAdd(a->grad_packed + base + corner_offset(j),
                 make_float4(fmul(g[0], gw[j]), fmul(g[1], gw[j]), fmul(g[2], gw[j]), gd[j]));
   }
-  __device__ __forceinline__ void operator()(const SampleCtx& s, float T, float A, float C0,
-                                             float C1, float C2) {
-    const float w = fmul(T, s.alpha);
-    const float ds = sample_dsigma(a, g, gout, s, T, w, A, C0, C1, C2);
+  __device__ __forceinline__ void operator()(const SampleCtx& s, float T, float w, float, float,
+                                             float, float) {
+    const float gc = ffma(g[2], s.col[2], ffma(g[1], s.col[1], ffma(g[0], s.col[0], g[3])));
+    const float ds = sample_dsigma(a, gc, gout, gb, s, T, w);
+    gb = ffma(w, gc, gb);
     if (s.base != base) {
       flush();
       base = s.base;
@@ -148,7 +152,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) volume_backward_kernel(Volume
     gv.gout = ffma(g4.w, o4.w, ffma(g4.z, o4.z, ffma(g4.y, o4.y, fmul(g4.x, o4.x))));
     gv.init();
     RayOut r;
-    march<P>(a.v, sg, nsg, o, d, gv, r);
+    march<P, GradVis, false>(a.v, sg, nsg, o, d, gv, r);
     gv.flush();
     bad |= r.bad;
   }

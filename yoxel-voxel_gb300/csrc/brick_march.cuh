@@ -221,8 +221,11 @@ struct RayOut {
   bool bad;
 };
 
-// One ray; `Vis` is called per sample with (sample, T, C before).
-template <int P, class Vis>
+// One ray; `Vis` is called per sample with (sample, T, T alpha, A and C
+// before the sample).
+// kColor = false (the adjoint's replay): the composited colour is not
+// accumulated (the visitor tracks what it needs; r.c stays 0).
+template <int P, class Vis, bool kColor = true>
 __device__ __forceinline__ void march(const VolumeView& a, const uint32_t* sg, uint32_t nsg,
                                       const float* o, const float* d, Vis& vis, RayOut& r) {
   r.c[0] = r.c[1] = r.c[2] = 0.f;
@@ -290,11 +293,13 @@ __device__ __forceinline__ void march(const VolumeView& a, const uint32_t* sg, u
         SampleCtx s;
         eval_sample<P>(a, b, ffma(t, D[0], L0), ffma(t, D[1], L1), ffma(t, D[2], L2), s);
         const float T = fsub(1.f, A);
-        vis(s, T, A, C0, C1, C2);
         const float w = fmul(T, s.alpha);
-        C0 = ffma(w, s.col[0], C0);
-        C1 = ffma(w, s.col[1], C1);
-        C2 = ffma(w, s.col[2], C2);
+        vis(s, T, w, A, C0, C1, C2);
+        if (kColor) {
+          C0 = ffma(w, s.col[0], C0);
+          C1 = ffma(w, s.col[1], C1);
+          C2 = ffma(w, s.col[2], C2);
+        }
         A = fadd(A, w);
         ++r.samples;
         if (A > 0.99f) goto done;
@@ -315,7 +320,7 @@ done:
 }
 
 struct NoVis {
-  __device__ __forceinline__ void operator()(const SampleCtx&, float, float, float, float,
+  __device__ __forceinline__ void operator()(const SampleCtx&, float, float, float, float, float,
                                              float) {}
 };
 
