@@ -134,6 +134,9 @@ struct Voxel<3> {
 
 struct SampleCtx {
   uint32_t base;  // brick*729 + corner-000 lattice index
+  int brick;      // brick and brick-local corner-000 lattice coordinates
+  int cell[3];
+  float f[3];     // fractional position inside the trilinear cell
   float w[8];     // trilinear weights, corner j: bit0 +x, bit1 +y, bit2 +z
   float sigma, alpha;
   float col[3];
@@ -161,6 +164,13 @@ __device__ __forceinline__ void eval_sample(const VolumeView& a, int b, float lx
     f[i] = fi;
   }
   s.base = (uint32_t)b * (uint32_t)kL3 + (uint32_t)((i0[2] * kL + i0[1]) * kL + i0[0]);
+  s.brick = b;
+  s.cell[0] = i0[0];
+  s.cell[1] = i0[1];
+  s.cell[2] = i0[2];
+  s.f[0] = f[0];
+  s.f[1] = f[1];
+  s.f[2] = f[2];
   const float gx = fsub(1.f, f[0]), gy = fsub(1.f, f[1]), gz = fsub(1.f, f[2]);
   const float w00 = fmul(gx, gy), w10 = fmul(f[0], gy), w01 = fmul(gx, f[1]),
               w11 = fmul(f[0], f[1]);
