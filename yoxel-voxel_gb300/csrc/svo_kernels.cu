@@ -20,10 +20,10 @@ int device_sm_count() {
 // Frames of the per-lane shared-memory stack ring.
 constexpr int kSvoRing = 4;
 
-template <int kMinBlocks>
+template <int kMinBlocks, bool kStaged>
 static cudaError_t launch_with(const SvoDeviceScene& sc, const SvoFrameArgs& a, int bt,
                                uint32_t nsm, uint32_t refill, int per_sm, cudaStream_t stream) {
-  auto kern = svo_frame_kernel<kMinBlocks, false, kSvoRing>;
+  auto kern = svo_frame_kernel<kMinBlocks, false, kSvoRing, kStaged>;
   const size_t smem = (size_t)nsm * 32u + (size_t)(bt / 32) * kSvoRing * 1024u;
   if (smem > 48u * 1024u) {
     static bool opted_in[64] = {false};
@@ -63,15 +63,24 @@ cudaError_t launch_svo_frame(const SvoDeviceScene& sc, const SvoFrameArgs& a,
   uint32_t refill = (uint32_t)(cfg.tile_rays <= 0 ? 32 : cfg.tile_rays);
   if (refill > 32) refill = 32;
   // register budget: blocks_per_sm 2 (up to 128 regs), 3 (80), 4 (64);
-  // 0 = default 3 (fastest on the 2048^3 and 256^3 frames)
-  const int mb = cfg.blocks_per_sm <= 0 ? 3 : (cfg.blocks_per_sm > 4 ? 4 : cfg.blocks_per_sm);
+  // 0 = default 4 (fastest on the 2048^3 frame with unstaged node reads)
+  const int mb = cfg.blocks_per_sm <= 0 ? 4 : (cfg.blocks_per_sm > 4 ? 4 : cfg.blocks_per_sm);
   cudaError_t e;
-  if (mb <= 2)
-    e = launch_with<2>(sc, a, bt, nsm, refill, 0, stream);
-  else if (mb == 3)
-    e = launch_with<3>(sc, a, bt, nsm, refill, 0, stream);
-  else
-    e = launch_with<4>(sc, a, bt, nsm, refill, 0, stream);
+  if (nsm == 0) {
+    if (mb <= 2)
+      e = launch_with<2, false>(sc, a, bt, nsm, refill, 0, stream);
+    else if (mb == 3)
+      e = launch_with<3, false>(sc, a, bt, nsm, refill, 0, stream);
+    else
+      e = launch_with<4, false>(sc, a, bt, nsm, refill, 0, stream);
+  } else {
+    if (mb <= 2)
+      e = launch_with<2, true>(sc, a, bt, nsm, refill, 0, stream);
+    else if (mb == 3)
+      e = launch_with<3, true>(sc, a, bt, nsm, refill, 0, stream);
+    else
+      e = launch_with<4, true>(sc, a, bt, nsm, refill, 0, stream);
+  }
   if (launches) *launches = 1;
   return e;
 }

@@ -110,7 +110,7 @@ extern "C" yv_status yv_render_svo_noalloc(const yv_vox_node* nodes, uint32_t co
   a.counters = scratch;
 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  auto kern = svo_frame_kernel<3, true, 0>;
+  auto kern = svo_frame_kernel<3, true, 0, false>;
   int resident = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, 256, 0);
   if (e == cudaSuccess && resident <= 0) e = cudaErrorInvalidConfiguration;

@@ -98,7 +98,8 @@ __device__ __forceinline__ void advance(uint32_t& ch, Box& t, int e) {
 // (top levels from shared memory).  kRef = true: the reference's 40-byte
 // VoxNode {flags, data, child[8]} read in place, its leaf / null flags
 // folded into the same word encoding.
-template <bool kRef>
+// kStaged: the first nsm records are read from shared memory.
+template <bool kRef, bool kStaged>
 __device__ __forceinline__ uint32_t child_word(const SvoDeviceScene& sc, const uint32_t* sm,
                                                uint32_t nsm, uint32_t id, uint32_t c) {
   if (kRef) {
@@ -107,7 +108,7 @@ __device__ __forceinline__ uint32_t child_word(const SvoDeviceScene& sc, const u
     const uint32_t cw = __ldg(p + 2 + c);
     return ((fl >> c) & 1u) ? (YV_DW_LEAF | cw) : ((cw & 0x80000000u) ? YV_DW_NULL : cw);
   }
-  if (id < nsm) return sm[8 * id + c];
+  if (kStaged && id < nsm) return sm[8 * id + c];
   return __ldg(reinterpret_cast<const uint32_t*>(sc.nodes) + 8 * (size_t)id + c);
 }
 
@@ -228,11 +229,11 @@ __device__ __forceinline__ bool begin_trace(const SvoDeviceScene& sc, float px, 
 // range and at most YV_MAX_DEPTH levels deep when it is built, so it needs
 // none of these.  In both cases a push happens at level < YV_MAX_DEPTH - 1,
 // so at most YV_MAX_DEPTH - 1 frames are ever held.
-template <bool kRef, int kRing>
+template <bool kRef, int kRing, bool kStaged = false>
 __device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint32_t* sm,
                                           uint32_t nsm, Frame* stk, uint4* ring, Trace& tr,
                                           bool cull, uint32_t& leaf, uint32_t& err) {
-  const uint32_t w = child_word<kRef>(sc, sm, nsm, tr.node, tr.ch ^ tr.df);
+  const uint32_t w = child_word<kRef, kStaged>(sc, sm, nsm, tr.node, tr.ch ^ tr.df);
   const bool ahead = fmin3(tr.t.x2, tr.t.y2, tr.t.z2) > 0.f;
   // exit axis of the current child and whether it is the last one along
   // the ray in this node (needed by both the descent and the sibling move)
@@ -362,11 +363,15 @@ __device__ __forceinline__ void write_pixel(const SvoFrameArgs& a, uint32_t off,
 // kRef: the node pool is the reference VoxNode layout (hit ids are then the
 // pool's own node indices); otherwise the library's device layout.
 // kRing: frames of the per-lane shared-memory ring (0: local memory only);
-// dynamic shared memory = 32 B x nsm staged nodes + 1 KB x kRing per warp.
-template <int kMinBlocks, bool kRef, int kRing>
+// kStaged: the first nsm node records are copied to shared memory and read
+// there (measured: reading every record through L1 is as fast or faster,
+// so the default is unstaged and nsm = 0).
+// Dynamic shared memory = 32 B x nsm staged nodes + 1 KB x kRing per warp.
+template <int kMinBlocks, bool kRef, int kRing, bool kStaged>
 __global__ void __launch_bounds__(256, kMinBlocks)
     svo_frame_kernel(SvoDeviceScene sc, SvoFrameArgs a, uint32_t nsm, uint32_t refill_min) {
   extern __shared__ uint4 smem[];
+  if (!kStaged) nsm = 0;
   for (uint32_t i = threadIdx.x; i < 2 * nsm; i += blockDim.x) smem[i] = __ldg(sc.nodes + i);
   __syncthreads();
   const uint32_t* smw = reinterpret_cast<const uint32_t*>(smem);
@@ -425,7 +430,8 @@ __global__ void __launch_bounds__(256, kMinBlocks)
 #pragma unroll
       for (int k = 0; k < kStepsPerVote; ++k)
         if ((mode == kPrimary || mode == kShadow) && r == kContinue)
-          r = trace_step<kRef, kRing>(sc, smw, nsm, stk, ring, tr, mode == kShadow, leaf, err);
+          r = trace_step<kRef, kRing, kStaged>(sc, smw, nsm, stk, ring, tr, mode == kShadow,
+                                               leaf, err);
       if (r != kContinue) {
         if (mode == kShadow) {
           // end of a shadow ray

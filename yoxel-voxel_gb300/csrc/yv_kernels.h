@@ -44,7 +44,7 @@ constexpr int kSvoCounterWords = 8;
 struct LaunchCfg {
   int block_threads = 256;
   int blocks_per_sm = 0;   // 0: occupancy-derived
-  int smem_nodes = 73;     // 1 + 8 + 64: three full top levels
+  int smem_nodes = 0;      // top-of-tree records staged in shared memory
   int tile_rays = 32;
 };
 
