@@ -200,3 +200,57 @@ def test_cuda_renderer_driver(yoxel_mod, spheres):
     assert "gpu time" in stat
     img = cr.getImage()
     assert img.shape == (96, 128, 3) and img.max() > 0
+
+
+def deep_random_tree(rng, levels=16):
+    """Random sparse pool with `levels` node levels: 1-3 node children per
+    node (more near the root), 1-4 leaves per bottom node."""
+    EMPTY = 0x80000000
+    nodes, attrs = [], []
+
+    def make(level):
+        idx = len(nodes)
+        nodes.append(None)
+        flags, child = 0, [EMPTY] * 8
+        if level == levels - 1:
+            for ch in rng.choice(8, int(rng.integers(1, 5)), replace=False):
+                flags |= 1 << int(ch)
+                child[int(ch)] = len(attrs)
+                attrs.append(list(rng.integers(0, 256, 4)) + list(rng.integers(-127, 128, 3)) + [0])
+        else:
+            k = int(rng.integers(2, 5)) if level < 4 else int(rng.integers(1, 3))
+            for ch in rng.choice(8, k, replace=False):
+                child[int(ch)] = make(level + 1)
+        for ch in range(8):
+            if not (flags >> ch) & 1 and child[ch] & 0x80000000:
+                flags |= 1 << (8 + ch)
+        nodes[idx] = (flags, child)
+        return idx
+
+    make(0)
+    n = np.zeros(len(nodes), dtype=np.dtype([("flags", "<u4"), ("data", "<u4"),
+                                             ("child", "<u4", (8,))]))
+    for i, (f, c) in enumerate(nodes):
+        n["flags"][i] = f
+        n["child"][i] = c
+    a = np.array(attrs, dtype=np.int64).astype(np.int8).view(np.uint8).reshape(-1, 8)
+    return n, a
+
+
+def test_deepest_tree_16_levels(yoxel_mod, oracle):
+    """16 node levels (the maximum): deep frame stacks spill out of the
+    shared-memory ring into local memory and back; hits, hit distances,
+    colours and per-ray fetch counts stay bit-exact."""
+    n, a = deep_random_tree(np.random.default_rng(5))
+    attrs = a.reshape(-1).view(yoxel_mod.ATTR_DTYPE)
+    nodes = n.view(yoxel_mod.NODE_DTYPE)
+    assert yoxel_mod.SVOScene.from_arrays(nodes, 0, attrs).depth == 16
+    pos = np.array([1.3, 1.1, 0.9], np.float32)
+    for view in ([-0.8, -0.6, -0.4], [-1.0, -0.2, -0.3]):
+        view = np.array(view, np.float32)
+        g, _ = render_gpu(yoxel_mod, None, pos, view, 128, 96, fov=70.0, shadows=True,
+                          arrays=(nodes, 0, attrs))
+        o = oracle.svo_render(nodes.view(np.uint32), 0, attrs.view(np.uint8), pos, view,
+                              [0, 0, 1], 70.0, 128, 96, LIGHT, shadows=True)
+        assert_bit_exact(g, o, True)
+        assert o["fetches"].max() >= 16

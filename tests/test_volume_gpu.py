@@ -285,3 +285,33 @@ def test_autograd_function_matches_naive_torch_marcher(yoxel_mod, oracle):
     ga = alb.grad.cpu().numpy().reshape(-1)
     assert np.linalg.norm(gd - gref_d) / np.linalg.norm(gref_d) < 1e-4
     assert np.linalg.norm(ga - gref_a) / np.linalg.norm(gref_a) < 1e-4
+
+
+def test_more_cameras_than_one_launch_holds(yoxel_mod):
+    """70 cameras run as launches of 64 + 6: the frames equal per-camera
+    renders bit for bit, and the adjoint of all 70 equals the sum of the
+    adjoints of the two groups."""
+    import torch
+    vol = yoxel_mod.BrickVolume.noise(1, 0.4, 1.4, 8)
+    tv = vol.to_torch()
+    desc = yoxel_mod.torch_desc(tv)
+    cams = yoxel_mod.sphere_cameras(70)
+    w, h = 16, 12
+    out = yoxel_mod.render_volume(desc, cams, w, h)
+    for i in (0, 63, 64, 69):
+        one = yoxel_mod.render_volume(desc, [cams[i]], w, h)[0]
+        assert torch.equal(one.view(torch.int32), out[i].view(torch.int32))
+    g = torch.randn(out.shape, generator=torch.Generator(device="cuda").manual_seed(3),
+                    device="cuda")
+    gd = torch.zeros_like(tv["density"])
+    ga = torch.zeros_like(tv["albedo"])
+    yoxel_mod.volume_backward(desc, cams, w, h, out, g, gd, ga, fold=False)
+    gd2 = torch.zeros_like(gd)
+    ga2 = torch.zeros_like(ga)
+    for lo, hi in ((0, 40), (40, 70)):
+        yoxel_mod.volume_backward(desc, cams[lo:hi], w, h, out[lo:hi].contiguous(),
+                                  g[lo:hi].contiguous(), gd2, ga2, fold=False)
+    # atomics add in a different order: compare as relative L2 error
+    assert float((gd - gd2).norm() / gd.norm()) < 1e-5
+    assert float((ga - ga2).norm() / ga.norm()) < 1e-5
+    assert gd.abs().sum() > 0
