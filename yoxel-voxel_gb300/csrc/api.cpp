@@ -97,7 +97,7 @@ yv_status renderer_adopt_scene(yv_renderer* r, uint32_t* d_words, uint32_t* d_or
   r->scene.root_word = root_word;
   r->scene_bytes = (uint64_t)nn * 36u + (uint64_t)na * 16u;
   r->has_scene = true;
-  (void)depth;
+  (void)depth;  // the device layout carries no depth: traversal is bounded by the validated tree
   return YV_OK;
 }
 
