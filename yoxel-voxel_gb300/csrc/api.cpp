@@ -31,6 +31,7 @@ struct yv_renderer {
   uint32_t* d_words = nullptr;
   uint32_t* d_orig = nullptr;
   uint4* d_attrs = nullptr;  // shading records, 16 B per leaf
+  size_t cap_nodes = 0, cap_attrs = 0;  // allocated records of the three
   SvoDeviceScene scene;
   bool has_scene = false;
   uint64_t scene_bytes = 0;
@@ -64,6 +65,7 @@ static void free_scene(yv_renderer* r) {
   r->d_words = nullptr;
   r->d_orig = nullptr;
   r->d_attrs = nullptr;
+  r->cap_nodes = r->cap_attrs = 0;
   r->has_scene = false;
   r->scene = SvoDeviceScene();
   r->scene_bytes = 0;
@@ -71,34 +73,49 @@ static void free_scene(yv_renderer* r) {
 
 namespace yv {
 
-// Installs device buffers built on the GPU (renderer layout: 32-byte child
-// records, id map, 16-byte shading records) as the renderer's scene; the
-// renderer owns them from here on, also on failure.
-yv_status renderer_adopt_scene(yv_renderer* r, uint32_t* d_words, uint32_t* d_orig,
-                               void* d_attrs, uint32_t nn, uint32_t na, uint32_t root_word,
-                               int depth) {
-  cudaError_t e = cudaSetDevice(r->device);
-  if (e != cudaSuccess) {
-    cudaFree(d_words);
-    cudaFree(d_orig);
-    cudaFree(d_attrs);
-    return cuda_fail(e, "cudaSetDevice");
-  }
+// Scene buffers for a scene built on the device: waits for the renderer's
+// last frame, drops the current scene and returns buffers for nn node
+// records (8 child words + id each) and na shading records, reusing the
+// existing allocations when they are large enough.
+yv_status renderer_scene_buffers(yv_renderer* r, uint32_t nn, uint32_t na, uint32_t** words,
+                                 uint32_t** orig, void** attrs) {
+  YV_CUDA(cudaSetDevice(r->device), "cudaSetDevice");
   if (r->frame_pending) cudaStreamSynchronize(r->last_stream);
-  free_scene(r);
-  r->d_words = d_words;
-  r->d_orig = d_orig;
-  r->d_attrs = static_cast<uint4*>(d_attrs);
-  r->scene.nodes = reinterpret_cast<const uint4*>(d_words);
-  r->scene.orig_id = d_orig;
-  r->scene.attrs = d_attrs;
+  r->has_scene = false;
+  r->scene = SvoDeviceScene();
+  const size_t want_n = nn ? nn : 1, want_a = na ? na : 1;
+  if (want_n > r->cap_nodes) {
+    cudaFree(r->d_words);
+    cudaFree(r->d_orig);
+    r->d_words = r->d_orig = nullptr;
+    r->cap_nodes = 0;
+    YV_CUDA(cudaMalloc(&r->d_words, want_n * 32u), "cudaMalloc(nodes)");
+    YV_CUDA(cudaMalloc(&r->d_orig, want_n * 4u), "cudaMalloc(ids)");
+    r->cap_nodes = want_n;
+  }
+  if (want_a > r->cap_attrs) {
+    cudaFree(r->d_attrs);
+    r->d_attrs = nullptr;
+    r->cap_attrs = 0;
+    YV_CUDA(cudaMalloc(&r->d_attrs, want_a * 16u), "cudaMalloc(attrs)");
+    r->cap_attrs = want_a;
+  }
+  *words = r->d_words;
+  *orig = r->d_orig;
+  *attrs = r->d_attrs;
+  return YV_OK;
+}
+
+// Makes the buffers filled after renderer_scene_buffers the current scene.
+void renderer_commit_scene(yv_renderer* r, uint32_t nn, uint32_t na, uint32_t root_word) {
+  r->scene.nodes = reinterpret_cast<const uint4*>(r->d_words);
+  r->scene.orig_id = r->d_orig;
+  r->scene.attrs = r->d_attrs;
   r->scene.n_nodes = nn;
   r->scene.n_attrs = na;
   r->scene.root_word = root_word;
   r->scene_bytes = (uint64_t)nn * 36u + (uint64_t)na * 16u;
   r->has_scene = true;
-  (void)depth;  // the device layout carries no depth: traversal is bounded by the validated tree
-  return YV_OK;
 }
 
 }  // namespace yv
@@ -205,6 +222,8 @@ yv_status yv_set_scene_svo(yv_renderer* r, const yv_vox_node* nodes,
     YV_CUDA(cudaMemcpy(r->d_attrs, rec.data(), (size_t)nattrs * 16u, cudaMemcpyHostToDevice),
             "upload attrs");
   }
+  r->cap_nodes = nn;
+  r->cap_attrs = nattrs;
   r->scene.nodes = reinterpret_cast<const uint4*>(r->d_words);
   r->scene.orig_id = r->d_orig;
   r->scene.attrs = r->d_attrs;

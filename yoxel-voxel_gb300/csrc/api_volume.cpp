@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "yv_internal.h"
+#include "yv_kernels.h"
 #include "yv_volume.h"
 
 using namespace yv;
@@ -264,7 +265,7 @@ yv_status yv_volume_backward(const yv_volume_device* vol, const yv_camera* cams,
   float4* packed = nullptr;
   cudaError_t e = cudaSuccess;
   if (npts) {
-    e = cudaMallocAsync(reinterpret_cast<void**>(&packed), npts * sizeof(float4), s);
+    e = scratch_alloc(reinterpret_cast<void**>(&packed), npts * sizeof(float4), s);
     if (e == cudaSuccess) e = cudaMemsetAsync(packed, 0, npts * sizeof(float4), s);
   }
   for (int c0 = 0; c0 < ncams && e == cudaSuccess && npts; c0 += kMaxVolumeCams) {
@@ -280,7 +281,7 @@ yv_status yv_volume_backward(const yv_volume_device* vol, const yv_camera* cams,
   if (e == cudaSuccess && npts)
     e = launch_unpack_grads(packed, (uint32_t)npts, grad_density, grad_albedo, s);
   if (packed) {
-    cudaError_t ef = cudaFreeAsync(packed, s);
+    cudaError_t ef = scratch_free(packed, s);
     if (e == cudaSuccess) e = ef;
   }
   delete a;

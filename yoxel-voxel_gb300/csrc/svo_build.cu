@@ -342,11 +342,9 @@ struct DevBuf {
   DevBuf& operator=(const DevBuf&) = delete;
   cudaError_t alloc(size_t bytes, cudaStream_t st) {
     s = st;
-    return cudaMallocAsync(&p, bytes ? bytes : 16, st);
+    return scratch_alloc(&p, bytes ? bytes : 16, st);
   }
-  ~DevBuf() {
-    if (p) cudaFreeAsync(p, s);
-  }
+  ~DevBuf() { scratch_free(p, s); }
   template <class T>
   T* as() const {
     return static_cast<T*>(p);
@@ -529,30 +527,26 @@ yv_status yv_set_scene_dense(yv_renderer* r, const float* density, const uint8_t
   BuildResult res;
   yv_status st = build_dense(density, rgb, depth, iso, s, res);
   if (st != YV_OK) return st;
-  // renderer layout: owned by the renderer once adopted
+  // renderer layout, written into the renderer's (reused) scene buffers
   uint32_t *words = nullptr, *orig = nullptr;
-  uint4* rec = nullptr;
-  cudaError_t e = cudaMalloc(&words, (size_t)(res.nn ? res.nn : 1) * 32u);
-  if (e == cudaSuccess) e = cudaMalloc(&orig, (size_t)(res.nn ? res.nn : 1) * 4u);
-  if (e == cudaSuccess) e = cudaMalloc(&rec, (size_t)(res.na ? res.na : 1) * 16u);
-  if (e == cudaSuccess && res.nn) {
+  void* rec = nullptr;
+  st = renderer_scene_buffers(r, res.nn, res.na, &words, &orig, &rec);
+  if (st != YV_OK) return st;
+  cudaError_t e = cudaSuccess;
+  if (res.nn) {
     device_layout_kernel<<<grid_for(res.nn), 256, 0, s>>>(res.nodes.as<yv_vox_node>(), res.nn,
                                                           words, orig);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess && res.na) {
-    shading_kernel<<<grid_for(res.na), 256, 0, s>>>(res.attrs.as<yv_leaf_attr>(), res.na, rec);
+    shading_kernel<<<grid_for(res.na), 256, 0, s>>>(res.attrs.as<yv_leaf_attr>(), res.na,
+                                                    static_cast<uint4*>(rec));
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) {
-    cudaFree(words);
-    cudaFree(orig);
-    cudaFree(rec);
-    return build_fail(e, "device layout");
-  }
-  const uint32_t root_word = (res.root & 0x80000000u) ? YV_DW_NULL : 0u;
-  return renderer_adopt_scene(r, words, orig, rec, res.nn, res.na, root_word, depth);
+  if (e != cudaSuccess) return build_fail(e, "device layout");
+  renderer_commit_scene(r, res.nn, res.na, (res.root & 0x80000000u) ? YV_DW_NULL : 0u);
+  return YV_OK;
 }
 
 }  // extern "C"

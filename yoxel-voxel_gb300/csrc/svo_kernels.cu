@@ -1,5 +1,7 @@
 // svo_kernels.cu - launcher of the sparse-voxel-octree frame kernel
 // (device code in svo_trace.cuh) for the library's device node layout.
+#include <mutex>
+
 #include "svo_trace.cuh"
 
 namespace yv {
@@ -19,6 +21,36 @@ int device_sm_count() {
 
 // Frames of the per-lane shared-memory stack ring.
 constexpr int kSvoRing = 4;
+
+cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t s) {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaMallocAsync(p, bytes, s);
+  cudaMemPool_t pool;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!pools[dev]) {
+      cudaMemPoolProps props = {};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = dev;
+      e = cudaMemPoolCreate(&pools[dev], &props);
+      if (e != cudaSuccess) {
+        pools[dev] = nullptr;
+        return e;
+      }
+      uint64_t keep = 4ull << 30;
+      cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    pool = pools[dev];
+  }
+  return cudaMallocFromPoolAsync(p, bytes, pool, s);
+}
+
+cudaError_t scratch_free(void* p, cudaStream_t s) { return p ? cudaFreeAsync(p, s) : cudaSuccess; }
 
 template <int kMinBlocks, bool kStaged>
 static cudaError_t launch_with(const SvoDeviceScene& sc, const SvoFrameArgs& a, int bt,

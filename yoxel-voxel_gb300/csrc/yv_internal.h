@@ -83,11 +83,12 @@ uint64_t hash64(uint64_t x);
 
 int hardware_threads();
 
-// Installs scene buffers built on the device into a renderer (which takes
-// ownership): d_words = 8 child words per node, d_orig = caller id per node,
-// d_attrs = 16-byte shading records.  Defined in api.cpp.
-yv_status renderer_adopt_scene(yv_renderer* r, uint32_t* d_words, uint32_t* d_orig,
-                               void* d_attrs, uint32_t nn, uint32_t na, uint32_t root_word,
-                               int depth);
+// Scenes built on the device (api.cpp): renderer_scene_buffers waits for
+// the renderer's last frame and returns its (reused or grown) buffers for nn
+// node records (8 child words, id) and na 16-byte shading records;
+// renderer_commit_scene then makes them the current scene.
+yv_status renderer_scene_buffers(yv_renderer* r, uint32_t nn, uint32_t na, uint32_t** words,
+                                 uint32_t** orig, void** attrs);
+void renderer_commit_scene(yv_renderer* r, uint32_t nn, uint32_t na, uint32_t root_word);
 
 }  // namespace yv

@@ -56,4 +56,12 @@ cudaError_t launch_svo_frame(const SvoDeviceScene& sc, const SvoFrameArgs& a,
 // Number of SMs of the current device (cached per device).
 int device_sm_count();
 
+// Stream-ordered scratch memory from a library-owned pool on the current
+// device that keeps up to 4 GiB cached across synchronisations, so calls
+// repeated every step (the adjoint's gradient scratch, scene builds) do not
+// go back to the driver for memory each time.  The caller's default pool is
+// left as it is.
+cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t s);
+cudaError_t scratch_free(void* p, cudaStream_t s);
+
 }  // namespace yv
