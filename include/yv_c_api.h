@@ -124,9 +124,11 @@ int                yv_svo_depth(const yv_svo_host* svo);
  * or NULL (white).  Voxel solid iff density > iso; surface voxel = solid
  * with a 6-neighbour outside the grid or not solid (a leaf); regions without
  * surface voxels are EmptyNode / FullNode; nodes and leaves breadth-first.
- * Leaf normal = quantised normalize (double) of the central difference
- * (d(x-1)-d(x+1), ...) with coordinates clamped to the grid.  1 <= depth
- * <= 11.  Runs on `stream`, then copies the pool into a new host container. */
+ * Leaf normal = floor(127 u + 0.5) of u = the central difference
+ * (d(x-1)-d(x+1), ...) (coordinates clamped to the grid) over its length,
+ * every step FP32 round-to-nearest (zero for a zero or non-finite length).
+ * 1 <= depth <= 11.  Runs on `stream`, then copies the pool into a new host
+ * container. */
 yv_status yv_svo_build_dense(const float* density, const uint8_t* rgb,
                              int32_t depth, float iso, void* stream,
                              yv_svo_host** out);

@@ -21,10 +21,13 @@
  *   - leaf attribute: RGB of the voxel (white without an rgb grid), A = 255,
  *     normal = the central difference (d(x-1) - d(x+1), d(y-1) - d(y+1),
  *     d(z-1) - d(z+1)) in float with coordinates clamped to the grid,
- *     normalised in double and quantised as floor(127 v + 0.5), clamped to
- *     [-127, 127] (nw = 0); a zero difference gives a zero normal.
+ *     normalised in float (len^2 = (x*x + y*y) + z*z, sqrt, three
+ *     divisions, each rounded to nearest) and quantised as
+ *     floor(127 v + 0.5) in float, clamped to [-127, 127] (nw = 0); a zero
+ *     or non-finite len^2 gives a zero normal.
  * Density is indexed x + G (y + G z), G = 2^depth.
  */
+#include <float.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -71,10 +74,10 @@ static int orc_surface(const orc_build* b, int x, int y, int z) {
          !orc_solid(b, x, y, z + 1) || !orc_solid(b, x, y, z - 1);
 }
 
-static int8_t orc_quant(double v) {
-  double q = floor(127.0 * v + 0.5);
-  if (q > 127.0) q = 127.0;
-  if (q < -127.0) q = -127.0;
+static int8_t orc_quant(float v) {
+  float q = floorf(127.0f * v + 0.5f);
+  if (q > 127.0f) q = 127.0f;
+  if (q < -127.0f) q = -127.0f;
   return (int8_t)(int)q;
 }
 
@@ -88,14 +91,13 @@ static void orc_leaf_attr(const orc_build* b, int x, int y, int z, uint8_t* a) {
   const float fx = orc_dens(b, x - 1, y, z) - orc_dens(b, x + 1, y, z);
   const float fy = orc_dens(b, x, y - 1, z) - orc_dens(b, x, y + 1, z);
   const float fz = orc_dens(b, x, y, z - 1) - orc_dens(b, x, y, z + 1);
-  double nx = fx, ny = fy, nz = fz;
-  const double len = sqrt(nx * nx + ny * ny + nz * nz);
-  if (len > 0) {
-    nx /= len;
-    ny /= len;
-    nz /= len;
-  } else {
-    nx = ny = nz = 0;
+  const float len2 = fx * fx + fy * fy + fz * fz;
+  float nx = 0.f, ny = 0.f, nz = 0.f;
+  if (len2 > 0.f && len2 <= FLT_MAX) {
+    const float len = sqrtf(len2);
+    nx = fx / len;
+    ny = fy / len;
+    nz = fz / len;
   }
   a[4] = (uint8_t)orc_quant(nx);
   a[5] = (uint8_t)orc_quant(ny);

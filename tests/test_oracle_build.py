@@ -25,11 +25,12 @@ def normals_numpy(d):
     fx = (p[1:-1, 1:-1, :-2] - p[1:-1, 1:-1, 2:]).astype(np.float32)
     fy = (p[1:-1, :-2, 1:-1] - p[1:-1, 2:, 1:-1]).astype(np.float32)
     fz = (p[:-2, 1:-1, 1:-1] - p[2:, 1:-1, 1:-1]).astype(np.float32)
-    v = np.stack([fx, fy, fz], -1).astype(np.float64)
-    ln = np.sqrt(v[..., 0] * v[..., 0] + v[..., 1] * v[..., 1] + v[..., 2] * v[..., 2])
-    with np.errstate(invalid="ignore", divide="ignore"):
-        u = np.where(ln[..., None] > 0, v / ln[..., None], 0.0)
-    q = np.clip(np.floor(127.0 * u + 0.5), -127, 127)
+    v = np.stack([fx, fy, fz], -1)
+    ln2 = (v[..., 0] * v[..., 0] + v[..., 1] * v[..., 1]) + v[..., 2] * v[..., 2]
+    ok = (ln2 > 0) & np.isfinite(ln2)
+    ln = np.sqrt(np.where(ok, ln2, np.float32(1)))
+    u = np.where(ok[..., None], v / ln[..., None], np.float32(0)).astype(np.float32)
+    q = np.clip(np.floor(np.float32(127) * u + np.float32(0.5)), -127, 127)
     return q.astype(np.int8)
 
 

@@ -13,12 +13,15 @@
 //   (id 0), children in child order c = x | y<<1 | z<<2, leaves in the same
 //   order.  Leaf: RGB of the voxel (white without an rgb grid), A = 255,
 //   normal = quantised normalize of the central difference (d(x-1) -
-//   d(x+1), ...) with coordinates clamped to the grid, in double precision.
+//   d(x+1), ...) with coordinates clamped to the grid, every step an FP32
+//   round-to-nearest operation (zero for a zero or non-finite length).
 //
 // GB300 design, level-synchronous with no recursion and no host loop over
 // regions:
-//   1. one thread per 2^3-voxel bottom region classifies its 8 voxels
-//      (empty / full / leaf, 2 bits each) and the region;
+//   1. one warp per 32-voxel row run packs the solid bits (ballot); one
+//      thread per word and 2x2 row pair finds the surface voxels by bit
+//      shifts and classifies the 16 bottom regions (2^3 voxels) it covers
+//      (voxel codes empty / full / leaf, 2 bits each);
 //   2. one pass per level folds 8 child classes into the parent class
 //      (EMPTY if all 8 EMPTY, FULL if all 8 FULL, else a node);
 //   3. top-down, the breadth-first node list of level k+1 is the
@@ -58,11 +61,6 @@ __device__ __forceinline__ size_t vidx(int G, int x, int y, int z) {
   return (size_t)x + (size_t)G * ((size_t)y + (size_t)G * (size_t)z);
 }
 
-__device__ __forceinline__ bool solid(const Grid& g, int x, int y, int z) {
-  if (x < 0 || y < 0 || z < 0 || x >= g.G || y >= g.G || z >= g.G) return false;
-  return __ldg(g.d + vidx(g.G, x, y, z)) > g.iso;
-}
-
 __device__ __forceinline__ float dens_clamped(const Grid& g, int x, int y, int z) {
   x = x < 0 ? 0 : (x >= g.G ? g.G - 1 : x);
   y = y < 0 ? 0 : (y >= g.G ? g.G - 1 : y);
@@ -70,32 +68,81 @@ __device__ __forceinline__ float dens_clamped(const Grid& g, int x, int y, int z
   return __ldg(g.d + vidx(g.G, x, y, z));
 }
 
-// Pass 1: bottom regions (2^3 voxels).  codes: 2 bits per voxel child.
-__global__ void classify_bottom_kernel(Grid g, uint32_t n, uint8_t* cls, uint16_t* codes) {
-  const uint64_t total = (uint64_t)n * n * n;
-  for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < total;
-       r += (uint64_t)gridDim.x * blockDim.x) {
-    const int rx = (int)(r % n), ry = (int)((r / n) % n), rz = (int)(r / ((uint64_t)n * n));
-    uint32_t code = 0;
-    int n_empty = 0, n_full = 0;
+// Pass 1a: solid bits, one 32-voxel run of a row per warp and word (lane i
+// tests x = 32 w + i, a ballot packs the run): S[(z G + y) WR + w],
+// WR = max(1, G / 32) words per row; bits beyond the grid are 0.  Four
+// words per iteration keep four coalesced 128-byte loads in flight.
+__global__ void solid_bits_kernel(Grid g, uint32_t WR, uint32_t* S) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint64_t total = (uint64_t)g.G * (uint64_t)g.G * WR;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t w0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; w0 < total;
+       w0 += 4 * nwarps) {
+    bool sol[4];
 #pragma unroll
-    for (int ch = 0; ch < 8; ++ch) {
-      const int x = 2 * rx + (ch & 1), y = 2 * ry + ((ch >> 1) & 1), z = 2 * rz + (ch >> 2);
-      uint32_t c;
-      if (!solid(g, x, y, z)) {
-        c = kVoxEmpty;
-        ++n_empty;
-      } else if (!solid(g, x + 1, y, z) || !solid(g, x - 1, y, z) || !solid(g, x, y + 1, z) ||
-                 !solid(g, x, y - 1, z) || !solid(g, x, y, z + 1) || !solid(g, x, y, z - 1)) {
-        c = kVoxLeaf;
-      } else {
-        c = kVoxFull;
-        ++n_full;
-      }
-      code |= c << (2 * ch);
+    for (int u = 0; u < 4; ++u) {
+      const uint64_t wi = w0 + (uint64_t)u * nwarps;
+      const uint32_t x = (uint32_t)(wi % WR) * 32u + lane;
+      sol[u] = wi < total && x < (uint32_t)g.G &&
+               __ldg(g.d + (wi / WR) * (uint64_t)g.G + x) > g.iso;
     }
-    cls[r] = n_empty == 8 ? kClsEmpty : (n_full == 8 ? kClsFull : kClsNode);
-    codes[r] = (uint16_t)code;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const uint64_t wi = w0 + (uint64_t)u * nwarps;
+      const uint32_t m = __ballot_sync(0xFFFFFFFFu, sol[u]);
+      if (lane == 0 && wi < total) S[wi] = m;
+    }
+  }
+}
+
+// Pass 1b: bottom regions (2^3 voxels) from the bits.  One thread per word
+// and pair of rows in y and in z: a voxel is a surface voxel when it is
+// solid and one of its 6 neighbours is not (bit shifts across the word and
+// its x neighbours, the words of the adjacent rows; outside the grid = not
+// solid).  Writes the class and the 2-bit voxel codes of the (up to) 16
+// regions the word covers.
+__global__ void classify_bits_kernel(const uint32_t* S, int G, uint32_t WR, uint32_t n,
+                                     uint8_t* cls, uint16_t* codes) {
+  const uint64_t total = (uint64_t)WR * n * n;
+  const int nreg = n < 16u ? (int)n : 16;
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t w = (uint32_t)(t % WR);
+    const uint32_t ry = (uint32_t)((t / WR) % n), rz = (uint32_t)(t / ((uint64_t)WR * n));
+    uint32_t sol[2][2], surf[2][2];
+#pragma unroll
+    for (int dz = 0; dz < 2; ++dz)
+#pragma unroll
+      for (int dy = 0; dy < 2; ++dy) {
+        const int y = 2 * (int)ry + dy, z = 2 * (int)rz + dz;
+        const uint64_t row = ((uint64_t)z * G + y) * WR;
+        const uint32_t W = S[row + w];
+        const uint32_t wl = (W << 1) | (w > 0 ? S[row + w - 1] >> 31 : 0u);
+        const uint32_t wr = (W >> 1) | (w + 1 < WR ? (S[row + w + 1] & 1u) << 31 : 0u);
+        const uint32_t ym = y > 0 ? S[row - WR + w] : 0u;
+        const uint32_t yp = y + 1 < G ? S[row + WR + w] : 0u;
+        const uint32_t zm = z > 0 ? S[row - (uint64_t)G * WR + w] : 0u;
+        const uint32_t zp = z + 1 < G ? S[row + (uint64_t)G * WR + w] : 0u;
+        sol[dz][dy] = W;
+        surf[dz][dy] = W & ~(wl & wr & ym & yp & zm & zp);
+      }
+    const uint64_t rbase = (uint64_t)16 * w + (uint64_t)n * (ry + (uint64_t)n * rz);
+    for (int k = 0; k < nreg; ++k) {
+      uint32_t code = 0;
+      int n_empty = 0, n_full = 0;
+#pragma unroll
+      for (int ch = 0; ch < 8; ++ch) {
+        const int bit = 2 * k + (ch & 1);
+        const uint32_t so = (sol[ch >> 2][(ch >> 1) & 1] >> bit) & 1u;
+        const uint32_t su = (surf[ch >> 2][(ch >> 1) & 1] >> bit) & 1u;
+        const uint32_t c = !so ? kVoxEmpty : (su ? kVoxLeaf : kVoxFull);
+        n_empty += !so;
+        n_full += so && !su;
+        code |= c << (2 * ch);
+      }
+      cls[rbase + k] = n_empty == 8 ? kClsEmpty : (n_full == 8 ? kClsFull : kClsNode);
+      codes[rbase + k] = (uint16_t)code;
+    }
   }
 }
 
@@ -194,10 +241,10 @@ __global__ void emit_nodes_kernel(const uint64_t* list, uint32_t m, const uint8_
   }
 }
 
-__device__ __forceinline__ int8_t quant_n(double v) {
-  double q = floor(__dadd_rn(__dmul_rn(127.0, v), 0.5));
-  if (q > 127.0) q = 127.0;
-  if (q < -127.0) q = -127.0;
+__device__ __forceinline__ int8_t quant_n(float v) {
+  float q = floorf(__fadd_rn(__fmul_rn(127.f, v), 0.5f));
+  if (q > 127.f) q = 127.f;
+  if (q < -127.f) q = -127.f;
   return (int8_t)(int)q;
 }
 
@@ -234,15 +281,14 @@ __global__ void emit_bottom_kernel(Grid g, const uint64_t* list, uint32_t m, con
       const float fx = __fsub_rn(dens_clamped(g, x - 1, y, z), dens_clamped(g, x + 1, y, z));
       const float fy = __fsub_rn(dens_clamped(g, x, y - 1, z), dens_clamped(g, x, y + 1, z));
       const float fz = __fsub_rn(dens_clamped(g, x, y, z - 1), dens_clamped(g, x, y, z + 1));
-      double nx = fx, ny = fy, nz = fz;
-      const double len = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(nx, nx), __dmul_rn(ny, ny)),
-                                              __dmul_rn(nz, nz)));
-      if (len > 0) {
-        nx = __ddiv_rn(nx, len);
-        ny = __ddiv_rn(ny, len);
-        nz = __ddiv_rn(nz, len);
-      } else {
-        nx = ny = nz = 0;
+      const float len2 =
+          __fadd_rn(__fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy)), __fmul_rn(fz, fz));
+      float nx = 0.f, ny = 0.f, nz = 0.f;
+      if (len2 > 0.f && len2 <= 3.402823466e38f) {
+        const float len = __fsqrt_rn(len2);
+        nx = __fdiv_rn(fx, len);
+        ny = __fdiv_rn(fy, len);
+        nz = __fdiv_rn(fz, len);
       }
       a.nx = quant_n(nx);
       a.ny = quant_n(ny);
@@ -410,9 +456,15 @@ yv_status build_dense(const float* density, const uint8_t* rgb, int depth, float
   }
   const uint32_t nb = (uint32_t)(G / 2);
   const uint64_t nb3 = (uint64_t)nb * nb * nb;
-  if ((e = codes.alloc(nb3 * 2, s)) != cudaSuccess) return build_fail(e, "alloc");
-  classify_bottom_kernel<<<grid_for(nb3), 256, 0, s>>>(g, nb, cls[(size_t)depth - 1].as<uint8_t>(),
-                                                       codes.as<uint16_t>());
+  const uint32_t WR = G >= 32 ? (uint32_t)(G / 32) : 1u;
+  DevBuf bits;
+  if ((e = codes.alloc(nb3 * 2, s)) != cudaSuccess ||
+      (e = bits.alloc((uint64_t)G * G * WR * 4, s)) != cudaSuccess)
+    return build_fail(e, "alloc");
+  solid_bits_kernel<<<grid_for((uint64_t)G * G * WR * 32 / 4), 256, 0, s>>>(
+      g, WR, bits.as<uint32_t>());
+  classify_bits_kernel<<<grid_for((uint64_t)WR * nb * nb), 256, 0, s>>>(
+      bits.as<uint32_t>(), G, WR, nb, cls[(size_t)depth - 1].as<uint8_t>(), codes.as<uint16_t>());
   for (int k = depth - 2; k >= 0; --k) {
     const uint32_t n = 1u << k;
     fold_level_kernel<<<grid_for((uint64_t)n * n * n), 256, 0, s>>>(
