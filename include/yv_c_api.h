@@ -283,6 +283,16 @@ const int32_t*  yv_volume_neighbors(const yv_volume_host* v, int upper);
 #define YV_PRECISION_F16_PACKED 3 /* 8 B {fp16 density | r<<16 | g<<24, b},
                                      RGB8 (render only)                     */
 
+/* GPU build of the brick volume from a dense DEVICE lattice of (S+1)^3
+ * floats, S = 8 * 4^levels, x fastest (index x + (S+1)*(y + (S+1)*z)), with
+ * an optional DEVICE uint8 RGB lattice (NULL: white): the result of
+ * yv_volume_from_dense (RangeBuilder, ntree/ntree/ntree.h:11-63), bit for
+ * bit, built on `stream` and copied into a new host container.  1 <= levels
+ * <= 4. */
+yv_status yv_volume_build_dense(const float* density, const uint8_t* rgb,
+                                int32_t levels, void* stream,
+                                yv_volume_host** out);
+
 /* Device view of a volume: all pointers are device pointers. */
 typedef struct yv_volume_device {
   const uint32_t* grids;
@@ -301,6 +311,13 @@ typedef struct yv_volume_gpu yv_volume_gpu;
 yv_status yv_volume_upload(const yv_volume_host* v, int32_t precision,
                            yv_volume_gpu** out);
 void      yv_volume_gpu_free(yv_volume_gpu* g);
+/* The same GPU build straight into a device pool of the given precision
+ * (the brick-pool construction of reaction/voxtree/density.cu:30-284 and
+ * BrickPool::Update, reaction/voxtree/brickpool/BrickPool.cpp:21-62): no host
+ * copy of the pool; equal to yv_volume_upload of yv_volume_from_dense. */
+yv_status yv_volume_upload_dense(const float* density, const uint8_t* rgb,
+                                 int32_t levels, int32_t precision, void* stream,
+                                 yv_volume_gpu** out);
 yv_status yv_volume_gpu_desc(const yv_volume_gpu* g, yv_volume_device* out);
 
 /* Pinhole camera (RendererBase fields, cell/renderer_base.h:13-21). */

@@ -111,6 +111,23 @@ bool cams_ok(const yv_camera* c, int n) {
 
 }  // namespace
 
+namespace yv {
+
+yv_status volume_gpu_from_device(void* mem[5], const yv_volume_device& d, yv_volume_gpu** out) {
+  yv_volume_gpu* g = new (std::nothrow) yv_volume_gpu();
+  if (!g) {
+    for (int i = 0; i < 5; ++i) cudaFree(mem[i]);
+    return YV_ERR_OUT_OF_MEMORY;
+  }
+  cudaGetDevice(&g->device);
+  for (int i = 0; i < 5; ++i) g->mem[i] = mem[i];
+  g->desc = d;
+  *out = g;
+  return YV_OK;
+}
+
+}  // namespace yv
+
 extern "C" {
 
 yv_status yv_volume_upload(const yv_volume_host* v, int32_t precision, yv_volume_gpu** out) {

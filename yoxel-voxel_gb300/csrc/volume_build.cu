@@ -1,0 +1,406 @@
+// volume_build.cu - GPU build of the ntree brick volume from a dense lattice:
+// RangeBuilder (ntree/ntree/ntree.h:11-63) over an (S+1)^3 lattice, the
+// producer side of the brick path (the GPU brick-pool construction of
+// reaction/voxtree/density.cu:30-284 and BrickPool::Update,
+// reaction/voxtree/brickpool/BrickPool.cpp:21-62: mark, scan, pack).
+//
+// Same result as the host builder yv_volume_from_dense, bit for bit: brick
+// cells whose 9^3 lattice (with the far-side apron) holds a nonzero density
+// are occupied; an N = 4 grid tree over them, grid nodes and bricks numbered
+// in breadth-first order (children c = x | y<<2 | z<<4), the root always a
+// grid node; bricks copy their 9^3 lattice values and RGB (white without an
+// rgb lattice); neighbour tables for the apron fold.
+//
+// Passes: one warp per brick cell marks it (ballot over its 729 values);
+// one pass per level ORs 64 child flags; top-down, an exclusive scan of the
+// per-node counts of occupied children expands level l's breadth-first list
+// into level l+1's and gives every node its first child id (bricks are the
+// last level's children); emit passes write the grid refs, pack the bricks
+// (optionally straight into a device pool format) and fill the neighbours.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "dev_scan.cuh"
+#include "yv_internal.h"
+#include "yv_kernels.h"
+
+namespace yv {
+namespace {
+
+constexpr int kVB = 8;  // brick cells per axis
+constexpr int kVL = 9;  // lattice points per axis with the apron
+constexpr int kVL3 = 729;
+
+struct Lattice {
+  const float* d;
+  const uint8_t* rgb;
+  uint64_t L;  // lattice points per axis (S + 1)
+  int nb;      // brick cells per axis
+};
+
+__device__ __forceinline__ uint64_t lat(const Lattice& g, int x, int y, int z) {
+  return ((uint64_t)z * g.L + (uint64_t)y) * g.L + (uint64_t)x;
+}
+
+// Mark: one warp per brick cell, any nonzero value among its 9^3.
+__global__ void mark_cells_kernel(Lattice g, uint8_t* occ) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint64_t cells = (uint64_t)g.nb * g.nb * g.nb;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  for (uint64_t c = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; c < cells;
+       c += nwarps) {
+    const int cx = (int)(c % g.nb), cy = (int)((c / g.nb) % g.nb),
+              cz = (int)(c / ((uint64_t)g.nb * g.nb));
+    bool nz = false;
+    for (int k = (int)lane; k < kVL3 && !nz; k += 32)
+      nz = __ldg(g.d + lat(g, cx * kVB + k % kVL, cy * kVB + (k / kVL) % kVL,
+                           cz * kVB + k / (kVL * kVL))) != 0.f;
+    const uint32_t any = __ballot_sync(0xFFFFFFFFu, nz);
+    if (lane == 0) occ[c] = any ? 1 : 0;
+  }
+}
+
+// Level l (n per axis) from level l+1 (4n per axis): OR of 64 children.
+__global__ void fold64_kernel(const uint8_t* child, uint32_t n, uint8_t* out) {
+  const uint64_t total = (uint64_t)n * n * n;
+  const uint64_t m = 4ull * n;
+  for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < total;
+       p += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t x = p % n, y = (p / n) % n, z = p / ((uint64_t)n * n);
+    uint8_t a = 0;
+    for (int c = 0; c < 64 && !a; ++c)
+      a = child[(4 * x + (c & 3)) + m * ((4 * y + ((c >> 2) & 3)) + m * (4 * z + (c >> 4)))];
+    out[p] = a;
+  }
+}
+
+__device__ __forceinline__ uint64_t child64(uint64_t p, uint32_t n, int c) {
+  const uint64_t m = 4ull * n;
+  const uint64_t x = p % n, y = (p / n) % n, z = p / ((uint64_t)n * n);
+  return (4 * x + (c & 3)) + m * ((4 * y + ((c >> 2) & 3)) + m * (4 * z + (c >> 4)));
+}
+
+__global__ void count64_kernel(const uint64_t* list, uint32_t m, const uint8_t* child_any,
+                               uint32_t n, uint32_t* counts) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    uint32_t k = 0;
+    for (int c = 0; c < 64; ++c) k += child_any[child64(list[i], n, c)] ? 1u : 0u;
+    counts[i] = k;
+  }
+}
+
+__global__ void expand64_kernel(const uint64_t* list, uint32_t m, const uint8_t* child_any,
+                                uint32_t n, const uint32_t* offsets, uint64_t* next) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    uint32_t o = offsets[i];
+    for (int c = 0; c < 64; ++c) {
+      const uint64_t q = child64(list[i], n, c);
+      if (child_any[q]) next[o++] = q;
+    }
+  }
+}
+
+// Grid refs of one level: occupied children are grid nodes (child_base +
+// rank) or, at the last level, bricks (0x40000000 | rank).
+__global__ void emit_grids_kernel(const uint64_t* list, uint32_t m, const uint8_t* child_any,
+                                  uint32_t n, const uint32_t* offsets, uint32_t node_base,
+                                  uint32_t child_base, bool bricks, uint32_t* grids) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+    uint32_t next = offsets[i];
+    uint32_t* g = grids + (size_t)(node_base + i) * 64;
+    for (int c = 0; c < 64; ++c) {
+      uint32_t ref = 0x80000000u;
+      if (child_any[child64(list[i], n, c)]) {
+        ref = bricks ? (0x40000000u | next) : (child_base + next);
+        ++next;
+      }
+      g[c] = ref;
+    }
+  }
+}
+
+__device__ __forceinline__ uint16_t f16_saturating(float f) {
+  if (f != f) return 0;  // NaN -> 0, as the host upload
+  uint16_t u = __half_as_ushort(__float2half_rn(f));
+  if ((u & 0x7FFFu) == 0x7C00u) u = (uint16_t)((u & 0x8000u) | 0x7BFFu);
+  return u;
+}
+
+// Pack: one warp per brick, its 729 lattice values (and RGB).  format < 0:
+// fp32 density + uint8 RGB (host container layout); else a device pool
+// format (YV_PRECISION_*), written to d_out / a_out.
+__global__ void pack_bricks_kernel(Lattice g, const uint64_t* cells, uint32_t nbricks, int format,
+                                   float* dens, uint8_t* rgb, void* d_out, void* a_out,
+                                   int32_t* cell_xyz, int32_t* map) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < nbricks; b += nwarps) {
+    const uint64_t c = cells[b];
+    const int cx = (int)(c % g.nb), cy = (int)((c / g.nb) % g.nb),
+              cz = (int)(c / ((uint64_t)g.nb * g.nb));
+    if (lane == 0) {
+      cell_xyz[3 * (size_t)b] = cx;
+      cell_xyz[3 * (size_t)b + 1] = cy;
+      cell_xyz[3 * (size_t)b + 2] = cz;
+      map[c] = (int32_t)b;
+    }
+    for (int k = (int)lane; k < kVL3; k += 32) {
+      const uint64_t src = lat(g, cx * kVB + k % kVL, cy * kVB + (k / kVL) % kVL,
+                               cz * kVB + k / (kVL * kVL));
+      const float v = __ldg(g.d + src);
+      uint8_t r = 255, gg = 255, bb = 255;
+      if (g.rgb) {
+        r = g.rgb[3 * src];
+        gg = g.rgb[3 * src + 1];
+        bb = g.rgb[3 * src + 2];
+      }
+      const size_t o = (size_t)b * kVL3 + (size_t)k;
+      if (format < 0) {
+        dens[o] = v;
+        rgb[3 * o] = r;
+        rgb[3 * o + 1] = gg;
+        rgb[3 * o + 2] = bb;
+      } else if (format == YV_PRECISION_F16) {
+        static_cast<uint16_t*>(d_out)[o] = f16_saturating(v);
+        static_cast<uchar4*>(a_out)[o] = make_uchar4(r, gg, bb, 255);
+      } else if (format == YV_PRECISION_F32) {
+        static_cast<float*>(d_out)[o] = v;
+        float* a = static_cast<float*>(a_out) + 3 * o;
+        a[0] = __fmul_rn((float)r, 1.0f / 255.0f);
+        a[1] = __fmul_rn((float)gg, 1.0f / 255.0f);
+        a[2] = __fmul_rn((float)bb, 1.0f / 255.0f);
+      } else if (format == YV_PRECISION_F32_PACKED) {
+        static_cast<float4*>(a_out)[o] =
+            make_float4(__fmul_rn((float)r, 1.0f / 255.0f), __fmul_rn((float)gg, 1.0f / 255.0f),
+                        __fmul_rn((float)bb, 1.0f / 255.0f), v);
+      } else {
+        static_cast<uint2*>(a_out)[o] =
+            make_uint2((uint32_t)f16_saturating(v) | ((uint32_t)r << 16) | ((uint32_t)gg << 24),
+                       (uint32_t)bb);
+      }
+    }
+  }
+}
+
+// Apron neighbour tables (index m-1 for the offset m = dx | dy<<1 | dz<<2).
+__global__ void neighbors_kernel(const int32_t* cell_xyz, const int32_t* map, uint32_t nbricks,
+                                 int nb, int32_t* up, int32_t* dn) {
+  for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < nbricks;
+       b += gridDim.x * blockDim.x) {
+    const int x = cell_xyz[3 * (size_t)b], y = cell_xyz[3 * (size_t)b + 1],
+              z = cell_xyz[3 * (size_t)b + 2];
+    for (int m = 1; m < 8; ++m) {
+      const int dx = m & 1, dy = (m >> 1) & 1, dz = (m >> 2) & 1;
+      const int ux = x + dx, uy = y + dy, uz = z + dz;
+      up[7 * (size_t)b + m - 1] =
+          (ux < nb && uy < nb && uz < nb) ? map[((size_t)uz * nb + uy) * nb + ux] : -1;
+      const int lx = x - dx, ly = y - dy, lz = z - dz;
+      dn[7 * (size_t)b + m - 1] =
+          (lx >= 0 && ly >= 0 && lz >= 0) ? map[((size_t)lz * nb + ly) * nb + lx] : -1;
+    }
+  }
+}
+
+yv_status vbuild_fail(cudaError_t e, const char* what) {
+  set_last_error(std::string("dense volume build: ") + what + ": " + cudaGetErrorString(e));
+  cudaGetLastError();
+  return e == cudaErrorMemoryAllocation ? YV_ERR_OUT_OF_MEMORY : YV_ERR_CUDA;
+}
+
+// Tree of a dense lattice on the device: grid refs (ngrids x 64) and the
+// breadth-first brick cells.  Buffers come from the scratch pool.
+struct VolumeTree {
+  DevBuf grids, cells;  // uint32 grids[ngrids*64], uint64 cells[nbricks]
+  uint32_t ngrids = 0, nbricks = 0;
+};
+
+yv_status build_volume_tree(const Lattice& g, int levels, cudaStream_t s, VolumeTree& t) {
+  cudaError_t e;
+  std::vector<DevBuf> any((size_t)levels + 1);
+  for (int l = 0; l <= levels; ++l) {
+    const uint64_t n = 1ull << (2 * l);
+    if ((e = any[(size_t)l].alloc(n * n * n, s)) != cudaSuccess) return vbuild_fail(e, "alloc");
+  }
+  const uint64_t cells = (uint64_t)g.nb * g.nb * g.nb;
+  mark_cells_kernel<<<grid_for(cells * 32), 256, 0, s>>>(g, any[(size_t)levels].as<uint8_t>());
+  for (int l = levels - 1; l >= 0; --l) {
+    const uint32_t n = 1u << (2 * l);
+    fold64_kernel<<<grid_for((uint64_t)n * n * n), 256, 0, s>>>(
+        any[(size_t)l + 1].as<uint8_t>(), n, any[(size_t)l].as<uint8_t>());
+  }
+  if ((e = cudaGetLastError()) != cudaSuccess) return vbuild_fail(e, "mark");
+  // breadth-first lists: level 0 = the root (always a grid node)
+  std::vector<DevBuf> list((size_t)levels + 1), offs((size_t)levels);
+  std::vector<uint32_t> m((size_t)levels + 1, 0), base((size_t)levels + 1, 0);
+  if ((e = list[0].alloc(8, s)) != cudaSuccess ||
+      (e = cudaMemsetAsync(list[0].p, 0, 8, s)) != cudaSuccess)
+    return vbuild_fail(e, "alloc");
+  m[0] = 1;
+  for (int l = 0; l < levels; ++l) {
+    const uint32_t n = 1u << (2 * l);
+    DevBuf counts;
+    if ((e = counts.alloc((size_t)m[(size_t)l] * 4, s)) != cudaSuccess ||
+        (e = offs[(size_t)l].alloc((size_t)m[(size_t)l] * 4, s)) != cudaSuccess)
+      return vbuild_fail(e, "alloc");
+    if (m[(size_t)l])
+      count64_kernel<<<grid_for(m[(size_t)l]), 256, 0, s>>>(
+          list[(size_t)l].as<uint64_t>(), m[(size_t)l], any[(size_t)l + 1].as<uint8_t>(), n,
+          counts.as<uint32_t>());
+    uint32_t total = 0;
+    if ((e = cudaGetLastError()) != cudaSuccess ||
+        (e = exclusive_scan(counts.as<uint32_t>(), offs[(size_t)l].as<uint32_t>(),
+                            m[(size_t)l], &total, s)) != cudaSuccess)
+      return vbuild_fail(e, "scan");
+    base[(size_t)l + 1] = base[(size_t)l] + m[(size_t)l];
+    m[(size_t)l + 1] = total;
+    if ((e = list[(size_t)l + 1].alloc((size_t)(total ? total : 1) * 8, s)) != cudaSuccess)
+      return vbuild_fail(e, "alloc");
+    if (m[(size_t)l])
+      expand64_kernel<<<grid_for(m[(size_t)l]), 256, 0, s>>>(
+          list[(size_t)l].as<uint64_t>(), m[(size_t)l], any[(size_t)l + 1].as<uint8_t>(), n,
+          offs[(size_t)l].as<uint32_t>(), list[(size_t)l + 1].as<uint64_t>());
+    if ((e = cudaGetLastError()) != cudaSuccess) return vbuild_fail(e, "expand");
+  }
+  // grid nodes: levels 0..levels-1; bricks: the last list
+  t.ngrids = base[(size_t)levels];
+  t.nbricks = m[(size_t)levels];
+  if ((e = t.grids.alloc((size_t)t.ngrids * 256, s)) != cudaSuccess)
+    return vbuild_fail(e, "alloc");
+  for (int l = 0; l < levels; ++l) {
+    if (!m[(size_t)l]) continue;
+    const bool last = l == levels - 1;
+    emit_grids_kernel<<<grid_for(m[(size_t)l]), 256, 0, s>>>(
+        list[(size_t)l].as<uint64_t>(), m[(size_t)l], any[(size_t)l + 1].as<uint8_t>(),
+        1u << (2 * l), offs[(size_t)l].as<uint32_t>(), base[(size_t)l],
+        last ? 0u : base[(size_t)l + 1], last, t.grids.as<uint32_t>());
+  }
+  if ((e = cudaGetLastError()) != cudaSuccess) return vbuild_fail(e, "grids");
+  // hand over the brick list
+  std::swap(t.cells.p, list[(size_t)levels].p);
+  t.cells.s = s;
+  return YV_OK;
+}
+
+bool lattice_args(const float* density, int levels, Lattice* g, const uint8_t* rgb) {
+  if (!density || levels < 1 || levels > 4) return false;
+  g->d = density;
+  g->rgb = rgb;
+  g->nb = 1 << (2 * levels);
+  g->L = (uint64_t)g->nb * kVB + 1;
+  return true;
+}
+
+}  // namespace
+}  // namespace yv
+
+using namespace yv;
+
+extern "C" {
+
+yv_status yv_volume_build_dense(const float* density, const uint8_t* rgb, int32_t levels,
+                                void* stream, yv_volume_host** out) {
+  if (!out) return YV_ERR_INVALID_ARG;
+  *out = nullptr;
+  Lattice g;
+  if (!lattice_args(density, levels, &g, rgb)) return YV_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  VolumeTree t;
+  yv_status st = build_volume_tree(g, levels, s, t);
+  if (st != YV_OK) return st;
+  const size_t n = (size_t)t.nbricks * kVL3;
+  DevBuf dens, col, cxyz, map;
+  const uint64_t cells = (uint64_t)g.nb * g.nb * g.nb;
+  cudaError_t e;
+  if ((e = dens.alloc(n * 4, s)) != cudaSuccess || (e = col.alloc(n * 3, s)) != cudaSuccess ||
+      (e = cxyz.alloc((size_t)t.nbricks * 12, s)) != cudaSuccess ||
+      (e = map.alloc(cells * 4, s)) != cudaSuccess)
+    return vbuild_fail(e, "alloc");
+  if (t.nbricks)
+    pack_bricks_kernel<<<grid_for((uint64_t)t.nbricks * 32), 256, 0, s>>>(
+        g, t.cells.as<uint64_t>(), t.nbricks, -1, dens.as<float>(), col.as<uint8_t>(), nullptr,
+        nullptr, cxyz.as<int32_t>(), map.as<int32_t>());
+  if ((e = cudaGetLastError()) != cudaSuccess) return vbuild_fail(e, "pack");
+  std::vector<uint32_t> grids((size_t)t.ngrids * 64);
+  std::vector<float> hd(n);
+  std::vector<uint8_t> hc(n * 3);
+  std::vector<int32_t> hcell((size_t)t.nbricks * 3);
+  if ((e = cudaMemcpyAsync(grids.data(), t.grids.p, grids.size() * 4, cudaMemcpyDeviceToHost,
+                           s)) != cudaSuccess ||
+      (n && (e = cudaMemcpyAsync(hd.data(), dens.p, n * 4, cudaMemcpyDeviceToHost, s)) !=
+                cudaSuccess) ||
+      (n && (e = cudaMemcpyAsync(hc.data(), col.p, n * 3, cudaMemcpyDeviceToHost, s)) !=
+                cudaSuccess) ||
+      (t.nbricks && (e = cudaMemcpyAsync(hcell.data(), cxyz.p, hcell.size() * 4,
+                                         cudaMemcpyDeviceToHost, s)) != cudaSuccess) ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return vbuild_fail(e, "download");
+  return volume_host_from_parts(levels, std::move(grids), std::move(hd), std::move(hc),
+                                std::move(hcell), out);
+}
+
+yv_status yv_volume_upload_dense(const float* density, const uint8_t* rgb, int32_t levels,
+                                 int32_t precision, void* stream, yv_volume_gpu** out) {
+  if (!out) return YV_ERR_INVALID_ARG;
+  *out = nullptr;
+  Lattice g;
+  if (!lattice_args(density, levels, &g, rgb) || precision < YV_PRECISION_F16 ||
+      precision > YV_PRECISION_F16_PACKED)
+    return YV_ERR_INVALID_ARG;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  VolumeTree t;
+  yv_status st = build_volume_tree(g, levels, s, t);
+  if (st != YV_OK) return st;
+  const size_t n = (size_t)t.nbricks * kVL3;
+  const uint64_t cells = (uint64_t)g.nb * g.nb * g.nb;
+  size_t dbytes = 0, abytes = 0;
+  switch (precision) {
+    case YV_PRECISION_F16: dbytes = n * 2; abytes = n * 4; break;
+    case YV_PRECISION_F32: dbytes = n * 4; abytes = n * 12; break;
+    case YV_PRECISION_F32_PACKED: abytes = n * 16; break;
+    default: abytes = n * 8; break;
+  }
+  // the device pool (owned by the yv_volume_gpu): grids, density, albedo,
+  // neighbours up / down
+  void* mem[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  const size_t bytes[5] = {(size_t)t.ngrids * 256, dbytes, abytes, (size_t)t.nbricks * 28,
+                           (size_t)t.nbricks * 28};
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 5 && e == cudaSuccess; ++i)
+    if (bytes[i]) e = cudaMalloc(&mem[i], bytes[i]);
+  DevBuf cxyz, map;
+  if (e == cudaSuccess) e = cxyz.alloc((size_t)t.nbricks * 12, s);
+  if (e == cudaSuccess) e = map.alloc(cells * 4, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(map.p, 0xFF, cells * 4, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(mem[0], t.grids.p, bytes[0], cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess && t.nbricks) {
+    pack_bricks_kernel<<<grid_for((uint64_t)t.nbricks * 32), 256, 0, s>>>(
+        g, t.cells.as<uint64_t>(), t.nbricks, precision, nullptr, nullptr, mem[1], mem[2],
+        cxyz.as<int32_t>(), map.as<int32_t>());
+    neighbors_kernel<<<grid_for(t.nbricks), 256, 0, s>>>(
+        cxyz.as<int32_t>(), map.as<int32_t>(), t.nbricks, g.nb, static_cast<int32_t*>(mem[3]),
+        static_cast<int32_t*>(mem[4]));
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    for (void* p : mem) cudaFree(p);
+    return vbuild_fail(e, "device pool");
+  }
+  yv_volume_device d;
+  d.grids = static_cast<const uint32_t*>(mem[0]);
+  d.ngrids = t.ngrids;
+  d.levels = levels;
+  d.density = mem[1];
+  d.albedo = mem[2];
+  d.nbricks = t.nbricks;
+  d.precision = precision;
+  d.nbr_up = static_cast<const int32_t*>(mem[3]);
+  d.nbr_dn = static_cast<const int32_t*>(mem[4]);
+  return volume_gpu_from_device(mem, d, out);
+}
+
+}  // extern "C"

@@ -206,6 +206,27 @@ void fill_neighbors(yv_volume_host* v) {
 }
 
 }  // namespace
+
+yv_status volume_host_from_parts(int levels, std::vector<uint32_t>&& grids,
+                                 std::vector<float>&& density, std::vector<uint8_t>&& albedo,
+                                 std::vector<int32_t>&& cells, yv_volume_host** out) {
+  try {
+    yv_volume_host* v = new yv_volume_host();
+    v->levels = levels;
+    v->nb = 1 << (2 * levels);
+    v->S = v->nb * kB;
+    v->grids = std::move(grids);
+    v->density = std::move(density);
+    v->albedo = std::move(albedo);
+    v->cell = std::move(cells);
+    fill_neighbors(v);
+    *out = v;
+    return YV_OK;
+  } catch (const std::bad_alloc&) {
+    return YV_ERR_OUT_OF_MEMORY;
+  }
+}
+
 }  // namespace yv
 
 using namespace yv;

@@ -91,4 +91,14 @@ yv_status renderer_scene_buffers(yv_renderer* r, uint32_t nn, uint32_t na, uint3
                                  uint32_t** orig, void** attrs);
 void renderer_commit_scene(yv_renderer* r, uint32_t nn, uint32_t na, uint32_t root_word);
 
+// A host brick volume from parts built on the device (volume_host.cpp):
+// grids (ngrids x 64 refs), fp32 lattice values and RGB per brick, brick
+// cells; the apron neighbour tables are derived here.
+yv_status volume_host_from_parts(int levels, std::vector<uint32_t>&& grids,
+                                 std::vector<float>&& density, std::vector<uint8_t>&& albedo,
+                                 std::vector<int32_t>&& cells, yv_volume_host** out);
+// A yv_volume_gpu that owns device buffers mem[0..4] (grids, density,
+// albedo, neighbours up, neighbours down) described by d (api_volume.cpp).
+yv_status volume_gpu_from_device(void* mem[5], const yv_volume_device& d, yv_volume_gpu** out);
+
 }  // namespace yv

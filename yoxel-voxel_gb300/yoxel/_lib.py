@@ -144,6 +144,8 @@ _SIGS = {
     "yv_volume_neighbors": (P, [P, I32]),
     "yv_volume_upload": (S, [P, C.c_int32, C.POINTER(P)]),
     "yv_volume_gpu_free": (None, [P]),
+    "yv_volume_build_dense": (S, [P, P, C.c_int32, P, C.POINTER(P)]),
+    "yv_volume_upload_dense": (S, [P, P, C.c_int32, C.c_int32, P, C.POINTER(P)]),
     "yv_volume_gpu_desc": (S, [P, C.POINTER(VolumeDevice)]),
     "yv_volume_render": (S, [C.POINTER(VolumeDevice), C.POINTER(Camera), C.c_int32, C.c_int32,
                              C.c_int32, C.POINTER(MarchParams), P, P, P, P]),

@@ -44,6 +44,19 @@ class BrickVolume:
         return cls(h.value)
 
     @classmethod
+    def build_dense(cls, density, levels, rgb=None, stream=None):
+        """GPU build of yv_volume_from_dense from a dense CUDA lattice
+        ((8*4^levels + 1)^3 float32, x fastest; rgb optional uint8 x 3),
+        copied into a host container."""
+        _check_lattice(density, levels, rgb)
+        h = C.c_void_p()
+        L.check(L.lib.yv_volume_build_dense(C.c_void_p(density.data_ptr()),
+                                            None if rgb is None else C.c_void_p(rgb.data_ptr()),
+                                            levels, _stream(stream), C.byref(h)),
+                "yv_volume_build_dense")
+        return cls(h.value)
+
+    @classmethod
     def from_dense(cls, levels, density, albedo=None):
         density = np.ascontiguousarray(density, np.float32)
         s = 8 * 4 ** levels + 1
@@ -135,14 +148,38 @@ class BrickVolume:
         )
 
 
-class VolumeGPU:
-    """Library-owned device copy of a BrickVolume (fp16 or fp32 pool)."""
+def _check_lattice(density, levels, rgb):
+    n = 8 * 4 ** int(levels) + 1
+    if not (density.is_cuda and density.is_contiguous() and str(density.dtype) == "torch.float32"
+            and density.numel() == n ** 3):
+        raise ValueError(f"density must be a contiguous CUDA float32 tensor of {n}^3 values")
+    if rgb is not None and not (rgb.is_cuda and rgb.is_contiguous() and
+                                str(rgb.dtype) == "torch.uint8" and rgb.numel() == 3 * n ** 3):
+        raise ValueError(f"rgb must be a contiguous CUDA uint8 tensor of {n}^3 x 3 values")
 
-    def __init__(self, vol, precision):
-        h = C.c_void_p()
-        L.check(L.lib.yv_volume_upload(vol.handle, precision, C.byref(h)), "yv_volume_upload")
+
+class VolumeGPU:
+    """Library-owned device copy of a BrickVolume (any YV_PRECISION_* pool)."""
+
+    def __init__(self, vol, precision, handle=None):
+        h = C.c_void_p(handle) if handle is not None else C.c_void_p()
+        if handle is None:
+            L.check(L.lib.yv_volume_upload(vol.handle, precision, C.byref(h)),
+                    "yv_volume_upload")
         self._h = h
         self.precision = precision
+
+    @classmethod
+    def from_dense(cls, density, levels, precision=L.YV_PRECISION_F16, rgb=None, stream=None):
+        """GPU build from a dense CUDA lattice ((8*4^levels + 1)^3 float32, x
+        fastest; rgb optional uint8 x 3) straight into a device pool."""
+        _check_lattice(density, levels, rgb)
+        h = C.c_void_p()
+        L.check(L.lib.yv_volume_upload_dense(C.c_void_p(density.data_ptr()),
+                                             None if rgb is None else C.c_void_p(rgb.data_ptr()),
+                                             levels, precision, _stream(stream), C.byref(h)),
+                "yv_volume_upload_dense")
+        return cls(None, precision, h.value)
 
     def __del__(self):
         h = getattr(self, "_h", None)
