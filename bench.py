@@ -73,6 +73,10 @@ CONFIGS = {
                   workload="GPU SVO build from a dense 1024^3 float32 density grid (union of "
                            "200 seeded sphere distance fields, iso 0): surface-voxel leaves, "
                            "canonical breadth-first pool straight into the renderer layout"),
+    "vbuild": dict(kind="vbuild", levels=3, precision=3, seed=1234,
+                   workload="GPU brick-volume build from a dense 513^3 float32 lattice (4 "
+                            "seeded sinusoid products - 0.4, clamped to [0, 1]): mark, N=4 tree, "
+                            "pack into the 8-byte fp16+RGB8 device pool"),
     "cfg5": dict(kind="batch", n=32, precision=3,
                  workload="32 seeded scenes (cfg1-type SVO or cfg3-type fp16 bricks), depth "
                           "6..11, resolution 128^2..1024^2, one persistent launch from a global "
@@ -833,6 +837,94 @@ def run_build(args, cfg):
     print(json.dumps(line), flush=True)
 
 
+def wave_lattice(torch, n, seed, device):
+    """(n, n, n) float32 [z, y, x]: clamp(sum of 4 seeded sinusoid products
+    - 0.4, 0, 1)."""
+    rng = np.random.default_rng(seed)
+    ax = torch.arange(n, dtype=torch.float32, device=device) / n
+    acc = torch.zeros((n, n, n), dtype=torch.float32, device=device)
+    for _ in range(4):
+        f = rng.uniform(2, 9, 3)
+        p = rng.uniform(0, 6.28, 3)
+        acc += (torch.sin(ax.view(-1, 1, 1) * float(f[2]) + float(p[2])) *
+                torch.sin(ax.view(1, -1, 1) * float(f[1]) + float(p[1])) *
+                torch.sin(ax.view(1, 1, -1) * float(f[0]) + float(p[0])))
+    return (acc * 0.5 - 0.4).clamp_(0, 1)
+
+
+def run_vbuild(args, cfg):
+    """GPU brick-volume build from a dense lattice, Mvoxels/s of lattice."""
+    import torch
+    import yoxel
+    torch.cuda.set_device(dist_env()[2])
+    levels = cfg["levels"]
+    n = 8 * 4 ** levels + 1
+    lat = wave_lattice(torch, n, cfg["seed"], "cuda")
+    torch.cuda.synchronize()
+    keep = []
+
+    def fn():
+        keep.append(yoxel.VolumeGPU.from_dense(lat, levels, cfg["precision"]))
+        if len(keep) > 1:
+            keep.pop(0)
+
+    for _ in range(args.warmup):
+        fn()
+    torch.cuda.synchronize()
+    host = yoxel.BrickVolume.build_dense(lat, levels)
+    nb = host.nbricks
+    sampler = ClockSampler(dist_env()[2])
+    sampler.start()
+    time.sleep(0.4)
+    ms, wall = _timed_steps(torch, args.steps, fn)
+    clocks = sampler.stop()
+    mean_ms = sum(ms) / len(ms)
+    vox = n ** 3
+    # lattice read once + the 8-byte pool + grid refs
+    alg = 4 * vox + 8 * 729 * nb + 256 * host.ngrids
+    peaks, kind = measured_peaks()
+    achieved = alg / (mean_ms / 1e3) / 1e9
+    line = _base_line(args, cfg, vox / (mean_ms / 1e3) / 1e6, mean_ms, "f32 lattice, fp16+RGB8 pool")
+    line["metric"] = "Mvoxels/s of dense lattice turned into a device brick pool on 1 GB300"
+    line["unit"] = "Mvoxels/s"
+    line["config"].update(lattice=f"{n}^3", bricks=nb, occupancy=round(host.occupancy, 4),
+                          l2="lattice (540 MB) > L2")
+    # end to end: lattice from pinned host memory, build, pool copied to the host
+    hl = torch.empty(lat.shape, dtype=torch.float32, pin_memory=True)
+    hl.copy_(lat)
+    dev = torch.empty_like(lat)
+    torch.cuda.synchronize()
+    te = time.perf_counter()
+    reps = max(1, args.steps // 4)
+    for _ in range(reps):
+        dev.copy_(hl, non_blocking=True)
+        v2 = yoxel.BrickVolume.build_dense(dev, levels)
+        del v2
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - te) / reps
+    line.update({
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"],
+                     "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
+                     "traffic": None, "peak_source": kind, "kernel": "volume build (all passes)",
+                     "algorithmic_bytes_per_step": alg},
+        "e2e": {"value": round(vox / e2e_s / 1e6, 3), "unit": "Mvoxels/s",
+                "h2d_bytes_per_step": 4 * vox, "d2h_bytes_per_step": 4 * 729 * nb * 4,
+                "path": "lattice from pinned host memory, yoxel.BrickVolume.build_dense (pool "
+                        "copied back into a host container)"},
+        "gpu_launches": None, "clocks": clocks, "wall_s_timed_region": round(wall, 4)})
+    if not args.no_cpu_baseline:
+        cpu = lat.cpu().numpy()
+        t0 = time.perf_counter()
+        v = yoxel.BrickVolume.from_dense(levels, cpu)
+        dt = time.perf_counter() - t0
+        assert v.nbricks == nb
+        line["cpu_baseline"] = {"value": round(vox / dt / 1e6, 3), "unit": "Mvoxels/s",
+                                "cores": 1, "kind": "port",
+                                "sample": f"the same {n}^3 lattice built once by the host "
+                                          "RangeBuilder restatement (yv_volume_from_dense)"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -864,6 +956,8 @@ def main():
         return run_batch(args, cfg)
     if cfg["kind"] == "build":
         return run_build(args, cfg)
+    if cfg["kind"] == "vbuild":
+        return run_vbuild(args, cfg)
     raise SystemExit(f"unknown workload kind {cfg['kind']}")
 
 
