@@ -77,6 +77,10 @@ CONFIGS = {
                    workload="GPU brick-volume build from a dense 513^3 float32 lattice (4 "
                             "seeded sinusoid products - 0.4, clamped to [0, 1]): mark, N=4 tree, "
                             "pack into the 8-byte fp16+RGB8 device pool"),
+    "dynsync": dict(kind="dynsync", depth=8, edits=1000, seed=1234,
+                    workload="editable SVO (200 seeded spheres in 256^3): 1000 random voxel "
+                             "edits per step, then a sync of the changed 256-node pages into "
+                             "the device mirror and one 512x512 frame traced from it"),
     "cfg5": dict(kind="batch", n=32, precision=3,
                  workload="32 seeded scenes (cfg1-type SVO or cfg3-type fp16 bricks), depth "
                           "6..11, resolution 128^2..1024^2, one persistent launch from a global "
@@ -925,6 +929,72 @@ def run_vbuild(args, cfg):
     print(json.dumps(line), flush=True)
 
 
+def run_dynsync(args, cfg):
+    """Incremental device sync of an edited SVO: frames per second of the
+    edit -> sync -> trace loop and the bytes each sync moves."""
+    import torch
+    import yoxel
+    torch.cuda.set_device(dist_env()[2])
+    depth = cfg["depth"]
+    scene = yoxel.SVOScene.spheres(depth, 200, 4.0, 24.0, cfg["seed"])
+    dyn = yoxel.DynamicSVO(scene.node_count + 64 * cfg["edits"] * (args.steps + args.warmup + 4),
+                           scene.attr_count + 2 * cfg["edits"] * (args.steps + args.warmup + 4))
+    dyn.load(scene)
+    full_bytes = dyn.transfer_bytes()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    dyn.sync()
+    torch.cuda.synchronize()
+    full_ms = (time.perf_counter() - t0) * 1e3
+    rng = np.random.default_rng(cfg["seed"])
+    G = 1 << depth
+    pos, view = camera()
+    w = h = 512
+
+    def edits():
+        for _ in range(cfg["edits"]):
+            x, y, z = (int(v) for v in rng.integers(0, G, 3))
+            if rng.random() < 0.5:
+                dyn.set_voxel(depth, x, y, z, rgb=(255, 128, 0))
+            else:
+                dyn.set_voxel(depth, x, y, z, None)
+
+    for _ in range(args.warmup):
+        edits()
+        dyn.sync()
+        dyn.render(pos, view, (0, 0, 1), 60.0, w, h, LIGHT)
+    torch.cuda.synchronize()
+    sync_ms, moved, frame_ms = [], [], []
+    for _ in range(args.steps):
+        edits()
+        moved.append(dyn.transfer_bytes())
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        c = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ts = time.perf_counter()
+        a.record()
+        dyn.sync()
+        b.record()
+        dyn.render(pos, view, (0, 0, 1), 60.0, w, h, LIGHT)
+        c.record()
+        torch.cuda.synchronize()
+        sync_ms.append((time.perf_counter() - ts) * 1e3)
+        frame_ms.append(b.elapsed_time(c))
+    mean_sync = sum(sync_ms) / len(sync_ms)
+    mean_frame = sum(frame_ms) / len(frame_ms)
+    step_ms = mean_sync + mean_frame
+    line = _base_line(args, cfg, (w * h) / (step_ms / 1e3) / 1e6, step_ms, "f32")
+    line["metric"] = "Mrays/s of the edit-sync-trace loop on 1 GB300"
+    line["config"].update(scene_nodes=scene.node_count, edits_per_step=cfg["edits"])
+    line.update({
+        "sync_ms_host_wall": round(mean_sync, 4), "frame_ms": round(mean_frame, 4),
+        "bytes_per_sync": int(sum(moved) / len(moved)), "full_upload_bytes": full_bytes,
+        "full_sync_ms": round(full_ms, 3),
+        "roofline": None, "e2e": None, "gpu_launches": None})
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -958,6 +1028,8 @@ def main():
         return run_build(args, cfg)
     if cfg["kind"] == "vbuild":
         return run_vbuild(args, cfg)
+    if cfg["kind"] == "dynsync":
+        return run_dynsync(args, cfg)
     raise SystemExit(f"unknown workload kind {cfg['kind']}")
 
 

@@ -425,6 +425,56 @@ yv_status yv_render_svo_noalloc(const yv_vox_node* nodes, uint32_t count,
                                 int32_t height, const yv_frame_outputs* out,
                                 void* stream);
 
+/* ------------------------------------------------------------------------ */
+/* Editable SVO with incremental device sync (DynamicSVO,                   */
+/* reaction/report/main.tex:67-71; SVORenderer::UpdateSVO,                  */
+/* demo/SVORenderer.cpp:39-53; CountChangedPages / CountTransfrerSize,      */
+/* qtview.py:69-73)                                                         */
+/* ------------------------------------------------------------------------ */
+/* A host VoxNode pool of fixed capacity (free list of node slots) and its
+ * device mirror, both split into pages of 256 nodes (and 256 leaf
+ * attributes) with a version per page bumped on every edit; a sync sends
+ * only the pages changed since the last one (gathered into one pinned
+ * staging copy and scattered on the device).  Frames are traced from the
+ * mirror with yv_render_svo_noalloc (caller node ids).  Not thread-safe. */
+typedef struct yv_svo_dynamic yv_svo_dynamic;
+yv_status yv_svo_dynamic_create(uint32_t node_capacity, uint32_t attr_capacity,
+                                yv_svo_dynamic** out);
+void      yv_svo_dynamic_destroy(yv_svo_dynamic* s);
+/* Replaces the contents with a host scene (all its pages become dirty). */
+yv_status yv_svo_dynamic_load(yv_svo_dynamic* s, const yv_svo_host* svo);
+yv_status yv_svo_dynamic_alloc_node(yv_svo_dynamic* s, uint32_t* id);
+yv_status yv_svo_dynamic_free_node(yv_svo_dynamic* s, uint32_t id);
+yv_status yv_svo_dynamic_set_node(yv_svo_dynamic* s, uint32_t id,
+                                  const yv_vox_node* n);
+yv_status yv_svo_dynamic_get_node(const yv_svo_dynamic* s, uint32_t id,
+                                  yv_vox_node* n);
+yv_status yv_svo_dynamic_add_attr(yv_svo_dynamic* s, const yv_leaf_attr* a,
+                                  uint32_t* index);
+yv_status yv_svo_dynamic_set_attr(yv_svo_dynamic* s, uint32_t index,
+                                  const yv_leaf_attr* a);
+yv_status yv_svo_dynamic_set_root(yv_svo_dynamic* s, uint32_t root,
+                                  int32_t depth);
+/* Sets (a != NULL) or clears one voxel of a 2^depth grid, splitting
+ * EmptyNode / FullNode regions on the way down (no collapse on clear). */
+yv_status yv_svo_dynamic_set_voxel(yv_svo_dynamic* s, int32_t depth,
+                                   uint32_t x, uint32_t y, uint32_t z,
+                                   const yv_leaf_attr* a);
+uint32_t  yv_svo_dynamic_changed_pages(const yv_svo_dynamic* s);
+uint64_t  yv_svo_dynamic_transfer_bytes(const yv_svo_dynamic* s);
+/* Sends the changed pages on `stream` (UpdateSVO). */
+yv_status yv_svo_dynamic_sync(yv_svo_dynamic* s, void* stream);
+/* The device mirror (after a sync) and the host pool. */
+yv_status yv_svo_dynamic_device(const yv_svo_dynamic* s,
+                                const yv_vox_node** nodes, uint32_t* count,
+                                uint32_t* root, const yv_leaf_attr** attrs,
+                                uint32_t* nattrs);
+const yv_vox_node*  yv_svo_dynamic_host_nodes(const yv_svo_dynamic* s);
+const yv_leaf_attr* yv_svo_dynamic_host_attrs(const yv_svo_dynamic* s);
+/* Copies the device mirror back into host arrays (verification). */
+yv_status yv_svo_dynamic_download(const yv_svo_dynamic* s, yv_vox_node* nodes,
+                                  yv_leaf_attr* attrs);
+
 #ifdef __cplusplus
 }
 #endif

@@ -12,8 +12,9 @@ from .volume import (BrickVolume, VolumeGPU, render_volume, volume_backward, vol
                      torch_desc, pack_volume, cameras, sphere_cameras)
 
 from .batch import Batch
+from .dynamic import DynamicSVO
 
 __all__ = ["SVOScene", "Renderer", "CudaRenderer", "YvError", "LIB_PATH", "Batch",
-           "NODE_DTYPE", "ATTR_DTYPE", "BrickVolume", "VolumeGPU", "render_volume",
+           "NODE_DTYPE", "ATTR_DTYPE", "DynamicSVO", "BrickVolume", "VolumeGPU", "render_volume",
            "volume_backward", "volume_march", "torch_desc", "pack_volume", "cameras",
            "sphere_cameras"]

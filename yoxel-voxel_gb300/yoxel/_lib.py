@@ -164,6 +164,25 @@ _SIGS = {
     "yv_batch_render": (S, [P, C.c_int32, P]),
     "yv_batch_render_separate": (S, [P, P]),
     "yv_batch_info": (S, [P, C.POINTER(C.c_uint32), C.POINTER(C.c_uint64)]),
+    "yv_svo_dynamic_create": (S, [U32, U32, C.POINTER(P)]),
+    "yv_svo_dynamic_destroy": (None, [P]),
+    "yv_svo_dynamic_load": (S, [P, P]),
+    "yv_svo_dynamic_alloc_node": (S, [P, C.POINTER(U32)]),
+    "yv_svo_dynamic_free_node": (S, [P, U32]),
+    "yv_svo_dynamic_set_node": (S, [P, U32, P]),
+    "yv_svo_dynamic_get_node": (S, [P, U32, P]),
+    "yv_svo_dynamic_add_attr": (S, [P, P, C.POINTER(U32)]),
+    "yv_svo_dynamic_set_attr": (S, [P, U32, P]),
+    "yv_svo_dynamic_set_root": (S, [P, U32, C.c_int32]),
+    "yv_svo_dynamic_set_voxel": (S, [P, C.c_int32, U32, U32, U32, P]),
+    "yv_svo_dynamic_changed_pages": (U32, [P]),
+    "yv_svo_dynamic_transfer_bytes": (C.c_uint64, [P]),
+    "yv_svo_dynamic_sync": (S, [P, P]),
+    "yv_svo_dynamic_device": (S, [P, C.POINTER(P), C.POINTER(U32), C.POINTER(U32),
+                                  C.POINTER(P), C.POINTER(U32)]),
+    "yv_svo_dynamic_host_nodes": (P, [P]),
+    "yv_svo_dynamic_host_attrs": (P, [P]),
+    "yv_svo_dynamic_download": (S, [P, P, P]),
     "yv_render_svo_noalloc": (S, [P, U32, U32, P, U32, C.POINTER(Camera), C.POINTER(Light),
                                   C.c_int32, C.c_int32, C.POINTER(FrameOutputs), P]),
 }
