@@ -160,6 +160,8 @@ typedef struct yv_light {
  *   fetches   : uint32 per pixel, node dereferences of the primary ray
  *               (RecTrace calls that reach cell/ppu_renderer.cpp:23)
  *   shadow_fetches : uint32 per pixel, same for the shadow ray
+ *   normal    : 3 floats per pixel, the unit normal of the hit leaf's
+ *               attribute (0, 0, 0 for a miss)
  * Row-major, y*width + x. */
 typedef struct yv_frame_outputs {
   void* rgba;
@@ -167,6 +169,7 @@ typedef struct yv_frame_outputs {
   void* hit_t;
   void* fetches;
   void* shadow_fetches;
+  void* normal;
 } yv_frame_outputs;
 
 /* Counters of the last frame (read by yv_renderer_frame_stats). */
@@ -474,6 +477,59 @@ const yv_leaf_attr* yv_svo_dynamic_host_attrs(const yv_svo_dynamic* s);
 /* Copies the device mirror back into host arrays (verification). */
 yv_status yv_svo_dynamic_download(const yv_svo_dynamic* s, yv_vox_node* nodes,
                                   yv_leaf_attr* attrs);
+
+/* ------------------------------------------------------------------------ */
+/* Screen-space normal approximation and point-light shading                */
+/* (SVORenderer::Render with m_ssna, demo/SVORenderer.cpp:88-146; the blur  */
+/* kernel of InitBlur, :55-78; the limited Gaussian depth blur and the      */
+/* depth normals of demo/dumps/ztools.py:23-43, 154-233, 252-266;           */
+/* LightParams as Demo.cpp:141-147 fills them; DumpTraceData, :158-186)     */
+/* ------------------------------------------------------------------------ */
+#define YV_SSNA_MAX_LIGHTS 4
+
+/* Point light: attenuation = 1 / (a0 + a1 d + a2 d^2) at distance d. */
+typedef struct yv_point_light {
+  float pos[3];
+  float diffuse[3];
+  float specular[3];
+  float attenuation[3];
+  int32_t enabled;
+} yv_point_light;
+
+typedef struct yv_ssna_params {
+  int32_t ssna;           /* 1: blur the depth, normals from the depth;
+                             0: the leaves' stored normals              */
+  int32_t show_normals;   /* 1: output the normal as colour n/2 + 1/2  */
+  int32_t blur_passes;    /* depth blur passes (5)                      */
+  float voxel_size;       /* world size of a finest voxel (1/2048)      */
+  float edge_threshold;   /* depth step treated as an edge (4/2048)     */
+  float edge_pad;         /* far taps replaced by d + edge_pad*thr (0.3) */
+  float ambient[3];       /* (0.1, 0.1, 0.1)                            */
+  float specular_exp;     /* Phong exponent (10)                        */
+  yv_point_light lights[YV_SSNA_MAX_LIGHTS];
+} yv_ssna_params;
+
+/* The reference's values; lights[0] = a white light at the eye
+ * (diffuse 0.7, specular 0.3, attenuation (1, 0, 0.5)), others disabled. */
+yv_status yv_ssna_defaults(const yv_renderer* r, yv_ssna_params* p);
+
+/* One frame: an unlit trace (albedo, hit distance, stored normals), the
+ * view depth z = t / |u| (u the pixel's unnormalised ray, forward
+ * component 1), blur_passes limited 5x5 Gaussian passes (pass i blurs the
+ * pixels with z <= 5 voxel_size / (pixel_angle * 3 (i + 1))), normals from
+ * the depth and Phong shading with the point lights.  device_rgba (Color32,
+ * required), device_depth (blurred z, 0 for a miss) and device_normals (3
+ * floats per pixel) are device pointers; the last two are optional.  Async
+ * on `stream`; the trace's counters are read with yv_renderer_frame_stats. */
+yv_status yv_render_ssna(yv_renderer* r, const yv_ssna_params* p,
+                         void* device_rgba, void* device_depth,
+                         void* device_normals, void* stream);
+
+/* DumpTraceData into host arrays (each optional): dist = the hit's ray
+ * distance (0 for a miss), color = the hit leaf's Color32 (0 for a miss),
+ * normal = its unit normal (3 floats, 0 for a miss).  Synchronous. */
+yv_status yv_renderer_trace_dump(yv_renderer* r, float* host_dist,
+                                 uint32_t* host_color, float* host_normal);
 
 #ifdef __cplusplus
 }

@@ -86,3 +86,35 @@ def test_product_package_does_not_import_oracle():
                 for bad in ("pyoracle", "liboracle", "orc_", "import oracle",
                             "from oracle", "yv_oracle"):
                     assert bad not in text, f"{f} references the oracle ({bad})"
+
+
+STRUCTS = {"VoxNode": "yv_vox_node", "LeafAttr": "yv_leaf_attr", "Light": "yv_light",
+           "FrameOutputs": "yv_frame_outputs", "PointLight": "yv_point_light",
+           "SsnaParams": "yv_ssna_params", "FrameStats": "yv_frame_stats",
+           "LaunchConfig": "yv_launch_config", "VolumeDevice": "yv_volume_device",
+           "Camera": "yv_camera", "MarchParams": "yv_march_params"}
+
+
+def test_struct_layouts_match_bindings(yoxel_mod, tmp_path):
+    """Every ctypes mirror has the size and field offsets the C compiler
+    gives the header's struct."""
+    from yoxel import _lib as L
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "yv_c_api.h"',
+             'int main(void) {']
+    expect = []
+    for py, cname in STRUCTS.items():
+        cls = getattr(L, py)
+        lines.append('printf("%%zu\\n", sizeof(%s));' % cname)
+        expect.append(C.sizeof(cls))
+        for f in cls._fields_:
+            lines.append('printf("%%zu\\n", offsetof(%s, %s));' % (cname, f[0]))
+            expect.append(getattr(cls, f[0]).offset)
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    assert got == expect

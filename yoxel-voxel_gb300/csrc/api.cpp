@@ -346,24 +346,34 @@ static void fill_frame_args(const yv_renderer* r, SvoFrameArgs& a) {
 
 namespace yv {
 bool renderer_view(const yv_renderer* r, yv_renderer_view* v) {
-  if (!r || !r->has_scene) return false;
+  if (!r) return false;
   v->sc = r->scene;
   fill_frame_args(r, v->fa);
-  return true;
+  v->fov_deg = r->fov;
+  return r->has_scene;
 }
 }  // namespace yv
 
 extern "C" {
 
-static yv_status enqueue_frame(yv_renderer* r, const yv_frame_outputs* out, cudaStream_t s) {
+// `unlit`: the light is replaced by ambient 1, diffuse 0 and no shadow rays,
+// so rgba carries the hit leaves' albedo.
+static yv_status enqueue_frame(yv_renderer* r, const yv_frame_outputs* out, cudaStream_t s,
+                               bool unlit = false) {
   if (!r->has_scene) return YV_ERR_NO_SCENE;
   SvoFrameArgs a;
   fill_frame_args(r, a);
+  if (unlit) {
+    a.ambient = 1.0f;
+    a.diffuse = 0.0f;
+    a.shadows = 0;
+  }
   a.rgba = static_cast<uint32_t*>(out->rgba);
   a.hit = static_cast<uint32_t*>(out->hit);
   a.hit_t = static_cast<float*>(out->hit_t);
   a.fetches = static_cast<uint32_t*>(out->fetches);
   a.shadow_fetches = static_cast<uint32_t*>(out->shadow_fetches);
+  a.normal = static_cast<float*>(out->normal);
   a.counters = r->d_counters;
   int launches = 0;
   YV_CUDA(launch_svo_frame(r->scene, a, r->cfg, s, &launches), "svo frame launch");
@@ -374,6 +384,18 @@ static yv_status enqueue_frame(yv_renderer* r, const yv_frame_outputs* out, cuda
   r->frame_pending = true;
   return YV_OK;
 }
+
+}  // extern "C"
+
+namespace yv {
+yv_status renderer_enqueue_unlit(yv_renderer* r, const yv_frame_outputs* out, cudaStream_t s) {
+  if (!r || !out) return YV_ERR_INVALID_ARG;
+  YV_CUDA(cudaSetDevice(r->device), "cudaSetDevice");
+  return enqueue_frame(r, out, s, true);
+}
+}  // namespace yv
+
+extern "C" {
 
 yv_status yv_render_frame_async(yv_renderer* r, const yv_frame_outputs* out, void* stream) {
   if (!r || !out) return YV_ERR_INVALID_ARG;

@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
                                           leaf, err);
     if (r == kContinue) continue;
     if (mode == kShadow) {
-      write_pixel(it.fa, off, shade(attr, it.fa, r == kHit), hitw, ht, fp, tr.fetches);
+      write_pixel(it.fa, off, shade(attr, it.fa, r == kHit), hitw, ht, fp, tr.fetches, attr);
       mode = kIdle;
     } else if (r == kMiss) {
       write_pixel(it.fa, off, 0u, 0xFFFFFFFFu, 0.f, tr.fetches, 0u);
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
         err |= YV_DEV_ERR_POOL;
       mode = kIdle;
       if (!it.fa.shadows) {
-        write_pixel(it.fa, off, shade(attr, it.fa, false), hitw, ht, fp, 0u);
+        write_pixel(it.fa, off, shade(attr, it.fa, false), hitw, ht, fp, 0u, attr);
       } else {
         float o[3];
         o[0] = __fadd_rn(it.fa.pos[0], __fmul_rn(dx, ht));
@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
                         it.fa.light_ray[2], tr, err))
           mode = kShadow;
         else
-          write_pixel(it.fa, off, shade(attr, it.fa, false), hitw, ht, fp, tr.fetches);
+          write_pixel(it.fa, off, shade(attr, it.fa, false), hitw, ht, fp, tr.fetches, attr);
       }
     }
   }

@@ -107,6 +107,7 @@ extern "C" yv_status yv_render_svo_noalloc(const yv_vox_node* nodes, uint32_t co
   a.hit_t = static_cast<float*>(out->hit_t);
   a.fetches = static_cast<uint32_t*>(out->fetches);
   a.shadow_fetches = static_cast<uint32_t*>(out->shadow_fetches);
+  a.normal = static_cast<float*>(out->normal);
   a.counters = scratch;
 
   cudaStream_t s = static_cast<cudaStream_t>(stream);

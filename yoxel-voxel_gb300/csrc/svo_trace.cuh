@@ -349,13 +349,21 @@ __device__ __forceinline__ uint32_t shade(uint4 at, const SvoFrameArgs& a, bool 
   return out;
 }
 
+// `at` is the hit leaf's shading record (zero for a miss): its normal goes to
+// the optional per-pixel normal output.
 __device__ __forceinline__ void write_pixel(const SvoFrameArgs& a, uint32_t off, uint32_t rgba,
-                                            uint32_t hitw, float ht, uint32_t f, uint32_t fs) {
+                                            uint32_t hitw, float ht, uint32_t f, uint32_t fs,
+                                            uint4 at = make_uint4(0u, 0u, 0u, 0u)) {
   if (a.rgba) a.rgba[off] = rgba;
   if (a.hit) a.hit[off] = hitw;
   if (a.hit_t) a.hit_t[off] = ht;
   if (a.fetches) a.fetches[off] = f;
   if (a.shadow_fetches) a.shadow_fetches[off] = fs;
+  if (a.normal) {
+    a.normal[3u * off] = __uint_as_float(at.y);
+    a.normal[3u * off + 1u] = __uint_as_float(at.z);
+    a.normal[3u * off + 2u] = __uint_as_float(at.w);
+  }
 }
 
 // kMinBlocks: resident 256-thread blocks per SM the register allocation is
@@ -437,7 +445,7 @@ __global__ void __launch_bounds__(256, kMinBlocks)
           // end of a shadow ray
           const bool sh = r == kHit;
           my_shadowed += sh ? 1u : 0u;
-          write_pixel(a, off, shade(attr, a, sh), hitw, ht, fp, tr.fetches);
+          write_pixel(a, off, shade(attr, a, sh), hitw, ht, fp, tr.fetches, attr);
           mode = kIdle;
         } else if (r == kMiss) {
           write_pixel(a, off, 0u, 0xFFFFFFFFu, 0.f, tr.fetches, 0u);
@@ -470,9 +478,9 @@ __global__ void __launch_bounds__(256, kMinBlocks)
                             a.light_ray[2], tr, err))
               mode = kShadow;
             else
-              write_pixel(a, off, shade(attr, a, false), hitw, ht, fp, tr.fetches);
+              write_pixel(a, off, shade(attr, a, false), hitw, ht, fp, tr.fetches, attr);
           } else {
-            write_pixel(a, off, shade(attr, a, false), hitw, ht, fp, 0u);
+            write_pixel(a, off, shade(attr, a, false), hitw, ht, fp, 0u, attr);
           }
         }
       }

@@ -44,7 +44,12 @@ cudaError_t launch_batch(const BatchLaunch& b, const LaunchCfg& cfg, cudaStream_
 struct yv_renderer_view {
   SvoDeviceScene sc;
   SvoFrameArgs fa;
+  float fov_deg;
 };
 bool renderer_view(const yv_renderer* r, yv_renderer_view* v);
+
+// Enqueues the renderer's frame unlit (ambient 1, diffuse 0, no shadow rays:
+// rgba = the hit leaves' albedo) into `out`; counters as for any frame.
+yv_status renderer_enqueue_unlit(yv_renderer* r, const yv_frame_outputs* out, cudaStream_t s);
 
 }  // namespace yv

@@ -34,6 +34,7 @@ struct SvoFrameArgs {
   float* hit_t;
   uint32_t* fetches;
   uint32_t* shadow_fetches;
+  float* normal;                 // 3 floats per pixel
   uint32_t* counters;            // device scratch, kSvoCounterWords words
 };
 

@@ -53,7 +53,25 @@ class Light(C.Structure):
 
 class FrameOutputs(C.Structure):
     _fields_ = [("rgba", C.c_void_p), ("hit", C.c_void_p), ("hit_t", C.c_void_p),
-                ("fetches", C.c_void_p), ("shadow_fetches", C.c_void_p)]
+                ("fetches", C.c_void_p), ("shadow_fetches", C.c_void_p),
+                ("normal", C.c_void_p)]
+
+
+YV_SSNA_MAX_LIGHTS = 4
+
+
+class PointLight(C.Structure):
+    _fields_ = [("pos", C.c_float * 3), ("diffuse", C.c_float * 3),
+                ("specular", C.c_float * 3), ("attenuation", C.c_float * 3),
+                ("enabled", C.c_int32)]
+
+
+class SsnaParams(C.Structure):
+    _fields_ = [("ssna", C.c_int32), ("show_normals", C.c_int32),
+                ("blur_passes", C.c_int32), ("voxel_size", C.c_float),
+                ("edge_threshold", C.c_float), ("edge_pad", C.c_float),
+                ("ambient", C.c_float * 3), ("specular_exp", C.c_float),
+                ("lights", PointLight * YV_SSNA_MAX_LIGHTS)]
 
 
 class FrameStats(C.Structure):
@@ -185,6 +203,9 @@ _SIGS = {
     "yv_svo_dynamic_download": (S, [P, P, P]),
     "yv_render_svo_noalloc": (S, [P, U32, U32, P, U32, C.POINTER(Camera), C.POINTER(Light),
                                   C.c_int32, C.c_int32, C.POINTER(FrameOutputs), P]),
+    "yv_ssna_defaults": (S, [P, C.POINTER(SsnaParams)]),
+    "yv_render_ssna": (S, [P, C.POINTER(SsnaParams), P, P, P, P]),
+    "yv_renderer_trace_dump": (S, [P, P, P, P]),
 }
 
 

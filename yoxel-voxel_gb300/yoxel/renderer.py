@@ -131,11 +131,13 @@ class Renderer:
         return np.array(d0, np.float32), np.array(du, np.float32), np.array(dv, np.float32)
 
     def render_async(self, rgba=None, hit=None, hit_t=None, fetches=None,
-                     shadow_fetches=None, stream=None):
-        """Enqueues a frame into caller-owned CUDA tensors (each optional)."""
+                     shadow_fetches=None, normal=None, stream=None):
+        """Enqueues a frame into caller-owned CUDA tensors (each optional;
+        normal is (h, w, 3) float32)."""
         def ptr(t):
             return None if t is None else C.c_void_p(t.data_ptr())
-        o = L.FrameOutputs(ptr(rgba), ptr(hit), ptr(hit_t), ptr(fetches), ptr(shadow_fetches))
+        o = L.FrameOutputs(ptr(rgba), ptr(hit), ptr(hit_t), ptr(fetches), ptr(shadow_fetches),
+                           ptr(normal))
         L.check(L.lib.yv_render_frame_async(self._h, C.byref(o), _stream_ptr(stream)),
                 "yv_render_frame_async")
 
@@ -171,6 +173,74 @@ class Renderer:
         L.check(L.lib.yv_get_device_scene_info(self._h, C.byref(n), C.byref(b)),
                 "yv_get_device_scene_info")
         return n.value, b.value
+
+    # ---- screen-space normals + point lights (SVORenderer::Render) ----------
+    def ssna_params(self):
+        """The reference's SSNA defaults (5 blur passes, voxel 1/2048,
+        ambient 0.1, specular exponent 10, a white light at the eye) as a
+        mutable L.SsnaParams."""
+        p = L.SsnaParams()
+        L.check(L.lib.yv_ssna_defaults(self._h, C.byref(p)), "yv_ssna_defaults")
+        return p
+
+    @staticmethod
+    def set_point_light(params, i, pos, diffuse=(0.7, 0.7, 0.7), specular=(0.3, 0.3, 0.3),
+                        attenuation=(1.0, 0.0, 0.5), enabled=True):
+        """SVORenderer::SetLigth (demo/SVORenderer.h:34) on a params block."""
+        if not 0 <= i < L.YV_SSNA_MAX_LIGHTS:
+            raise ValueError("light index out of range")
+        lp = params.lights[i]
+        lp.pos[:] = [float(v) for v in pos]
+        lp.diffuse[:] = [float(v) for v in diffuse]
+        lp.specular[:] = [float(v) for v in specular]
+        lp.attenuation[:] = [float(v) for v in attenuation]
+        lp.enabled = 1 if enabled else 0
+
+    def render_ssna(self, params=None, rgba=None, depth=None, normals=None, stream=None):
+        """Enqueues an SSNA frame into CUDA tensors: rgba (h, w) int32
+        (allocated when None), optional depth (h, w) float32 and normals
+        (h, w, 3) float32.  Returns rgba."""
+        torch = _torch()
+        w, h = self.GetResolution()
+        if params is None:
+            params = self.ssna_params()
+        if rgba is None:
+            rgba = torch.empty((h, w), dtype=torch.int32,
+                               device=torch.device("cuda", torch.cuda.current_device()))
+        for t, shape in ((rgba, (h, w)), (depth, (h, w)), (normals, (h, w, 3))):
+            if t is not None and (tuple(t.shape) != shape or not t.is_cuda
+                                  or not t.is_contiguous() or t.element_size() != 4):
+                raise ValueError("render_ssna outputs must be contiguous 4-byte CUDA tensors "
+                                 "of shape %s" % (shape,))
+
+        def ptr(t):
+            return None if t is None else C.c_void_p(t.data_ptr())
+        L.check(L.lib.yv_render_ssna(self._h, C.byref(params), ptr(rgba), ptr(depth),
+                                     ptr(normals), _stream_ptr(stream)), "yv_render_ssna")
+        return rgba
+
+    def trace_dump(self):
+        """DumpTraceData into arrays: dist (h, w) float32, color (h, w, 4)
+        uint8, normal (h, w, 3) float32 (zero for misses)."""
+        w, h = self.GetResolution()
+        dist = np.empty((h, w), np.float32)
+        color = np.empty((h, w), np.uint32)
+        normal = np.empty((h, w, 3), np.float32)
+        L.check(L.lib.yv_renderer_trace_dump(self._h, dist.ctypes.data, color.ctypes.data,
+                                             normal.ctypes.data), "yv_renderer_trace_dump")
+        return dist, color.view(np.uint8).reshape(h, w, 4), normal
+
+    def DumpTraceData(self, fnbase):
+        """SVORenderer::DumpTraceData (demo/SVORenderer.cpp:158-186): writes
+        <fnbase>_<w>x<h>.dist (float32), .color (Color32) and .normal (3
+        float32) per pixel, row-major."""
+        w, h = self.GetResolution()
+        dist, color, normal = self.trace_dump()
+        base = "%s_%dx%d" % (fnbase, w, h)
+        dist.tofile(base + ".dist")
+        color.tofile(base + ".color")
+        normal.tofile(base + ".normal")
+        return base
 
 
 class CudaRenderer:
