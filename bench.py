@@ -81,6 +81,13 @@ CONFIGS = {
                     workload="editable SVO (200 seeded spheres in 256^3): 1000 random voxel "
                              "edits per step, then a sync of the changed 256-node pages into "
                              "the device mirror and one 512x512 frame traced from it"),
+    "ssna": dict(kind="ssna", scene=("terrain", dict(depth=11, n_cubes=10000, cube_min=2,
+                                                     cube_max=16, seed=1234)),
+                 width=1920, height=1080, passes=5,
+                 workload="cfg2 scene and camera (2048^3 SVO terrain), 1920x1080: unlit trace "
+                          "(albedo, hit distance, leaf normal), view depth, 5 depth-limited 5x5 "
+                          "blur passes (voxel 1/2048), depth normals, Phong with one point light "
+                          "at the eye"),
     "cfg5": dict(kind="batch", n=32, precision=3,
                  workload="32 seeded scenes (cfg1-type SVO or cfg3-type fp16 bricks), depth "
                           "6..11, resolution 128^2..1024^2, one persistent launch from a global "
@@ -995,6 +1002,125 @@ def run_dynsync(args, cfg):
     print(json.dumps(line), flush=True)
 
 
+def run_ssna(args, cfg):
+    """Screen-space normal approximation frame (trace + post passes): pixels
+    per second of the whole frame; the post chain timed against the unlit
+    trace alone."""
+    import ctypes as C
+
+    import torch
+    import yoxel
+    from yoxel import _lib as L
+    torch.cuda.set_device(dist_env()[2])
+    scene = make_scene(cfg)
+    pos, view = camera()
+    w, h = cfg["width"], cfg["height"]
+    npix = w * h
+    r = yoxel.Renderer()
+    r.SetScene(scene)
+    r.SetViewPos(pos)
+    r.SetViewDir(view)
+    r.SetViewUp([0, 0, 1])
+    r.SetResolution(w, h)
+    r.SetFOV(60.0)
+    r.SetLight(LIGHT, 1.0, 0.0, False)
+    p = r.ssna_params()
+    p.blur_passes = cfg["passes"]
+    dev = torch.device("cuda", torch.cuda.current_device())
+    rgba = torch.empty((h, w), dtype=torch.int32, device=dev)
+    alb = torch.empty((h, w), dtype=torch.int32, device=dev)
+    ht = torch.empty((h, w), dtype=torch.float32, device=dev)
+    nrm = torch.empty((h, w, 3), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def frame():
+        r.render_ssna(p, rgba=rgba, stream=stream)
+
+    def unlit():
+        r.render_async(rgba=alb, hit_t=ht, normal=nrm, stream=stream)
+
+    for _ in range(args.warmup):
+        frame()
+        unlit()
+    st = r.frame_stats()
+    sampler = ClockSampler(dist_env()[2])
+    sampler.start()
+    time.sleep(0.4)
+    ms, wall = _timed_steps(torch, args.steps, frame, flush=lambda: flush.fill_(1))
+    ms_trace, _ = _timed_steps(torch, args.steps, unlit, flush=lambda: flush.fill_(1))
+    clocks = sampler.stop()
+    st = r.frame_stats()
+    mean = sum(ms) / len(ms)
+    mean_trace = sum(ms_trace) / len(ms_trace)
+    post_ms = max(mean - mean_trace, 1e-6)
+    # algorithmic bytes of the post chain per pixel: depth (albedo + t in, z
+    # out: 12), each blur pass (z in + out: 8), shading (albedo, z, stored
+    # normal in, rgba out: 24)
+    post_bytes = npix * (12 + 8 * cfg["passes"] + 24)
+    peaks, peak_kind = measured_peaks()
+    achieved = post_bytes / (post_ms / 1e3) / 1e9
+
+    # end to end: yv_render_ssna + the frame read back into pinned memory
+    host = torch.empty((h, w), dtype=torch.int32, pin_memory=True)
+    torch.cuda.synchronize()
+    te = time.perf_counter()
+    for _ in range(args.steps):
+        frame()
+        host.copy_(rgba, non_blocking=True)
+        stream.synchronize()
+    e2e_s = (time.perf_counter() - te) / args.steps
+    r.frame_stats()
+
+    line = _base_line(args, cfg, npix / (mean / 1e3) / 1e6, mean, "f32")
+    line["metric"] = "Mpixels/s of the SSNA frame (trace + post passes) on 1 GB300"
+    line["unit"] = "Mpixels/s"
+    line["config"].update(pixels=npix, blur_passes=cfg["passes"])
+    line.update({
+        "unlit_trace_ms": round(mean_trace, 4), "post_chain_ms": round(post_ms, 4),
+        "post_chain_mpix_s": round(npix / (post_ms / 1e3) / 1e6, 2),
+        "wall_s_timed_region": round(wall, 4),
+        "roofline": {"bound": "hbm", "kernel": "post chain (depth + blur passes + shade)",
+                     "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
+                     "peak_source": peak_kind, "algorithmic_bytes_per_step": post_bytes,
+                     "note": "the 8 MB depth buffers stay in L2 between passes"},
+        "e2e": {"value": round(npix / e2e_s / 1e6, 3), "unit": "Mpixels/s",
+                "h2d_bytes_per_step": C.sizeof(L.SsnaParams),
+                "d2h_bytes_per_step": npix * 4,
+                "path": "yv_render_ssna (C ABI) + frame copy into pinned host memory"},
+        "gpu_launches": (int(st["launches"]) + 2 + cfg["passes"]) * args.steps,
+        "clocks": clocks})
+    if not args.no_cpu_baseline:
+        from oracle import ssna as O
+        r.render_async(rgba=alb, hit_t=ht, normal=nrm, stream=stream)
+        r.frame_stats()
+        sw, sh = w // 4, h // 4
+        y0, x0 = (h - sh) // 2, (w - sw) // 2
+        a_np = alb.cpu().numpy().view(np.uint32)[y0:y0 + sh, x0:x0 + sw]
+        t_np = ht.cpu().numpy()[y0:y0 + sh, x0:x0 + sw]
+        n_np = nrm.cpu().numpy()[y0:y0 + sh, x0:x0 + sw]
+        d0, du, dv = r.ray_basis()
+        d0 = (d0 + du * np.float32(x0) + dv * np.float32(y0)).astype(np.float32)
+        lt = p.lights[0]
+        light = dict(pos=list(lt.pos), diffuse=list(lt.diffuse), specular=list(lt.specular),
+                     attenuation=list(lt.attenuation))
+        runs, tc = 0, time.perf_counter()
+        while True:
+            O.ssna_frame(a_np, t_np, n_np, pos, d0, du, dv, 60.0, passes=cfg["passes"],
+                         lights=[light])
+            runs += 1
+            if time.perf_counter() - tc > 10.0 or runs >= 200:
+                break
+        cpu_s = (time.perf_counter() - tc) / runs
+        line["cpu_baseline"] = {
+            "value": round(sw * sh / cpu_s / 1e6, 4), "unit": "Mpixels/s", "cores": 1,
+            "kind": "port",
+            "sample": f"post chain only on the central {sw}x{sh} crop of the device's unlit "
+                      f"trace, numpy FP32 restatement, {runs} runs"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1030,6 +1156,8 @@ def main():
         return run_vbuild(args, cfg)
     if cfg["kind"] == "dynsync":
         return run_dynsync(args, cfg)
+    if cfg["kind"] == "ssna":
+        return run_ssna(args, cfg)
     raise SystemExit(f"unknown workload kind {cfg['kind']}")
 
 

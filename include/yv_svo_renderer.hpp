@@ -7,6 +7,10 @@
  *                                            SetResolution, GetResolution,
  *                                            SetFOV, RenderFrame)
  *   CreateSimpleRenderer / CreateThreadedRenderer  cell/svorenderer.h:26-27
+ *   LightParams, SetSSNA / SetShowNormals / SetLigth, Render(d_dstBuf),
+ *   DumpTraceData   demo/SVORenderer.h:8-64 (the point-light renderer with
+ *                   screen-space normals; lights start disabled as the
+ *                   SVORenderer constructor leaves them)
  *
  * Semantics kept from the reference: SetScene stores a non-owning pointer
  * (RendererBase::SetScene, cell/renderer_base.h:28; the pool is copied to
@@ -20,7 +24,9 @@
 #pragma once
 
 #include <cstdint>
+#include <cstdio>
 #include <memory>
+#include <string>
 #include <vector>
 
 #include "yv_c_api.h"
@@ -115,6 +121,13 @@ class ISVORenderer {
 };
 
 /* The GB300 renderer behind ISVORenderer. */
+/* LightParams as demo/Demo.cpp:141-147 fills it: attenuation
+ * 1 / (c.x + c.y d + c.z d^2). */
+struct LightParams {
+  bool enabled = false;
+  point_3f pos, diffuse, specular, attenuationCoefs;
+};
+
 class GPURenderer : public ISVORenderer {
  public:
   GPURenderer() { status_ = yv_renderer_create(&r_); }
@@ -171,13 +184,73 @@ class GPURenderer : public ISVORenderer {
   yv_status Status() const { return status_; }
   yv_renderer* Handle() const { return r_; }
 
+  /* demo/SVORenderer.h:28-36: screen-space normals, normal display, the
+   * point lights and a frame into a device RGBA8 buffer (async on the
+   * default stream). */
+  void SetSSNA(bool enable) { Ssna().ssna = enable ? 1 : 0; }
+  bool GetSSNA() { return Ssna().ssna != 0; }
+  void SetShowNormals(bool enable) { Ssna().show_normals = enable ? 1 : 0; }
+  bool GetShowNormals() { return Ssna().show_normals != 0; }
+  void SetLigth(int i, const LightParams& lp) {
+    if (i < 0 || i >= YV_SSNA_MAX_LIGHTS) {
+      status_ = YV_ERR_INVALID_ARG;
+      return;
+    }
+    yv_point_light& l = Ssna().lights[i];
+    l.enabled = lp.enabled ? 1 : 0;
+    const point_3f* src[4] = {&lp.pos, &lp.diffuse, &lp.specular, &lp.attenuationCoefs};
+    float* dst[4] = {l.pos, l.diffuse, l.specular, l.attenuation};
+    for (int k = 0; k < 4; ++k) {
+      dst[k][0] = src[k]->x;
+      dst[k][1] = src[k]->y;
+      dst[k][2] = src[k]->z;
+    }
+  }
+  yv_ssna_params& SsnaParams() { return Ssna(); }
+  void Render(void* d_dstBuf) {
+    if (!r_) return;
+    status_ = yv_render_ssna(r_, &Ssna(), d_dstBuf, nullptr, nullptr, nullptr);
+  }
+  /* demo/SVORenderer.cpp:158-186: <fnbase>_<w>x<h>.dist / .color /
+   * .normal, one float, Color32 and 3 floats per pixel. */
+  bool DumpTraceData(const std::string& fnbase) {
+    if (!r_) return false;
+    const point_2i res = GetResolution();
+    const size_t n = (size_t)res.x * (size_t)res.y;
+    std::vector<float> dist(n), normal(3 * n);
+    std::vector<uint32_t> color(n);
+    status_ = yv_renderer_trace_dump(r_, dist.data(), color.data(), normal.data());
+    if (status_ != YV_OK) return false;
+    const std::string base =
+        fnbase + "_" + std::to_string(res.x) + "x" + std::to_string(res.y);
+    return WriteFile(base + ".dist", dist.data(), n * 4) &&
+           WriteFile(base + ".color", color.data(), n * 4) &&
+           WriteFile(base + ".normal", normal.data(), n * 12);
+  }
+
  private:
+  yv_ssna_params& Ssna() {
+    if (!ssna_init_) {
+      if (r_) yv_ssna_defaults(r_, &ssna_);
+      for (int i = 0; i < YV_SSNA_MAX_LIGHTS; ++i) ssna_.lights[i].enabled = 0;
+      ssna_init_ = true;
+    }
+    return ssna_;
+  }
+  static bool WriteFile(const std::string& fn, const void* p, size_t bytes) {
+    FILE* f = std::fopen(fn.c_str(), "wb");
+    if (!f) return false;
+    const bool ok = std::fwrite(p, 1, bytes, f) == bytes;
+    return std::fclose(f) == 0 && ok;
+  }
   void Vec(yv_status (*fn)(yv_renderer*, const float*), const point_3f& p) {
     if (!r_) return;
     const float v[3] = {p.x, p.y, p.z};
     status_ = fn(r_, v);
   }
   yv_renderer* r_ = nullptr;
+  yv_ssna_params ssna_{};
+  bool ssna_init_ = false;
   SVOData* scene_ = nullptr;
   std::vector<Color32> buf_;
   yv_status status_ = YV_OK;

@@ -21,7 +21,9 @@ the device passes use:
     positions z * u instead of its small-angle form, turned toward the eye;
   - Phong point lights with LightParams (Demo.cpp:141-147):
     albedo * (ambient + diffuse * max(n.L, 0) * att)
-    + specular * max(R.V, 0)^e * att, att = 1 / (a0 + a1 d + a2 d^2).
+    + specular * max(R.V, 0)^e * att, att = 1 / (a0 + a1 d + a2 d^2),
+    evaluated as n.L = (n.lv) / d and R.V = (lv.u - 2 (n.L) (n.u) d) / (d |u|)
+    (lv = light - P, u the pixel's ray, R = 2 (n.L) n - L, V = -u / |u|).
 Parity status: the reference's BlurZ / ShadeSimple CUDA kernels are absent
 from its snapshot, so this restatement is unpinned against reference outputs;
 it pins the device passes to this specification.
@@ -153,34 +155,32 @@ def shade(albedo, z, stored_n, pos, dir0, du, dv, ssna=True, show_normals=False,
             cr = np.where(flip[..., None], -cr, cr)
             len2 = _dot(cr, cr)
             ok = okx & oky & (len2 > 0) & (len2 <= FLT_MAX)
-            nn = cr / np.sqrt(len2)[..., None]
+            inv = F(1) / np.sqrt(len2)
+            nn = cr * inv[..., None]
             n = np.where(ok[..., None], nn, n)
         if show_normals:
             rgb = [_to_u8(n[..., i] * F(0.5) + F(0.5)) for i in range(3)]
         else:
-            a = [((albedo >> (8 * i)) & 0xFF).astype(F) / F(255) for i in range(3)]
+            a = [((albedo >> (8 * i)) & 0xFF).astype(F) * (F(1) / F(255)) for i in range(3)]
             col = [a[i] * F(ambient[i]) for i in range(3)]
             ulen = np.sqrt(_dot(u, u))
-            vv = -u / ulen[..., None]
+            nu = _dot(n, u)
             for lt in lights:
                 lpos = np.asarray(lt["pos"], F)
                 lv = np.stack([F(lpos[i]) - (F(pos[i]) + p[..., i]) for i in range(3)], -1)
                 d2 = _dot(lv, lv)
                 d = np.sqrt(d2)
-                lok = d > 0
-                L = lv / d[..., None]
+                ndl = _dot(n, lv) / d
+                dok = (d > 0) & (ndl > 0)
                 at = np.asarray(lt["attenuation"], F)
                 den = (at[0] + at[1] * d) + at[2] * d2
                 att = np.where(den > 0, F(1) / den, F(0))
-                ndl = _dot(n, L)
-                dok = lok & (ndl > 0)
                 na = ndl * att
                 dif = np.asarray(lt["diffuse"], F)
                 for i in range(3):
                     col[i] = np.where(dok, col[i] + a[i] * (na * dif[i]), col[i])
-                two = F(2) * ndl
-                R = np.stack([two * n[..., i] - L[..., i] for i in range(3)], -1)
-                rv = _dot(R, vv)
+                num = _dot(lv, u) - ((F(2) * ndl) * nu) * d
+                rv = num / (d * ulen)
                 sok = dok & (rv > 0)
                 sp = np.power(np.where(sok, rv, F(1)), F(specular_exp)).astype(F) * att
                 spec = np.asarray(lt["specular"], F)

@@ -3,10 +3,12 @@
 // camera, render one frame and write it as raw RGBA8 (uint32 per pixel).
 //
 // usage: render_svo host <vox path>          (no GPU: host-side API only)
-//        render_svo gpu  <vox path> <out.raw> (one 64x48 frame)
+//        render_svo gpu  <vox path> <out.raw> (one 64x48 frame, plus the
+//                                             trace dump <out.raw>.dmp_64x48.*)
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <string>
 
 #include "yv_svo_renderer.hpp"
 
@@ -52,6 +54,10 @@ int main(int argc, char** argv) {
   if (!out) return 14;
   std::fwrite(f, sizeof(yv::Color32), (size_t)res.x * res.y, out);
   std::fclose(out);
+  // SVORenderer::DumpTraceData: <base>_64x48.dist / .color / .normal
+  g->SetSSNA(true);
+  if (!g->GetSSNA() || g->GetShowNormals()) return 15;
+  if (!g->DumpTraceData(std::string(argv[3]) + ".dmp")) return 16;
   std::printf("frame written\n");
   return 0;
 }

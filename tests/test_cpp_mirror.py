@@ -51,3 +51,12 @@ def test_cpp_mirror_renders_oracle_frame(tmp_path, oracle):
                             f32(-0.6, 0.05, -0.22), f32(0, 0, 1), 55.0, 64, 48, light, 0.15,
                             0.85, True)
     assert np.array_equal(got, ref["rgba"].reshape(48, 64).astype(np.uint32))
+    # the trace dump: distances of the hits, colours with alpha set on hits
+    dist = np.fromfile(raw + ".dmp_64x48.dist", np.float32).reshape(48, 64)
+    color = np.fromfile(raw + ".dmp_64x48.color", np.uint32).reshape(48, 64)
+    normal = np.fromfile(raw + ".dmp_64x48.normal", np.float32).reshape(48, 64, 3)
+    hits = ref["hit"].reshape(48, 64) != 0xFFFFFFFF
+    assert np.array_equal(dist[hits], ref["hit_t"].reshape(48, 64)[hits])
+    assert np.array_equal((color >> 24) != 0, hits)
+    nl = np.linalg.norm(normal[hits], axis=-1)
+    assert np.all((np.abs(nl - 1.0) < 1e-5) | (nl == 0)) and (nl > 0).mean() > 0.9

@@ -94,7 +94,7 @@ def fine_voxel(p):
 
 
 @pytest.mark.parametrize("case", ["default", "fine_voxel", "two_lights", "show_normals",
-                                  "stored_normals", "close_up"])
+                                  "stored_normals", "close_up", "one_pass", "many_passes"])
 def test_ssna_matches_oracle(yoxel_mod, spheres, case):
     r, pos = make_renderer(yoxel_mod, spheres, dist=0.9 if case == "close_up" else 1.5)
     p = r.ssna_params()
@@ -109,13 +109,18 @@ def test_ssna_matches_oracle(yoxel_mod, spheres, case):
         p.show_normals = 1
     if case == "stored_normals":
         p.ssna = 0
+    if case == "one_pass":
+        p.blur_passes = 1
+    if case == "many_passes":
+        # more passes than the fused one-launch chain takes: one launch per pass
+        p.blur_passes = 9
     tr = unlit_trace(r)
     hits = (tr["rgba"] >> 24) != 0
     assert hits.mean() > 0.2
     got = run_ssna(r, p)
     want = oracle_frame(r, pos, tr, p)
     assert_close(got, want)
-    if case in ("fine_voxel", "close_up"):
+    if case in ("fine_voxel", "close_up", "many_passes"):
         # the blur changed the depth of some pixels
         z0 = O.depth(tr["rgba"], tr["hit_t"], *r.ray_basis())
         assert (got[1][hits] != z0[hits]).mean() > 0.05

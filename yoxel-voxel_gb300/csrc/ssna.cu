@@ -32,8 +32,11 @@
 // the depth and normals are reproducible on the CPU; the specular power is
 // powf.
 //
-// Cost at 1024^2: each pass streams 4 MB in and out of L2 with a shared
-// 36x12 tile per 32x8 block; the frame kernel dominates.
+// Launch shape: every pass works on 32x32-pixel tiles with 256 threads, 4
+// pixels a thread, and issues all of a thread's global loads before it uses
+// any, so the depth-buffer passes (8 MB in, 8 MB out at 1920x1080, L2
+// resident) are not bound by load latency.  A pass whose limit blurs no pixel
+// is a copy.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -49,8 +52,11 @@ namespace yv {
 namespace {
 
 constexpr float kFar = 1e30f;
-constexpr int kTileX = 32, kTileY = 8, kHalo = 2;
-constexpr int kSmemX = kTileX + 2 * kHalo, kSmemY = kTileY + 2 * kHalo;
+constexpr int kTX = 32, kTY = 8;       // threads of a block
+constexpr int kTile = 32;              // kTile x kTile pixels per block
+constexpr int kRowsPer = kTile / kTY;  // pixels (rows) per thread
+constexpr int kHalo = 2;
+constexpr int kSm = kTile + 2 * kHalo;  // shared tile side of the blur
 
 struct BlurWeights {
   float k[25];  // [oy + 2][ox + 2]
@@ -85,91 +91,133 @@ __device__ __forceinline__ float dot3(const float a[3], const float b[3]) {
                    __fmul_rn(a[2], b[2]));
 }
 
-__global__ void depth_kernel(const uint32_t* __restrict__ albedo, const float* __restrict__ hit_t,
-                             View v, float* __restrict__ z) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= v.width || y >= v.height) return;
-  const size_t off = (size_t)y * (size_t)v.width + (size_t)x;
-  float out = kFar;
-  if (albedo[off] >> 24) {
-    float u[3];
-    ray_u(v, x, y, u);
-    out = __fdiv_rn(hit_t[off], __fsqrt_rn(dot3(u, u)));
+__global__ void __launch_bounds__(kTX* kTY)
+    depth_kernel(const uint32_t* __restrict__ albedo, const float* __restrict__ hit_t, View v,
+                 float* __restrict__ z) {
+  const int x = blockIdx.x * kTile + threadIdx.x;
+  const int y0 = blockIdx.y * kTile + threadIdx.y;
+  if (x >= v.width) return;
+  uint32_t a[kRowsPer];
+  float t[kRowsPer];
+#pragma unroll
+  for (int r = 0; r < kRowsPer; ++r) {
+    const int y = y0 + r * kTY;
+    const size_t off = (size_t)y * (size_t)v.width + (size_t)x;
+    a[r] = y < v.height ? __ldg(albedo + off) : 0u;
+    t[r] = y < v.height ? __ldg(hit_t + off) : 0.f;
   }
-  z[off] = out;
+#pragma unroll
+  for (int r = 0; r < kRowsPer; ++r) {
+    const int y = y0 + r * kTY;
+    if (y >= v.height) continue;
+    float out = kFar;
+    if (a[r] >> 24) {
+      float u[3];
+      ray_u(v, x, y, u);
+      out = __fdiv_rn(t[r], __fsqrt_rn(dot3(u, u)));
+    }
+    z[(size_t)y * (size_t)v.width + (size_t)x] = out;
+  }
 }
 
-__global__ void __launch_bounds__(kTileX * kTileY)
+// Blurred depth of pixel (x, y) of a w x h frame; at(dx, dy) is the depth of
+// the pixel at offset (dx, dy), asked only for offsets inside the frame.
+// kEdge = false: the pixel is 2 or more pixels inside the frame, so every
+// tap and mirrored tap is (the bounds tests drop out).
+template <bool kEdge, class At>
+__device__ __forceinline__ float blur_taps(At at, float d, int x, int y, int w, int h,
+                                           float thr, float pad_thr, const BlurWeights& bw) {
+  const float d_far = __fadd_rn(d, thr), d_pad = __fadd_rn(d, pad_thr);
+  float acc = 0.f, c = 0.f;
+#pragma unroll
+  for (int oy = -2; oy <= 2; ++oy) {
+#pragma unroll
+    for (int ox = -2; ox <= 2; ++ox) {
+      const int sx = x + ox, sy = y + oy;
+      if (kEdge && (sx < 0 || sy < 0 || sx >= w || sy >= h)) continue;
+      float s = at(ox, oy);
+      float k = bw.k[(oy + 2) * 5 + ox + 2];
+      if (s > d_far) {
+        s = d_pad;
+      } else if (d > __fadd_rn(s, thr)) {
+        const int mx = x - ox, my = y - oy;
+        if (kEdge && (mx < 0 || my < 0 || mx >= w || my >= h)) {
+          k = 0.f;
+        } else {
+          const float m = at(-ox, -oy);
+          if (d > __fadd_rn(m, thr)) k = 0.f;
+          else s = m > d_far ? d_pad : m;
+        }
+      }
+      acc = __fadd_rn(acc, __fmul_rn(s, k));
+      c = __fadd_rn(c, k);
+    }
+  }
+  return __fdiv_rn(acc, c);
+}
+
+template <class At>
+__device__ __forceinline__ float blur_pixel(At at, int x, int y, int w, int h, float zlimit,
+                                            float thr, float pad_thr, const BlurWeights& bw) {
+  const float d = at(0, 0);
+  if (!(d > 0.f && d <= zlimit)) return d;
+  if (x >= 2 && y >= 2 && x + 2 < w && y + 2 < h)
+    return blur_taps<false>(at, d, x, y, w, h, thr, pad_thr, bw);
+  return blur_taps<true>(at, d, x, y, w, h, thr, pad_thr, bw);
+}
+
+__global__ void __launch_bounds__(kTX* kTY)
     blur_kernel(const float* __restrict__ zin, float* __restrict__ zout, int w, int h,
                 float zlimit, float thr, float pad_thr, BlurWeights bw) {
-  __shared__ float tile[kSmemY][kSmemX];
-  const int x0 = blockIdx.x * kTileX - kHalo, y0 = blockIdx.y * kTileY - kHalo;
-  const int tid = threadIdx.y * kTileX + threadIdx.x;
-  for (int i = tid; i < kSmemX * kSmemY; i += kTileX * kTileY) {
-    const int gx = x0 + i % kSmemX, gy = y0 + i / kSmemX;
-    tile[i / kSmemX][i % kSmemX] =
-        (gx >= 0 && gy >= 0 && gx < w && gy < h) ? zin[(size_t)gy * w + gx] : kFar;
+  __shared__ float tile[kSm][kSm];
+  constexpr int kLoads = (kSm * kSm + kTX * kTY - 1) / (kTX * kTY);
+  const int x0 = blockIdx.x * kTile - kHalo, y0 = blockIdx.y * kTile - kHalo;
+  const int tid = threadIdx.y * kTX + threadIdx.x;
+  float ld[kLoads];
+#pragma unroll
+  for (int j = 0; j < kLoads; ++j) {
+    const int i = tid + j * kTX * kTY;
+    const int gx = x0 + i % kSm, gy = y0 + i / kSm;
+    ld[j] = (i < kSm * kSm && gx >= 0 && gy >= 0 && gx < w && gy < h)
+                ? __ldg(zin + (size_t)gy * w + gx)
+                : kFar;
+  }
+#pragma unroll
+  for (int j = 0; j < kLoads; ++j) {
+    const int i = tid + j * kTX * kTY;
+    if (i < kSm * kSm) tile[i / kSm][i % kSm] = ld[j];
   }
   __syncthreads();
-  const int x = blockIdx.x * kTileX + threadIdx.x, y = blockIdx.y * kTileY + threadIdx.y;
-  if (x >= w || y >= h) return;
-  const int tx = threadIdx.x + kHalo, ty = threadIdx.y + kHalo;
-  const float d = tile[ty][tx];
-  float res = d;
-  if (d > 0.f && d <= zlimit) {
-    const float d_far = __fadd_rn(d, thr), d_pad = __fadd_rn(d, pad_thr);
-    float acc = 0.f, c = 0.f;
+  const int x = blockIdx.x * kTile + threadIdx.x;
+  if (x >= w) return;
+  const int tx = threadIdx.x + kHalo;
 #pragma unroll
-    for (int oy = -2; oy <= 2; ++oy) {
-#pragma unroll
-      for (int ox = -2; ox <= 2; ++ox) {
-        const int sx = x + ox, sy = y + oy;
-        if (sx < 0 || sy < 0 || sx >= w || sy >= h) continue;
-        float s = tile[ty + oy][tx + ox];
-        float k = bw.k[(oy + 2) * 5 + ox + 2];
-        if (s > d_far) {
-          s = d_pad;
-        } else if (d > __fadd_rn(s, thr)) {
-          const int mx = x - ox, my = y - oy;
-          if (mx < 0 || my < 0 || mx >= w || my >= h) {
-            k = 0.f;
-          } else {
-            const float m = tile[ty - oy][tx - ox];
-            if (d > __fadd_rn(m, thr)) k = 0.f;
-            else s = m > d_far ? d_pad : m;
-          }
-        }
-        acc = __fadd_rn(acc, __fmul_rn(s, k));
-        c = __fadd_rn(c, k);
-      }
-    }
-    res = __fdiv_rn(acc, c);
+  for (int r = 0; r < kRowsPer; ++r) {
+    const int y = blockIdx.y * kTile + threadIdx.y + r * kTY;
+    if (y >= h) break;
+    const int ty = threadIdx.y + r * kTY + kHalo;
+    zout[(size_t)y * w + x] =
+        blur_pixel([&](int dx, int dy) { return tile[ty + dy][tx + dx]; }, x, y, w, h, zlimit,
+                   thr, pad_thr, bw);
   }
-  zout[(size_t)y * w + x] = res;
 }
 
-// Tangent along one axis from the depth of the pixel and its two neighbours
-// (`lo` = index - step, `hi` = index + step); false when neither neighbour
-// holds a hit.
-__device__ __forceinline__ bool tangent(const View& v, const float* __restrict__ z, int x, int y,
-                                        int sx, int sy, float zc, const float pc[3],
-                                        float t[3]) {
-  const int xl = x - sx, yl = y - sy, xh = x + sx, yh = y + sy;
-  const bool has_lo = xl >= 0 && yl >= 0 && z[(size_t)yl * v.width + xl] < kFar;
-  const bool has_hi = xh < v.width && yh < v.height && z[(size_t)yh * v.width + xh] < kFar;
+// Tangent along one axis from the pixel's depth zc (position pc) and its
+// neighbours' depths zl at -step and zh at +step (kFar: no hit or outside
+// the frame); false when neither neighbour holds a hit.
+__device__ __forceinline__ bool tangent(const View& v, int x, int y, int sx, int sy, float zc,
+                                        const float pc[3], float zl, float zh, float t[3]) {
+  const bool has_lo = zl < kFar, has_hi = zh < kFar;
   if (!has_lo && !has_hi) return false;
-  const float zl = has_lo ? z[(size_t)yl * v.width + xl] : 0.f;
-  const float zh = has_hi ? z[(size_t)yh * v.width + xh] : 0.f;
   const bool use_hi =
       has_hi && (!has_lo || fabsf(__fsub_rn(zh, zc)) < fabsf(__fsub_rn(zc, zl)));
   float u[3];
   if (use_hi) {
-    ray_u(v, xh, yh, u);
+    ray_u(v, x + sx, y + sy, u);
 #pragma unroll
     for (int i = 0; i < 3; ++i) t[i] = __fsub_rn(__fmul_rn(zh, u[i]), pc[i]);
   } else {
-    ray_u(v, xl, yl, u);
+    ray_u(v, x - sx, y - sy, u);
 #pragma unroll
     for (int i = 0; i < 3; ++i) t[i] = __fsub_rn(pc[i], __fmul_rn(zl, u[i]));
   }
@@ -181,34 +229,22 @@ __device__ __forceinline__ uint32_t to_u8(float c) {
   return __float2uint_rz(__fadd_rn(__fmul_rn(c, 255.f), 0.5f));
 }
 
-__global__ void shade_kernel(const uint32_t* __restrict__ albedo, const float* __restrict__ z,
-                             const float* __restrict__ stored_n, View v, Shading sh,
-                             uint32_t* __restrict__ rgba, float* __restrict__ depth_out,
-                             float* __restrict__ normal_out) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= v.width || y >= v.height) return;
-  const size_t off = (size_t)y * (size_t)v.width + (size_t)x;
-  const uint32_t alb = albedo[off];
-  if (!(alb >> 24)) {
-    rgba[off] = 0u;
-    if (depth_out) depth_out[off] = 0.f;
-    if (normal_out) {
-      normal_out[3 * off] = 0.f;
-      normal_out[3 * off + 1] = 0.f;
-      normal_out[3 * off + 2] = 0.f;
-    }
-    return;
-  }
-  const float zc = z[off];
+// Colour of a hit pixel; n holds the stored normal on entry and the normal
+// used on return.  zn = depths of the (x-1, x+1, y-1, y+1) neighbours.
+// Per light, with lv = light - P, d = |lv| and u the pixel's ray:
+//   n.L = (n.lv) / d,  R.V = (lv.u - 2 (n.L) (n.u) d) / (d |u|)
+// (R = 2 (n.L) n - L, V = -u / |u|), one division each.
+__device__ __forceinline__ uint32_t shade_pixel(uint32_t alb, float zc, const float zn[4],
+                                                float n[3], const View& v, const Shading& sh,
+                                                int x, int y) {
   float u[3], p[3];
   ray_u(v, x, y, u);
 #pragma unroll
   for (int i = 0; i < 3; ++i) p[i] = __fmul_rn(zc, u[i]);
-  float n[3] = {stored_n[3 * off], stored_n[3 * off + 1], stored_n[3 * off + 2]};
   if (sh.ssna) {
     float tx[3], ty[3];
-    if (tangent(v, z, x, y, 1, 0, zc, p, tx) && tangent(v, z, x, y, 0, 1, zc, p, ty)) {
+    if (tangent(v, x, y, 1, 0, zc, p, zn[0], zn[1], tx) &&
+        tangent(v, x, y, 0, 1, zc, p, zn[2], zn[3], ty)) {
       float c[3] = {__fsub_rn(__fmul_rn(tx[1], ty[2]), __fmul_rn(tx[2], ty[1])),
                     __fsub_rn(__fmul_rn(tx[2], ty[0]), __fmul_rn(tx[0], ty[2])),
                     __fsub_rn(__fmul_rn(tx[0], ty[1]), __fmul_rn(tx[1], ty[0]))};
@@ -219,9 +255,9 @@ __global__ void shade_kernel(const uint32_t* __restrict__ albedo, const float* _
       }
       const float len2 = dot3(c, c);
       if (len2 > 0.f && len2 <= 3.402823466e38f) {
-        const float len = __fsqrt_rn(len2);
+        const float inv = __fdiv_rn(1.f, __fsqrt_rn(len2));
 #pragma unroll
-        for (int i = 0; i < 3; ++i) n[i] = __fdiv_rn(c[i], len);
+        for (int i = 0; i < 3; ++i) n[i] = __fmul_rn(c[i], inv);
       }
     }
   }
@@ -229,51 +265,90 @@ __global__ void shade_kernel(const uint32_t* __restrict__ albedo, const float* _
   if (sh.show_normals) {
 #pragma unroll
     for (int i = 0; i < 3; ++i) out |= to_u8(__fadd_rn(__fmul_rn(n[i], 0.5f), 0.5f)) << (8 * i);
-  } else {
-    float a[3], col[3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      a[i] = __fdiv_rn((float)((alb >> (8 * i)) & 0xFFu), 255.f);
-      col[i] = __fmul_rn(a[i], sh.ambient[i]);
-    }
-    const float ulen = __fsqrt_rn(dot3(u, u));
-    const float vv[3] = {__fdiv_rn(-u[0], ulen), __fdiv_rn(-u[1], ulen), __fdiv_rn(-u[2], ulen)};
-    for (int l = 0; l < sh.nlights; ++l) {
-      float lv[3];
-#pragma unroll
-      for (int i = 0; i < 3; ++i) lv[i] = __fsub_rn(sh.lpos[l][i], __fadd_rn(v.pos[i], p[i]));
-      const float d2 = dot3(lv, lv);
-      const float d = __fsqrt_rn(d2);
-      if (!(d > 0.f)) continue;
-      const float L[3] = {__fdiv_rn(lv[0], d), __fdiv_rn(lv[1], d), __fdiv_rn(lv[2], d)};
-      const float den = __fadd_rn(__fadd_rn(sh.latt[l][0], __fmul_rn(sh.latt[l][1], d)),
-                                  __fmul_rn(sh.latt[l][2], d2));
-      const float att = den > 0.f ? __fdiv_rn(1.f, den) : 0.f;
-      const float ndl = dot3(n, L);
-      if (!(ndl > 0.f)) continue;
-      const float na = __fmul_rn(ndl, att);
-#pragma unroll
-      for (int i = 0; i < 3; ++i)
-        col[i] = __fadd_rn(col[i], __fmul_rn(a[i], __fmul_rn(na, sh.ldif[l][i])));
-      const float two_ndl = __fmul_rn(2.f, ndl);
-      const float R[3] = {__fsub_rn(__fmul_rn(two_ndl, n[0]), L[0]),
-                          __fsub_rn(__fmul_rn(two_ndl, n[1]), L[1]),
-                          __fsub_rn(__fmul_rn(two_ndl, n[2]), L[2])};
-      const float rv = dot3(R, vv);
-      if (!(rv > 0.f)) continue;
-      const float sp = __fmul_rn(powf(rv, sh.spec_exp), att);
-#pragma unroll
-      for (int i = 0; i < 3; ++i) col[i] = __fadd_rn(col[i], __fmul_rn(sh.lspec[l][i], sp));
-    }
-#pragma unroll
-    for (int i = 0; i < 3; ++i) out |= to_u8(col[i]) << (8 * i);
+    return out;
   }
-  rgba[off] = out;
-  if (depth_out) depth_out[off] = zc;
-  if (normal_out) {
-    normal_out[3 * off] = n[0];
-    normal_out[3 * off + 1] = n[1];
-    normal_out[3 * off + 2] = n[2];
+  float a[3], col[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    a[i] = __fmul_rn((float)((alb >> (8 * i)) & 0xFFu), 1.0f / 255.0f);
+    col[i] = __fmul_rn(a[i], sh.ambient[i]);
+  }
+  const float ulen = __fsqrt_rn(dot3(u, u));
+  const float nu = dot3(n, u);
+  for (int l = 0; l < sh.nlights; ++l) {
+    float lv[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) lv[i] = __fsub_rn(sh.lpos[l][i], __fadd_rn(v.pos[i], p[i]));
+    const float d2 = dot3(lv, lv);
+    const float d = __fsqrt_rn(d2);
+    if (!(d > 0.f)) continue;
+    const float ndl = __fdiv_rn(dot3(n, lv), d);
+    if (!(ndl > 0.f)) continue;
+    const float den = __fadd_rn(__fadd_rn(sh.latt[l][0], __fmul_rn(sh.latt[l][1], d)),
+                                __fmul_rn(sh.latt[l][2], d2));
+    const float att = den > 0.f ? __fdiv_rn(1.f, den) : 0.f;
+    const float na = __fmul_rn(ndl, att);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+      col[i] = __fadd_rn(col[i], __fmul_rn(a[i], __fmul_rn(na, sh.ldif[l][i])));
+    const float num = __fsub_rn(dot3(lv, u), __fmul_rn(__fmul_rn(__fmul_rn(2.f, ndl), nu), d));
+    const float rv = __fdiv_rn(num, __fmul_rn(d, ulen));
+    if (!(rv > 0.f)) continue;
+    const float sp = __fmul_rn(powf(rv, sh.spec_exp), att);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) col[i] = __fadd_rn(col[i], __fmul_rn(sh.lspec[l][i], sp));
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) out |= to_u8(col[i]) << (8 * i);
+  return out;
+}
+
+__global__ void __launch_bounds__(kTX* kTY)
+    shade_kernel(const uint32_t* __restrict__ albedo, const float* __restrict__ z,
+                 const float* __restrict__ stored_n, View v, Shading sh,
+                 uint32_t* __restrict__ rgba, float* __restrict__ depth_out,
+                 float* __restrict__ normal_out) {
+  const int x = blockIdx.x * kTile + threadIdx.x;
+  const int y0 = blockIdx.y * kTile + threadIdx.y;
+  const int w = v.width, h = v.height;
+  if (x >= w) return;
+  // loads first: albedo, the depth cross, then the stored normals of the hits
+  uint32_t a[kRowsPer];
+  float zc[kRowsPer], zn[kRowsPer][4], sn[kRowsPer][3];
+#pragma unroll
+  for (int r = 0; r < kRowsPer; ++r) {
+    const int y = y0 + r * kTY;
+    const size_t off = (size_t)y * (size_t)w + (size_t)x;
+    const bool in = y < h;
+    a[r] = in ? __ldg(albedo + off) : 0u;
+    zc[r] = in ? __ldg(z + off) : kFar;
+    zn[r][0] = in && x > 0 ? __ldg(z + off - 1) : kFar;
+    zn[r][1] = in && x + 1 < w ? __ldg(z + off + 1) : kFar;
+    zn[r][2] = in && y > 0 ? __ldg(z + off - w) : kFar;
+    zn[r][3] = in && y + 1 < h ? __ldg(z + off + w) : kFar;
+  }
+#pragma unroll
+  for (int r = 0; r < kRowsPer; ++r) {
+    const size_t off = (size_t)(y0 + r * kTY) * (size_t)w + (size_t)x;
+    const bool hit = (a[r] >> 24) != 0u;
+    sn[r][0] = hit ? __ldg(stored_n + 3 * off) : 0.f;
+    sn[r][1] = hit ? __ldg(stored_n + 3 * off + 1) : 0.f;
+    sn[r][2] = hit ? __ldg(stored_n + 3 * off + 2) : 0.f;
+  }
+#pragma unroll
+  for (int r = 0; r < kRowsPer; ++r) {
+    const int y = y0 + r * kTY;
+    if (y >= h) break;
+    const size_t off = (size_t)y * (size_t)w + (size_t)x;
+    const bool hit = (a[r] >> 24) != 0u;
+    float n[3] = {sn[r][0], sn[r][1], sn[r][2]};
+    rgba[off] = hit ? shade_pixel(a[r], zc[r], zn[r], n, v, sh, x, y) : 0u;
+    if (depth_out) depth_out[off] = hit ? zc[r] : 0.f;
+    if (normal_out) {
+      normal_out[3 * off] = n[0];
+      normal_out[3 * off + 1] = n[1];
+      normal_out[3 * off + 2] = n[2];
+    }
   }
 }
 
@@ -360,11 +435,12 @@ yv_status yv_render_ssna(yv_renderer* r, const yv_ssna_params* p, void* device_r
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const View v = make_view(rv);
   const size_t px = (size_t)v.width * (size_t)v.height;
+  const int passes = p->ssna ? p->blur_passes : 0;
   DevBuf alb, ht, nrm, za, zb;
   cudaError_t e;
   if ((e = alb.alloc(px * 4, s)) != cudaSuccess || (e = ht.alloc(px * 4, s)) != cudaSuccess ||
       (e = nrm.alloc(px * 12, s)) != cudaSuccess || (e = za.alloc(px * 4, s)) != cudaSuccess ||
-      (e = zb.alloc(px * 4, s)) != cudaSuccess)
+      (passes > 0 && (e = zb.alloc(px * 4, s)) != cudaSuccess))
     return ssna_fail(e, "scratch");
   yv_frame_outputs fo;
   std::memset(&fo, 0, sizeof(fo));
@@ -374,28 +450,6 @@ yv_status yv_render_ssna(yv_renderer* r, const yv_ssna_params* p, void* device_r
   yv_status st = renderer_enqueue_unlit(r, &fo, s);
   if (st != YV_OK) return st;
 
-  const dim3 blk(kTileX, kTileY);
-  const dim3 grd((unsigned)((v.width + kTileX - 1) / kTileX),
-                 (unsigned)((v.height + kTileY - 1) / kTileY));
-  depth_kernel<<<grd, blk, 0, s>>>(alb.as<uint32_t>(), ht.as<float>(), v, za.as<float>());
-  if ((e = cudaGetLastError()) != cudaSuccess) return ssna_fail(e, "depth launch");
-  float* src = za.as<float>();
-  float* dst = zb.as<float>();
-  if (p->ssna) {
-    const BlurWeights bw = blur_weights();
-    // pixel angle = fov / width in radians (RenderParams::pixelAng)
-    const double pix = (double)rv.fov_deg * (3.14159265358979323846 / 180.0) / v.width;
-    const float thr = p->edge_threshold;
-    const float pad_thr = p->edge_pad * thr;
-    for (int i = 0; i < p->blur_passes; ++i) {
-      const float zlimit = (float)(5.0 * p->voxel_size / (pix * 3.0 * (i + 1)));
-      blur_kernel<<<grd, blk, 0, s>>>(src, dst, v.width, v.height, zlimit, thr, pad_thr, bw);
-      if ((e = cudaGetLastError()) != cudaSuccess) return ssna_fail(e, "blur launch");
-      float* t = src;
-      src = dst;
-      dst = t;
-    }
-  }
   Shading sh;
   std::memset(&sh, 0, sizeof(sh));
   std::memcpy(sh.ambient, p->ambient, sizeof(sh.ambient));
@@ -410,6 +464,28 @@ yv_status yv_render_ssna(yv_renderer* r, const yv_ssna_params* p, void* device_r
     std::memcpy(sh.ldif[k], L.diffuse, 12);
     std::memcpy(sh.lspec[k], L.specular, 12);
     std::memcpy(sh.latt[k], L.attenuation, 12);
+  }
+  const BlurWeights bw = blur_weights();
+  // pixel angle = fov / width in radians (RenderParams::pixelAng); pass i
+  // blurs z <= 5 voxSize / (pixelAng * blurSize), blurSize = 3 (i + 1)
+  const double pix = (double)rv.fov_deg * (3.14159265358979323846 / 180.0) / v.width;
+  const float thr = p->edge_threshold;
+  const float pad_thr = p->edge_pad * thr;
+
+  const dim3 blk(kTX, kTY);
+  const dim3 grd((unsigned)((v.width + kTile - 1) / kTile),
+                 (unsigned)((v.height + kTile - 1) / kTile));
+  depth_kernel<<<grd, blk, 0, s>>>(alb.as<uint32_t>(), ht.as<float>(), v, za.as<float>());
+  if ((e = cudaGetLastError()) != cudaSuccess) return ssna_fail(e, "depth launch");
+  float* src = za.as<float>();
+  float* dst = zb.as<float>();
+  for (int i = 0; i < passes; ++i) {
+    const float zlimit = (float)(5.0 * p->voxel_size / (pix * 3.0 * (i + 1)));
+    blur_kernel<<<grd, blk, 0, s>>>(src, dst, v.width, v.height, zlimit, thr, pad_thr, bw);
+    if ((e = cudaGetLastError()) != cudaSuccess) return ssna_fail(e, "blur launch");
+    float* t = src;
+    src = dst;
+    dst = t;
   }
   shade_kernel<<<grd, blk, 0, s>>>(alb.as<uint32_t>(), src, nrm.as<float>(), v, sh,
                                    static_cast<uint32_t*>(device_rgba),
@@ -439,8 +515,8 @@ yv_status yv_renderer_trace_dump(yv_renderer* r, float* host_dist, uint32_t* hos
   fo.normal = nrm.p;
   yv_status st = renderer_enqueue_unlit(r, &fo, s);
   if (st != YV_OK) return st;
-  const dim3 blk(kTileX, kTileY);
-  const dim3 grd((unsigned)((w + kTileX - 1) / kTileX), (unsigned)((h + kTileY - 1) / kTileY));
+  const dim3 blk(32, 8);
+  const dim3 grd((unsigned)((w + 31) / 32), (unsigned)((h + 7) / 8));
   dump_kernel<<<grd, blk, 0, s>>>(alb.as<uint32_t>(), ht.as<float>(), w, h, dist.as<float>());
   if ((e = cudaGetLastError()) != cudaSuccess) return ssna_fail(e, "dump launch");
   yv_frame_stats fs;
