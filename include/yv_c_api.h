@@ -58,7 +58,8 @@ const char* yv_last_error(void);
  *   flags bits 0..7  : child i is a leaf (child[i] holds VoxData)
  *   flags bits 8..15 : child i is null (EmptyNode / FullNode)
  *   flags bit  19    : empty flag
- *   data             : coarse-LOD VoxData of the subtree (not used by tracing)
+ *   data             : coarse-LOD VoxData of the subtree (the level-of-detail
+ *                      attribute index, see yv_svo_build_lod)
  *   child[i]         : node index, VoxData (leaf) or a null id (bit 31 set).
  * Child order: bit 0 of i = +x half, bit 1 = +y half, bit 2 = +z half.
  * VoxData of a leaf is an index into the leaf attribute array. */
@@ -104,9 +105,24 @@ yv_status yv_svo_from_arrays(yv_svo_host** out, const yv_vox_node* nodes,
 
 /* .vox file (SVOData::Load, cell/svodata.h:31-50): little-endian
  * uint32 root, uint32, uint32, uint32 size, VoxNode[size]; followed by an
- * optional attribute section "YVAT" uint32 count, yv_leaf_attr[count]. */
+ * optional attribute section "YVAT" uint32 count, yv_leaf_attr[count], and
+ * an optional marker "YVLD" saying that every node's `data` indexes its
+ * level-of-detail attribute.  A file without the attribute section holds
+ * the reference's packed VoxData (16-bit colour, 16-bit normal) in leaves
+ * and in node `data`; both are decoded into attributes (the scene then has
+ * level-of-detail data). */
 yv_status yv_svo_load_vox(yv_svo_host** out, const char* path);
 yv_status yv_svo_save_vox(const yv_svo_host* svo, const char* path);
+
+/* Level-of-detail data (the node `data` field of
+ * reaction/report/main.tex:61: the subtree shown at a coarser level): for
+ * every node, the mean colour and mean normal of all leaves of its subtree
+ * (each component the integer mean rounded half away from zero, alpha 255)
+ * become a new attribute, appended after the existing ones in node order,
+ * and the node's `data` indexes it. */
+yv_status yv_svo_build_lod(yv_svo_host* svo);
+/* 1 if every node's `data` is a level-of-detail attribute index. */
+int       yv_svo_has_lod(const yv_svo_host* svo);
 
 void               yv_svo_free(yv_svo_host* svo);
 uint32_t           yv_svo_node_count(const yv_svo_host* svo);
@@ -217,6 +233,15 @@ yv_status yv_set_resolution(yv_renderer* r, int width, int height);
 yv_status yv_get_resolution(const yv_renderer* r, int* width, int* height);
 yv_status yv_set_fov(yv_renderer* r, float fov_deg);
 yv_status yv_set_light(yv_renderer* r, const yv_light* light);
+/* SVORenderer::SetDetailCoef / GetDetailCoef (demo/SVORenderer.h:25-26):
+ * level-of-detail cut-off.  With coef > 0 and a scene set from a host
+ * container with level-of-detail data, a ray stops at a subtree whose cube
+ * side is smaller than t * coef * radians(fov / 2) / width (t the distance
+ * to the subtree's entry face; SVORenderer.cpp:104) and shades it with the
+ * subtree's attribute; the hit word is then (parent << 3) | child slot, as
+ * for a leaf in that slot.  0 (the default): exact leaves. */
+yv_status yv_set_detail_coef(yv_renderer* r, float coef);
+yv_status yv_get_detail_coef(const yv_renderer* r, float* coef);
 yv_status yv_set_launch_config(yv_renderer* r, const yv_launch_config* cfg);
 yv_status yv_get_launch_config(const yv_renderer* r, yv_launch_config* cfg);
 

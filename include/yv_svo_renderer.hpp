@@ -89,6 +89,9 @@ class SVOData {
   yv_status Save(const char* fn) const {
     return h_ ? yv_svo_save_vox(h_, fn) : YV_ERR_INVALID_ARG;
   }
+  /* The node `data` of reaction/report/main.tex:61: mean colour and normal
+   * of every subtree, for the renderer's level-of-detail cut-off. */
+  yv_status BuildLOD() { return h_ ? yv_svo_build_lod(h_) : YV_ERR_INVALID_ARG; }
 
   uint32_t GetRoot() const { return h_ ? yv_svo_root(h_) : kEmptyNode; }
   uint32_t Size() const { return h_ ? yv_svo_node_count(h_) : 0u; }
@@ -187,6 +190,15 @@ class GPURenderer : public ISVORenderer {
   /* demo/SVORenderer.h:28-36: screen-space normals, normal display, the
    * point lights and a frame into a device RGBA8 buffer (async on the
    * default stream). */
+  /* demo/SVORenderer.h:25-26 (0 = exact leaves, the default here). */
+  void SetDetailCoef(float coef) {
+    if (r_) status_ = yv_set_detail_coef(r_, coef);
+  }
+  float GetDetailCoef() const {
+    float c = 0.f;
+    if (r_) yv_get_detail_coef(r_, &c);
+    return c;
+  }
   void SetSSNA(bool enable) { Ssna().ssna = enable ? 1 : 0; }
   bool GetSSNA() { return Ssna().ssna != 0; }
   void SetShowNormals(bool enable) { Ssna().show_normals = enable ? 1 : 0; }

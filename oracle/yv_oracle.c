@@ -20,6 +20,7 @@
 #define FLOOR floorf
 #define CEIL ceilf
 #define COPYSIGN copysignf
+#define LDEXP ldexpf
 #include "yv_oracle_impl.h"
 #undef REAL
 #undef SFX
@@ -28,6 +29,7 @@
 #undef FLOOR
 #undef CEIL
 #undef COPYSIGN
+#undef LDEXP
 #undef V3
 
 /* ---- double instantiation ---- */
@@ -38,6 +40,7 @@
 #define FLOOR floor
 #define CEIL ceil
 #define COPYSIGN copysign
+#define LDEXP ldexp
 #include "yv_oracle_impl.h"
 
 /* ------------------------------------------------------------------------ */
@@ -94,6 +97,20 @@ int orc_svo_render_f32(const uint32_t* nodes, uint32_t count, uint32_t root,
                        uint32_t* rgba, uint32_t* hit, float* hit_t,
                        uint32_t* fetches, uint32_t* shadow_fetches,
                        uint8_t* shadowed) {
+  return orc_svo_render_lod_f32(nodes, count, root, attrs, nattrs, pos, dir0, du, dv, width,
+                                height, light, ambient, diffuse, shadows, 0.0f, y0, y1, rgba,
+                                hit, hit_t, fetches, shadow_fetches, shadowed);
+}
+
+int orc_svo_render_lod_f32(const uint32_t* nodes, uint32_t count, uint32_t root,
+                           const uint8_t* attrs, uint32_t nattrs,
+                           const float pos[3], const float dir0[3],
+                           const float du[3], const float dv[3], int width,
+                           int height, const float light[3], float ambient,
+                           float diffuse, int shadows, float lod_coef, int y0,
+                           int y1, uint32_t* rgba, uint32_t* hit, float* hit_t,
+                           uint32_t* fetches, uint32_t* shadow_fetches,
+                           uint8_t* shadowed) {
   if (y0 < 0) y0 = 0;
   if (y1 > height) y1 = height;
   float ldir[3] = {light[0], light[1], light[2]};
@@ -109,7 +126,7 @@ int orc_svo_render_f32(const uint32_t* nodes, uint32_t count, uint32_t root,
       float d[3];
       pixel_dir_f32(dir0, du, dv, x, y, d);
       adjust_dir_f32(d);
-      trace_ctx_f32 c = {nodes, count, 0, 0, 0};
+      trace_ctx_f32 c = {nodes, count, 0, 0, 0, lod_coef};
       hit_rec_f32 h;
       uint32_t dir_flags = 0;
       int ok = trace_one_f32(&c, root, pos, d, &h, &dir_flags);
@@ -117,6 +134,8 @@ int orc_svo_render_f32(const uint32_t* nodes, uint32_t count, uint32_t root,
       if (fetches) fetches[off] = c.fetches;
       if (!ok) continue;
       uint32_t vd = nodes[(size_t)h.node * 10u + 2u + (uint32_t)h.child];
+      /* a level-of-detail hit shades with the subtree's data attribute */
+      if (h.lod) vd = nodes[(size_t)vd * 10u + 1u];
       if (vd >= nattrs) return 3;
       if (hit) hit[off] = (h.node << 3) | (uint32_t)h.child;
       if (hit_t) hit_t[off] = h.t;
@@ -124,7 +143,7 @@ int orc_svo_render_f32(const uint32_t* nodes, uint32_t count, uint32_t root,
       if (shadows) {
         float so[3];
         shadow_origin_f32(pos, d, &h, dir_flags, so);
-        trace_ctx_f32 cs = {nodes, count, 1, 0, 0};
+        trace_ctx_f32 cs = {nodes, count, 1, 0, 0, lod_coef};
         hit_rec_f32 hs;
         sh = trace_one_f32(&cs, root, so, ldir, &hs, 0);
         if (cs.err) return cs.err;

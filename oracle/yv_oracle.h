@@ -51,6 +51,21 @@ int orc_svo_render_f32(const uint32_t* nodes, uint32_t count, uint32_t root,
                        uint32_t* fetches, uint32_t* shadow_fetches,
                        uint8_t* shadowed);
 
+/* The same with the level-of-detail cut-off of SVORenderer (detailCoef):
+ * a subtree ahead of the ray whose cube side 2^-(level+1) is below
+ * max(t_enter, 0) * lod_coef ends the ray there; it is shaded with the
+ * attribute its node's `data` word indexes, and reported as the hit
+ * (parent << 3 | child slot).  lod_coef = 0: orc_svo_render_f32. */
+int orc_svo_render_lod_f32(const uint32_t* nodes, uint32_t count, uint32_t root,
+                           const uint8_t* attrs, uint32_t nattrs,
+                           const float pos[3], const float dir0[3],
+                           const float du[3], const float dv[3], int width,
+                           int height, const float light[3], float ambient,
+                           float diffuse, int shadows, float lod_coef, int y0,
+                           int y1, uint32_t* rgba, uint32_t* hit, float* hit_t,
+                           uint32_t* fetches, uint32_t* shadow_fetches,
+                           uint8_t* shadowed);
+
 /* Same over all rows on nthreads POSIX threads in row bands
  * (TreadedRenderer, cell/ppu_renderer.cpp:121-144). */
 int orc_svo_render_mt(int nthreads, const uint32_t* nodes, uint32_t count,

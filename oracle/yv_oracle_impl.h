@@ -148,6 +148,7 @@ typedef struct {
   REAL t;
   int level;
   REAL t1[3];
+  int lod;         /* 1: stopped at the subtree in (node, child) */
 } FN(hit_rec);
 
 typedef struct {
@@ -156,6 +157,7 @@ typedef struct {
   int cull_behind; /* shadow rays: leaves entirely behind the origin skip */
   int err;
   uint32_t fetches;
+  REAL lod_coef;   /* > 0: level-of-detail cut-off (see rec_trace) */
 } FN(trace_ctx);
 
 /* RecTrace (cell/ppu_renderer.cpp:18-41), recursive as in the reference.  */
@@ -183,11 +185,33 @@ static int FN(rec_trace)(FN(trace_ctx) * c, uint32_t node_id, REAL* pt1,
         res->t1[0] = t1[0];
         res->t1[1] = t1[1];
         res->t1[2] = t1[2];
+        res->lod = 0;
         return 1;
       }
-    } else if (FN(rec_trace)(c, node[2 + cc], t1, t2, dir_flags, level + 1,
-                             res)) {
-      return 1;
+    } else {
+      /* Level-of-detail cut-off (SVORenderer::SetDetailCoef,
+       * demo/SVORenderer.cpp:104; node data = the subtree at a coarser
+       * level, reaction/report/main.tex:61): a subtree ahead of the ray
+       * whose cube side 2^-(level+1) is below max(t_enter, 0) * lod_coef
+       * ends the ray there.  Sides are powers of two (exact). */
+      uint32_t sub = node[2 + cc];
+      if (c->lod_coef > 0 && !(sub & 0x80000000u) && FN(min3)(t2) > 0) {
+        REAL side = LDEXP((REAL)1, -(level + 1));
+        REAL te = FN(max3)(t1);
+        if (te < 0) te = 0;
+        if (side < te * c->lod_coef) {
+          res->node = node_id;
+          res->child = cc;
+          res->t = FN(max3)(t1);
+          res->level = level;
+          res->t1[0] = t1[0];
+          res->t1[1] = t1[1];
+          res->t1[2] = t1[2];
+          res->lod = 1;
+          return 1;
+        }
+      }
+      if (FN(rec_trace)(c, sub, t1, t2, dir_flags, level + 1, res)) return 1;
     }
     if (c->err) return 0;
     if (!FN(go_next)(&ch, t1, t2)) return 0;

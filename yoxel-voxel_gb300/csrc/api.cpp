@@ -31,7 +31,9 @@ struct yv_renderer {
   uint32_t* d_words = nullptr;
   uint32_t* d_orig = nullptr;
   uint4* d_attrs = nullptr;  // shading records, 16 B per leaf
+  uint32_t* d_node_data = nullptr;  // level-of-detail attribute per node, or null
   size_t cap_nodes = 0, cap_attrs = 0;  // allocated records of the three
+  float detail = 0.f;  // SVORenderer::m_detailCoef; 0 = exact leaves
   SvoDeviceScene scene;
   bool has_scene = false;
   uint64_t scene_bytes = 0;
@@ -62,9 +64,11 @@ static void free_scene(yv_renderer* r) {
   cudaFree(r->d_words);
   cudaFree(r->d_orig);
   cudaFree(r->d_attrs);
+  cudaFree(r->d_node_data);
   r->d_words = nullptr;
   r->d_orig = nullptr;
   r->d_attrs = nullptr;
+  r->d_node_data = nullptr;
   r->cap_nodes = r->cap_attrs = 0;
   r->has_scene = false;
   r->scene = SvoDeviceScene();
@@ -83,6 +87,8 @@ yv_status renderer_scene_buffers(yv_renderer* r, uint32_t nn, uint32_t na, uint3
   if (r->frame_pending) cudaStreamSynchronize(r->last_stream);
   r->has_scene = false;
   r->scene = SvoDeviceScene();
+  cudaFree(r->d_node_data);
+  r->d_node_data = nullptr;
   const size_t want_n = nn ? nn : 1, want_a = na ? na : 1;
   if (want_n > r->cap_nodes) {
     cudaFree(r->d_words);
@@ -175,9 +181,13 @@ void yv_renderer_destroy(yv_renderer* r) {
   delete r;
 }
 
-yv_status yv_set_scene_svo(yv_renderer* r, const yv_vox_node* nodes,
-                           uint32_t count, uint32_t root,
-                           const yv_leaf_attr* attrs, uint32_t nattrs) {
+}  // extern "C"
+
+// lod: every node's `data` is a level-of-detail attribute index, uploaded in
+// device order for the level-of-detail cut-off.
+static yv_status set_scene_impl(yv_renderer* r, const yv_vox_node* nodes, uint32_t count,
+                                uint32_t root, const yv_leaf_attr* attrs, uint32_t nattrs,
+                                bool lod) {
   if (!r || (count && !nodes) || (nattrs && !attrs)) return YV_ERR_INVALID_ARG;
   DeviceLayout dl;
   std::string why;
@@ -185,6 +195,18 @@ yv_status yv_set_scene_svo(yv_renderer* r, const yv_vox_node* nodes,
   if (st != YV_OK) {
     set_last_error(why);
     return st;
+  }
+  std::vector<uint32_t> node_data;
+  if (lod) {
+    node_data.resize(dl.orig_id.size());
+    for (size_t i = 0; i < node_data.size(); ++i) {
+      node_data[i] = nodes[dl.orig_id[i]].data;
+      if (node_data[i] >= nattrs) {
+        set_last_error("level-of-detail attribute of node " + std::to_string(dl.orig_id[i]) +
+                       " out of range");
+        return YV_ERR_BAD_POOL;
+      }
+    }
   }
   YV_CUDA(cudaSetDevice(r->device), "cudaSetDevice");
   if (r->frame_pending) cudaStreamSynchronize(r->last_stream);
@@ -231,14 +253,41 @@ yv_status yv_set_scene_svo(yv_renderer* r, const yv_vox_node* nodes,
   r->scene.n_attrs = nattrs;
   r->scene.root_word = dl.root_word;
   r->scene_bytes = (uint64_t)nn * 36u + (uint64_t)nattrs * 16u;
+  if (lod && nn) {
+    YV_CUDA(cudaMalloc(&r->d_node_data, nn * 4u), "cudaMalloc(node data)");
+    YV_CUDA(cudaMemcpy(r->d_node_data, node_data.data(), nn * 4u, cudaMemcpyHostToDevice),
+            "upload node data");
+    r->scene.node_data = r->d_node_data;
+    r->scene_bytes += (uint64_t)nn * 4u;
+  }
   r->has_scene = true;
   return YV_OK;
 }
 
+extern "C" {
+
+yv_status yv_set_scene_svo(yv_renderer* r, const yv_vox_node* nodes,
+                           uint32_t count, uint32_t root,
+                           const yv_leaf_attr* attrs, uint32_t nattrs) {
+  return set_scene_impl(r, nodes, count, root, attrs, nattrs, false);
+}
+
 yv_status yv_set_scene_host(yv_renderer* r, const yv_svo_host* svo) {
   if (!r || !svo) return YV_ERR_INVALID_ARG;
-  return yv_set_scene_svo(r, yv_svo_nodes(svo), yv_svo_node_count(svo), yv_svo_root(svo),
-                          yv_svo_attrs(svo), yv_svo_attr_count(svo));
+  return set_scene_impl(r, yv_svo_nodes(svo), yv_svo_node_count(svo), yv_svo_root(svo),
+                        yv_svo_attrs(svo), yv_svo_attr_count(svo), yv_svo_has_lod(svo) != 0);
+}
+
+yv_status yv_set_detail_coef(yv_renderer* r, float coef) {
+  if (!r || !std::isfinite(coef) || coef < 0.f) return YV_ERR_INVALID_ARG;
+  r->detail = coef;
+  return YV_OK;
+}
+
+yv_status yv_get_detail_coef(const yv_renderer* r, float* coef) {
+  if (!r || !coef) return YV_ERR_INVALID_ARG;
+  *coef = r->detail;
+  return YV_OK;
 }
 
 yv_status yv_load_scene_vox(yv_renderer* r, const char* path) {
@@ -340,6 +389,12 @@ static void fill_frame_args(const yv_renderer* r, SvoFrameArgs& a) {
   a.shadows = r->light.shadows ? 1 : 0;
   a.width = r->width;
   a.height = r->height;
+  // SVORenderer::Render: rp.detailCoef = m_detailCoef * (fov / 2 in
+  // radians) / width (demo/SVORenderer.cpp:104), in double, rounded once
+  a.lod_coef = (r->detail > 0.f && r->scene.node_data)
+                   ? (float)((double)r->detail * (double)r->fov *
+                             (3.14159265358979323846 / 360.0) / (double)r->width)
+                   : 0.f;
 }
 
 }  // extern "C"

@@ -738,22 +738,25 @@ yv_status yv_svo_load_vox(yv_svo_host** out, const char* path) {
         std::fclose(f);
         return YV_ERR_IO;
       }
+      char lod_magic[4];
+      h->lod = std::fread(lod_magic, 1, 4, f) == 4 && std::memcmp(lod_magic, "YVLD", 4) == 0;
     } else {
+      // the reference's packed VoxData, in leaves and in every node's data
+      // (the subtree at a coarser level, reaction/report/main.tex:61)
       std::unordered_map<uint32_t, uint32_t> remap;
+      auto attr_of = [&](uint32_t v) {
+        auto it = remap.find(v);
+        if (it != remap.end()) return it->second;
+        const uint32_t idx = (uint32_t)h->attrs.size();
+        remap.emplace(v, idx);
+        h->attrs.push_back(decode_packed_voxdata(v));
+        return idx;
+      };
       for (auto& n : h->nodes)
         for (int ch = 0; ch < 8; ++ch)
-          if ((n.flags >> ch) & 1u) {
-            auto it = remap.find(n.child[ch]);
-            uint32_t idx;
-            if (it == remap.end()) {
-              idx = (uint32_t)h->attrs.size();
-              remap.emplace(n.child[ch], idx);
-              h->attrs.push_back(decode_packed_voxdata(n.child[ch]));
-            } else {
-              idx = it->second;
-            }
-            n.child[ch] = idx;
-          }
+          if ((n.flags >> ch) & 1u) n.child[ch] = attr_of(n.child[ch]);
+      for (auto& n : h->nodes) n.data = attr_of(n.data);
+      h->lod = !h->nodes.empty();
     }
     std::fclose(f);
     DeviceLayout dl;
@@ -781,6 +784,7 @@ yv_status yv_svo_save_vox(const yv_svo_host* svo, const char* path) {
                 svo->nodes.size() &&
             std::fwrite("YVAT", 1, 4, f) == 4 && std::fwrite(&na, 4, 1, f) == 1 &&
             std::fwrite(svo->attrs.data(), sizeof(yv_leaf_attr), na, f) == na;
+  if (ok && svo->lod) ok = std::fwrite("YVLD", 1, 4, f) == 4;
   ok = (std::fclose(f) == 0) && ok;
   return ok ? YV_OK : YV_ERR_IO;
 }
@@ -793,6 +797,98 @@ const yv_vox_node* yv_svo_nodes(const yv_svo_host* s) { return s ? s->nodes.data
 uint32_t yv_svo_attr_count(const yv_svo_host* s) { return s ? (uint32_t)s->attrs.size() : 0; }
 const yv_leaf_attr* yv_svo_attrs(const yv_svo_host* s) { return s ? s->attrs.data() : nullptr; }
 int yv_svo_depth(const yv_svo_host* s) { return s ? s->depth : 0; }
+int yv_svo_has_lod(const yv_svo_host* s) { return s && s->lod ? 1 : 0; }
+
+// Integer mean rounded half away from zero.
+static int64_t mean_round(int64_t sum, int64_t n) {
+  return sum >= 0 ? (2 * sum + n) / (2 * n) : -((-2 * sum + n) / (2 * n));
+}
+
+yv_status yv_svo_build_lod(yv_svo_host* s) {
+  if (!s) return YV_ERR_INVALID_ARG;
+  const size_t nn = s->nodes.size(), na = s->attrs.size();
+  if (na + nn > 0x7FFFFFFFu) return YV_ERR_UNSUPPORTED;
+  for (const auto& n : s->nodes)
+    for (int ch = 0; ch < 8; ++ch) {
+      const uint32_t c = n.child[ch];
+      if ((n.flags >> ch) & 1u) {
+        if (c >= na) return YV_ERR_BAD_POOL;
+      } else if (!(c & 0x80000000u) && c >= nn) {
+        return YV_ERR_BAD_POOL;
+      }
+    }
+  // per node: sums of r, g, b, nx, ny, nz and the leaf count of its subtree,
+  // post-order over an explicit stack (children before parents)
+  struct Acc {
+    int64_t v[6];
+    int64_t n;
+  };
+  try {
+    std::vector<Acc> acc(nn);
+    std::vector<uint8_t> state(nn, 0);  // 0 new, 1 open, 2 done
+    std::vector<uint32_t> stack;
+    for (size_t start = 0; start < nn; ++start) {
+      if (state[start]) continue;
+      stack.push_back((uint32_t)start);
+      while (!stack.empty()) {
+        const uint32_t id = stack.back();
+        const yv_vox_node& n = s->nodes[id];
+        if (state[id] == 0) {
+          state[id] = 1;
+          for (int ch = 0; ch < 8; ++ch) {
+            const uint32_t c = n.child[ch];
+            if (((n.flags >> ch) & 1u) || (c & 0x80000000u)) continue;
+            if (state[c] == 1) return YV_ERR_BAD_POOL;  // cycle
+            if (state[c] == 0) stack.push_back(c);
+          }
+          continue;
+        }
+        stack.pop_back();
+        if (state[id] == 2) continue;
+        Acc a{};
+        for (int ch = 0; ch < 8; ++ch) {
+          const uint32_t c = n.child[ch];
+          if ((n.flags >> ch) & 1u) {
+            const yv_leaf_attr& l = s->attrs[c];
+            a.v[0] += l.r;
+            a.v[1] += l.g;
+            a.v[2] += l.b;
+            a.v[3] += l.nx;
+            a.v[4] += l.ny;
+            a.v[5] += l.nz;
+            a.n += 1;
+          } else if (!(c & 0x80000000u)) {
+            for (int k = 0; k < 6; ++k) a.v[k] += acc[c].v[k];
+            a.n += acc[c].n;
+          }
+        }
+        acc[id] = a;
+        state[id] = 2;
+      }
+    }
+    s->attrs.reserve(na + nn);
+    for (size_t id = 0; id < nn; ++id) {
+      const Acc& a = acc[id];
+      yv_leaf_attr l;
+      std::memset(&l, 0, sizeof(l));
+      if (a.n > 0) {
+        l.r = (uint8_t)mean_round(a.v[0], a.n);
+        l.g = (uint8_t)mean_round(a.v[1], a.n);
+        l.b = (uint8_t)mean_round(a.v[2], a.n);
+        l.a = 255;
+        l.nx = (int8_t)mean_round(a.v[3], a.n);
+        l.ny = (int8_t)mean_round(a.v[4], a.n);
+        l.nz = (int8_t)mean_round(a.v[5], a.n);
+      }
+      s->attrs.push_back(l);
+      s->nodes[id].data = (uint32_t)(na + id);
+    }
+    s->lod = true;
+    return YV_OK;
+  } catch (const std::bad_alloc&) {
+    return YV_ERR_OUT_OF_MEMORY;
+  }
+}
 
 yv_status yv_svo_validate(const yv_vox_node* nodes, uint32_t count,
                           uint32_t root, uint32_t nattrs) {

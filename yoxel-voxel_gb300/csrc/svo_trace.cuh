@@ -229,10 +229,14 @@ __device__ __forceinline__ bool begin_trace(const SvoDeviceScene& sc, float px, 
 // range and at most YV_MAX_DEPTH levels deep when it is built, so it needs
 // none of these.  In both cases a push happens at level < YV_MAX_DEPTH - 1,
 // so at most YV_MAX_DEPTH - 1 frames are ever held.
-template <bool kRef, int kRing, bool kStaged = false>
+// kLod (library layout only): before descending into a subtree whose cube
+// side 2^-(level+1) is smaller than max(t_enter, 0) * lod_coef, the ray stops
+// there as at a leaf, with the subtree's level-of-detail attribute.
+template <bool kRef, int kRing, bool kStaged = false, bool kLod = false>
 __device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint32_t* sm,
                                           uint32_t nsm, Frame* stk, uint4* ring, Trace& tr,
-                                          bool cull, uint32_t& leaf, uint32_t& err) {
+                                          bool cull, uint32_t& leaf, uint32_t& err,
+                                          float lod_coef = 0.f) {
   const uint32_t w = child_word<kRef, kStaged>(sc, sm, nsm, tr.node, tr.ch ^ tr.df);
   const bool ahead = fmin3(tr.t.x2, tr.t.y2, tr.t.z2) > 0.f;
   // exit axis of the current child and whether it is the last one along
@@ -245,6 +249,14 @@ __device__ __forceinline__ int trace_step(const SvoDeviceScene& sc, const uint32
       return kHit;
     }
   } else if (!(w & YV_DW_NULL) && ahead) {
+    if (kLod) {
+      const float side = __int_as_float((126 - tr.level) << 23);  // 2^-(level+1)
+      const float te = fmaxf(fmax3(tr.t.x1, tr.t.y1, tr.t.z1), 0.f);
+      if (side < __fmul_rn(te, lod_coef)) {
+        leaf = __ldg(sc.node_data + w);
+        return kHit;
+      }
+    }
     // descend: the recursive call of cell/ppu_renderer.cpp:34
     if (kRef) {
       if (tr.fetches >= kFetchCap) {
@@ -375,7 +387,8 @@ __device__ __forceinline__ void write_pixel(const SvoFrameArgs& a, uint32_t off,
 // there (measured: reading every record through L1 is as fast or faster,
 // so the default is unstaged and nsm = 0).
 // Dynamic shared memory = 32 B x nsm staged nodes + 1 KB x kRing per warp.
-template <int kMinBlocks, bool kRef, int kRing, bool kStaged>
+// kLod: level-of-detail cut-off (a.lod_coef, sc.node_data; library layout).
+template <int kMinBlocks, bool kRef, int kRing, bool kStaged, bool kLod = false>
 __global__ void __launch_bounds__(256, kMinBlocks)
     svo_frame_kernel(SvoDeviceScene sc, SvoFrameArgs a, uint32_t nsm, uint32_t refill_min) {
   extern __shared__ uint4 smem[];
@@ -438,8 +451,8 @@ __global__ void __launch_bounds__(256, kMinBlocks)
 #pragma unroll
       for (int k = 0; k < kStepsPerVote; ++k)
         if ((mode == kPrimary || mode == kShadow) && r == kContinue)
-          r = trace_step<kRef, kRing, kStaged>(sc, smw, nsm, stk, ring, tr, mode == kShadow,
-                                               leaf, err);
+          r = trace_step<kRef, kRing, kStaged, kLod>(sc, smw, nsm, stk, ring, tr,
+                                                     mode == kShadow, leaf, err, a.lod_coef);
       if (r != kContinue) {
         if (mode == kShadow) {
           // end of a shadow ray

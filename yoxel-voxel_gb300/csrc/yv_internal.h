@@ -39,6 +39,7 @@ struct yv_svo_host {
   std::vector<yv_leaf_attr> attrs;
   uint32_t root = YV_EMPTY_NODE;
   int depth = 0;
+  bool lod = false;  // every node's `data` indexes its level-of-detail attribute
 };
 
 namespace yv {

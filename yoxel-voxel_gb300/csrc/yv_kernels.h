@@ -15,6 +15,8 @@ struct SvoDeviceScene {
   // library layout: 16-byte shading records {RGBA8, unit normal xyz fp32};
   // caller VoxNode pools: the caller's yv_leaf_attr (8 bytes)
   const void* attrs = nullptr;
+  // level-of-detail attribute index of every node (device order), or null
+  const uint32_t* node_data = nullptr;
   uint32_t n_nodes = 0;
   uint32_t n_attrs = 0;
   uint32_t root_word = 0x40000000u;
@@ -29,6 +31,7 @@ struct SvoFrameArgs {
   float ambient, diffuse;
   int shadows;
   int width, height;
+  float lod_coef;                // > 0: stop at subtrees smaller than t * lod_coef
   uint32_t* rgba;                // optional outputs (device)
   uint32_t* hit;
   float* hit_t;

@@ -120,6 +120,8 @@ _SIGS = {
     "yv_svo_from_arrays": (S, [C.POINTER(P), P, U32, U32, P, U32]),
     "yv_svo_load_vox": (S, [C.POINTER(P), C.c_char_p]),
     "yv_svo_save_vox": (S, [P, C.c_char_p]),
+    "yv_svo_build_lod": (S, [P]),
+    "yv_svo_has_lod": (I32, [P]),
     "yv_svo_free": (None, [P]),
     "yv_svo_node_count": (U32, [P]),
     "yv_svo_root": (U32, [P]),
@@ -141,6 +143,8 @@ _SIGS = {
     "yv_set_resolution": (S, [P, I32, I32]),
     "yv_get_resolution": (S, [P, C.POINTER(I32), C.POINTER(I32)]),
     "yv_set_fov": (S, [P, C.c_float]),
+    "yv_set_detail_coef": (S, [P, C.c_float]),
+    "yv_get_detail_coef": (S, [P, C.POINTER(C.c_float)]),
     "yv_set_light": (S, [P, C.POINTER(Light)]),
     "yv_set_launch_config": (S, [P, C.POINTER(LaunchConfig)]),
     "yv_get_launch_config": (S, [P, C.POINTER(LaunchConfig)]),

@@ -44,6 +44,7 @@ class Renderer:
         L.check(L.lib.yv_renderer_create(C.byref(h)), "yv_renderer_create")
         self._h = h
         self._scene = None
+        self._fov = 70.0  # RendererBase default (cell/renderer_base.h:25)
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -98,6 +99,27 @@ class Renderer:
 
     def SetFOV(self, fov):
         L.check(L.lib.yv_set_fov(self._h, float(fov)), "SetFOV")
+        self._fov = float(np.float32(fov))
+
+    def SetDetailCoef(self, coef):
+        """SVORenderer::SetDetailCoef: level-of-detail cut-off (0 = exact
+        leaves; needs a scene with level-of-detail data)."""
+        L.check(L.lib.yv_set_detail_coef(self._h, float(coef)), "SetDetailCoef")
+
+    def GetDetailCoef(self):
+        c = C.c_float()
+        L.check(L.lib.yv_get_detail_coef(self._h, C.byref(c)), "GetDetailCoef")
+        return c.value
+
+    def lod_coef(self):
+        """The per-frame cut-off coefficient detail * radians(fov / 2) /
+        width, as the frame uses it (float32)."""
+        import math
+        w, _ = self.GetResolution()
+        f = C.c_float()
+        L.check(L.lib.yv_get_detail_coef(self._h, C.byref(f)), "GetDetailCoef")
+        return float(np.float32(float(f.value) * float(np.float32(self._fov)) *
+                                (math.pi / 360.0) / float(w)))
 
     def SetLight(self, direction, ambient=0.15, diffuse=0.85, shadows=False):
         lt = L.Light(_f3(direction), float(ambient), float(diffuse), 1 if shadows else 0)

@@ -77,6 +77,17 @@ class SVOScene:
     def save(self, path):
         L.check(L.lib.yv_svo_save_vox(self._h, str(path).encode()), "yv_svo_save_vox")
 
+    def build_lod(self):
+        """Level-of-detail data (reaction/report/main.tex:61): every node's
+        `data` indexes a new attribute holding the mean colour and normal
+        of its subtree's leaves.  Returns self."""
+        L.check(L.lib.yv_svo_build_lod(self._h), "yv_svo_build_lod")
+        return self
+
+    @property
+    def has_lod(self):
+        return bool(L.lib.yv_svo_has_lod(self._h))
+
     # ---- views --------------------------------------------------------
     @property
     def handle(self):
