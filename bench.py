@@ -15,6 +15,7 @@ steps outside the events.  The K steps sit between barrier + synchronize.
 """
 import argparse
 import json
+import math
 import os
 import re
 import statistics
@@ -58,6 +59,12 @@ CONFIGS = {
                  workload="2048^3 (SVO depth 11) seeded 6-octave value-noise terrain + 10k "
                           "floating cubes, 1920x1080 FP32 primary rays + 1 hard-shadow ray "
                           "per hit"),
+    "lod": dict(kind="svo", scene=("terrain", dict(depth=11, n_cubes=10000, cube_min=2,
+                                                   cube_max=16, seed=1234)),
+                width=1920, height=1080, shadows=True, detail=4.0,
+                workload="cfg2 (2048^3 terrain, 1920x1080 + 1 hard-shadow ray per hit) with "
+                         "level-of-detail data and the cut-off at detail coefficient 4 "
+                         "(subtrees under 2 pixels: side < t * 4 * radians(30) / 1920)"),
     "cfg3": dict(kind="brick", levels=3, width=1024, height=1024, alpha_scale=1.0,
                  step_vox=0.5, precision=3,
                  workload="N=4 brick tree, 3 grid levels + 8^3 bricks = 512^3, fp16 density "
@@ -197,14 +204,19 @@ def make_scene(cfg):
     import yoxel
     kind, kw = cfg["scene"]
     if kind == "spheres":
-        return yoxel.SVOScene.spheres(**kw)
-    return yoxel.SVOScene.terrain(**kw)
+        s = yoxel.SVOScene.spheres(**kw)
+    else:
+        s = yoxel.SVOScene.terrain(**kw)
+    if cfg.get("detail"):
+        s.build_lod()
+    return s
 
 
 # --------------------------------------------------------------- CPU oracle
-def cpu_svo(cfg, scene, width, height, threads, min_seconds=0.0, max_runs=1):
+def cpu_svo(cfg, scene, width, height, threads, min_seconds=0.0, max_runs=1, lod_coef=0.0):
     """Times the FP32 oracle (restatement of the reference CPU renderer) on
-    `threads` host threads.  Returns (Mrays/s, seconds per run, rays per run)."""
+    `threads` host threads.  Returns (Mrays/s, seconds per run, rays per run).
+    lod_coef: the level-of-detail cut-off of the full-size frame."""
     from oracle import pyoracle
     pos, view = camera()
     runs, t_tot, rays = 0, 0.0, 0
@@ -212,7 +224,7 @@ def cpu_svo(cfg, scene, width, height, threads, min_seconds=0.0, max_runs=1):
         t0 = time.perf_counter()
         o = pyoracle.svo_render(scene.nodes_u32, scene.root, scene.attrs_u8, pos, view,
                                 [0, 0, 1], 60.0, width, height, LIGHT,
-                                shadows=cfg["shadows"], threads=threads)
+                                shadows=cfg["shadows"], threads=threads, lod_coef=lod_coef)
         t_tot += time.perf_counter() - t0
         runs += 1
         hits = int((o["hit"] != 0xFFFFFFFF).sum())
@@ -234,7 +246,10 @@ def run_reference(args, cfg):
     w, h = cfg["width"] // 2, cfg["height"] // 2
     if cfg["kind"] == "svo":
         scene = make_scene(cfg)
-        step = lambda: cpu_svo(cfg, scene, w, h, threads)
+        # the cut-off of the full-size frame (detail * radians(fov / 2) / width)
+        lod = (float(np.float32(cfg["detail"] * 60.0 * (math.pi / 360.0) / cfg["width"]))
+               if cfg.get("detail") else 0.0)
+        step = lambda: cpu_svo(cfg, scene, w, h, threads, lod_coef=lod)
     else:
         import yoxel
         from oracle import pyoracle
@@ -307,6 +322,8 @@ def run_svo(args, cfg):
     r.SetResolution(w, h)
     r.SetFOV(60.0)
     r.SetLight(LIGHT, 0.15, 0.85, cfg["shadows"])
+    r.SetDetailCoef(cfg.get("detail", 0.0))
+    lod_coef = r.lod_coef() if cfg.get("detail") else 0.0
     dev_nodes, dev_bytes = r.device_scene_info()
 
     # algorithmic bytes of this frame: 40 B per node dereference (RecTrace
@@ -419,9 +436,10 @@ def run_svo(args, cfg):
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         sw, sh = w // 4, h // 4
-        v, s, rr = cpu_svo(cfg, scene, sw, sh, threads, min_seconds=10.0, max_runs=50)
-        v1, s1, rr1 = cpu_svo(cfg, scene, w // 16, h // 16, 1)
-        v4, s4, rr4 = cpu_svo(cfg, scene, w // 8, h // 8, 4)
+        v, s, rr = cpu_svo(cfg, scene, sw, sh, threads, min_seconds=10.0, max_runs=50,
+                           lod_coef=lod_coef)
+        v1, s1, rr1 = cpu_svo(cfg, scene, w // 16, h // 16, 1, lod_coef=lod_coef)
+        v4, s4, rr4 = cpu_svo(cfg, scene, w // 8, h // 8, 4, lod_coef=lod_coef)
         line["cpu_baseline"] = {
             "value": round(v, 4), "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{sw}x{sh} frame of the same scene and camera ({rr} rays incl. shadow "

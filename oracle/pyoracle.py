@@ -39,6 +39,8 @@ def load_library(build_if_missing=True):
                                        P, P, P, P, P, P]),
         "orc_svo_render_mt": (I, [I, P, U, U, P, U, P, P, P, P, I, I, P, F, F, I,
                                   P, P, P, P, P, P]),
+        "orc_svo_render_mt_lod": (I, [I, P, U, U, P, U, P, P, P, P, I, I, P, F, F, I, F,
+                                      P, P, P, P, P, P]),
         "orc_svo_hits_f64": (I, [P, U, U, P, P, P, D, I, I, I, I, P, P]),
         "orc_svo_trace_ray_f32": (I, [P, U, U, P, P, I, P, P, P, P]),
         "orc_find_first_child_f32": (None, [P, P, P]),
@@ -126,7 +128,7 @@ def svo_render(nodes_u32, root, attrs_u8, pos, dir_, up, fov, width, height, lig
                ambient=0.15, diffuse=0.85, shadows=False, threads=1, rows=None, lod_coef=0.0):
     """FP32 oracle render.  Returns dict of numpy arrays (rgba u32, hit u32,
     hit_t f32, fetches u32, shadow_fetches u32, shadowed u8).  lod_coef > 0:
-    the level-of-detail cut-off (single thread)."""
+    the level-of-detail cut-off."""
     nodes_u32 = np.ascontiguousarray(nodes_u32, dtype=np.uint32)
     attrs_u8 = np.ascontiguousarray(attrs_u8, dtype=np.uint8)
     count = len(nodes_u32) // 10
@@ -137,7 +139,7 @@ def svo_render(nodes_u32, root, attrs_u8, pos, dir_, up, fov, width, height, lig
                hit_t=np.zeros(n, np.float32), fetches=np.zeros(n, np.uint32),
                shadow_fetches=np.zeros(n, np.uint32), shadowed=np.zeros(n, np.uint8))
     ps, lt = f32(pos), f32(light)
-    if threads <= 1 or rows is not None or lod_coef > 0:
+    if threads <= 1 or rows is not None:
         y0, y1 = (0, height) if rows is None else rows
         st = lib().orc_svo_render_lod_f32(_p(nodes_u32), count, root, _p(attrs_u8), nattrs,
                                           _p(ps), _p(d0), _p(du), _p(dv), width, height,
@@ -147,12 +149,13 @@ def svo_render(nodes_u32, root, attrs_u8, pos, dir_, up, fov, width, height, lig
                                           _p(out["fetches"]), _p(out["shadow_fetches"]),
                                           _p(out["shadowed"]))
     else:
-        st = lib().orc_svo_render_mt(threads, _p(nodes_u32), count, root, _p(attrs_u8),
-                                     nattrs, _p(ps), _p(d0), _p(du), _p(dv), width, height,
-                                     _p(lt), ambient, diffuse, 1 if shadows else 0,
-                                     _p(out["rgba"]), _p(out["hit"]), _p(out["hit_t"]),
-                                     _p(out["fetches"]), _p(out["shadow_fetches"]),
-                                     _p(out["shadowed"]))
+        st = lib().orc_svo_render_mt_lod(threads, _p(nodes_u32), count, root, _p(attrs_u8),
+                                         nattrs, _p(ps), _p(d0), _p(du), _p(dv), width,
+                                         height, _p(lt), ambient, diffuse,
+                                         1 if shadows else 0, float(lod_coef),
+                                         _p(out["rgba"]), _p(out["hit"]), _p(out["hit_t"]),
+                                         _p(out["fetches"]), _p(out["shadow_fetches"]),
+                                         _p(out["shadowed"]))
     if st != 0:
         raise RuntimeError(f"oracle svo render failed: {st}")
     return {k: v.reshape(height, width) for k, v in out.items()}

@@ -172,6 +172,7 @@ typedef struct {
   int width, height;
   float ambient, diffuse;
   int shadows;
+  float lod_coef;
   uint32_t *rgba, *hit, *fetches, *shadow_fetches;
   float* hit_t;
   uint8_t* shadowed;
@@ -191,10 +192,10 @@ static void* band_main(void* arg) {
   /* rows y0, y0+stride, ... (interleaved rows keep threads balanced) */
   for (int y = j->y0; y < j->height && !j->status; y += j->y1) {
     if (j->kind == 0) {
-      j->status = orc_svo_render_f32(
+      j->status = orc_svo_render_lod_f32(
           j->nodes, j->count, j->root, j->attrs, j->nattrs, j->pos, j->dir0,
           j->du, j->dv, j->width, j->height, j->light, j->ambient, j->diffuse,
-          j->shadows, y, y + 1, j->rgba, j->hit, j->hit_t, j->fetches,
+          j->shadows, j->lod_coef, y, y + 1, j->rgba, j->hit, j->hit_t, j->fetches,
           j->shadow_fetches, j->shadowed);
     } else {
       j->status = orc_brick_render_f32(
@@ -248,6 +249,19 @@ int orc_svo_render_mt(int nthreads, const uint32_t* nodes, uint32_t count,
                       float diffuse, int shadows, uint32_t* rgba,
                       uint32_t* hit, float* hit_t, uint32_t* fetches,
                       uint32_t* shadow_fetches, uint8_t* shadowed) {
+  return orc_svo_render_mt_lod(nthreads, nodes, count, root, attrs, nattrs, pos, dir0, du, dv,
+                               width, height, light, ambient, diffuse, shadows, 0.0f, rgba,
+                               hit, hit_t, fetches, shadow_fetches, shadowed);
+}
+
+int orc_svo_render_mt_lod(int nthreads, const uint32_t* nodes, uint32_t count,
+                          uint32_t root, const uint8_t* attrs, uint32_t nattrs,
+                          const float pos[3], const float dir0[3],
+                          const float du[3], const float dv[3], int width,
+                          int height, const float light[3], float ambient,
+                          float diffuse, int shadows, float lod_coef, uint32_t* rgba,
+                          uint32_t* hit, float* hit_t, uint32_t* fetches,
+                          uint32_t* shadow_fetches, uint8_t* shadowed) {
   band_job p;
   memset(&p, 0, sizeof(p));
   p.kind = 0;
@@ -272,6 +286,7 @@ int orc_svo_render_mt(int nthreads, const uint32_t* nodes, uint32_t count,
   p.fetches = fetches;
   p.shadow_fetches = shadow_fetches;
   p.shadowed = shadowed;
+  p.lod_coef = lod_coef;
   return run_bands(&p, nthreads);
 }
 

@@ -77,6 +77,16 @@ int orc_svo_render_mt(int nthreads, const uint32_t* nodes, uint32_t count,
                       uint32_t* hit, float* hit_t, uint32_t* fetches,
                       uint32_t* shadow_fetches, uint8_t* shadowed);
 
+/* The same with the level-of-detail cut-off (see orc_svo_render_lod_f32). */
+int orc_svo_render_mt_lod(int nthreads, const uint32_t* nodes, uint32_t count,
+                          uint32_t root, const uint8_t* attrs, uint32_t nattrs,
+                          const float pos[3], const float dir0[3],
+                          const float du[3], const float dv[3], int width,
+                          int height, const float light[3], float ambient,
+                          float diffuse, int shadows, float lod_coef, uint32_t* rgba,
+                          uint32_t* hit, float* hit_t, uint32_t* fetches,
+                          uint32_t* shadow_fetches, uint8_t* shadowed);
+
 /* FP64 evaluation of the primary hits (camera basis recomputed in double);
  * used to count rays whose hit voxel is decided by a float rounding tie. */
 int orc_svo_hits_f64(const uint32_t* nodes, uint32_t count, uint32_t root,
