@@ -216,6 +216,14 @@ yv_status yv_set_scene_svo(yv_renderer* r, const yv_vox_node* nodes,
                            const yv_leaf_attr* attrs, uint32_t nattrs);
 yv_status yv_set_scene_host(yv_renderer* r, const yv_svo_host* svo);
 yv_status yv_load_scene_vox(yv_renderer* r, const char* path);
+/* SVORenderer::SetScene(DynamicSVO*) (demo/SVORenderer.cpp:33-53): the
+ * renderer keeps a non-owning pointer to an editable scene (declared below)
+ * and traces its device mirror in place, as of the scene's last
+ * yv_svo_dynamic_sync (UpdateSVO); hit words carry the pool's own node ids.
+ * The scene must outlive the binding.  Not batchable; no level-of-detail
+ * cut-off. */
+typedef struct yv_svo_dynamic yv_svo_dynamic;
+yv_status yv_set_scene_dynamic(yv_renderer* r, const yv_svo_dynamic* s);
 /* The same GPU build (yv_svo_build_dense) straight into the renderer's
  * device layout: no host copy of the pool.  Node ids are the breadth-first
  * ids of yv_svo_build_dense. */
@@ -464,8 +472,8 @@ yv_status yv_render_svo_noalloc(const yv_vox_node* nodes, uint32_t count,
  * attributes) with a version per page bumped on every edit; a sync sends
  * only the pages changed since the last one (gathered into one pinned
  * staging copy and scattered on the device).  Frames are traced from the
- * mirror with yv_render_svo_noalloc (caller node ids).  Not thread-safe. */
-typedef struct yv_svo_dynamic yv_svo_dynamic;
+ * mirror with yv_render_svo_noalloc (caller node ids) or by a renderer bound
+ * with yv_set_scene_dynamic (type declared above).  Not thread-safe. */
 yv_status yv_svo_dynamic_create(uint32_t node_capacity, uint32_t attr_capacity,
                                 yv_svo_dynamic** out);
 void      yv_svo_dynamic_destroy(yv_svo_dynamic* s);
@@ -492,7 +500,12 @@ uint32_t  yv_svo_dynamic_changed_pages(const yv_svo_dynamic* s);
 uint64_t  yv_svo_dynamic_transfer_bytes(const yv_svo_dynamic* s);
 /* Sends the changed pages on `stream` (UpdateSVO). */
 yv_status yv_svo_dynamic_sync(yv_svo_dynamic* s, void* stream);
-/* The device mirror (after a sync) and the host pool. */
+/* The device mirror as of the last sync (pointers, node slots in use, root,
+ * attributes in use) and the host pool.  yv_svo_dynamic_host_info gives the
+ * host pool's current node slots in use, root and attribute count
+ * (download and host arrays are sized by them). */
+yv_status yv_svo_dynamic_host_info(const yv_svo_dynamic* s, uint32_t* count,
+                                   uint32_t* root, uint32_t* nattrs);
 yv_status yv_svo_dynamic_device(const yv_svo_dynamic* s,
                                 const yv_vox_node** nodes, uint32_t* count,
                                 uint32_t* root, const yv_leaf_attr** attrs,

@@ -66,3 +66,66 @@ def test_dynamic_from_empty_and_paging(yoxel_mod, oracle):
     dyn.set_voxel(5, 31, 31, 31, rgb=(1, 2, 3))
     assert 1 <= dyn.changed_pages() <= 4
     check_mirror_and_frame(yoxel_mod, oracle, dyn, False)
+
+
+def test_renderer_bound_to_editable_scene(yoxel_mod, oracle):
+    """SVORenderer::SetScene(DynamicSVO*) + UpdateSVO: the renderer traces
+    the mirror in place as of the last sync; edits show after a sync."""
+    import torch
+    depth = 6
+    scene = yoxel_mod.SVOScene.spheres(depth, 30, 2.0, 8.0, 21)
+    dyn = yoxel_mod.DynamicSVO(scene.node_count + 4096, scene.attr_count + 8192)
+    dyn.load(scene)
+    dyn.sync()
+    r = yoxel_mod.Renderer()
+    r.SetSceneDynamic(dyn)
+    pos, view = camera_for()
+    up = np.array([0, 0, 1], np.float32)
+    r.SetViewPos(pos)
+    r.SetViewDir(view)
+    r.SetViewUp(up)
+    r.SetResolution(80, 64)
+    r.SetFOV(60.0)
+    r.SetLight(LIGHT, 0.15, 0.85, True)
+
+    def frame():
+        o = r.render_outputs()
+        o.pop("stats")
+        return {k: v.cpu().numpy().view(np.uint32).reshape(-1)
+                for k, v in o.items() if k in ("hit", "rgba", "fetches")}
+
+    def oracle_frame():
+        nodes, root, attrs = dyn.host_arrays()
+        return oracle.svo_render(nodes.view(np.uint32), root, attrs.view(np.uint8), pos, view,
+                                 up, 60.0, 80, 64, LIGHT, shadows=True)
+
+    g0 = frame()
+    o0 = oracle_frame()
+    for k in g0:
+        assert np.array_equal(g0[k], o0[k].reshape(-1)), k
+    # edit: until the sync the renderer still shows the synced state
+    rng = np.random.default_rng(5)
+    G = 1 << depth
+    for _ in range(60):
+        x, y, z = (int(v) for v in rng.integers(G // 4, 3 * G // 4, 3))
+        dyn.set_voxel(depth, x, y, z, rgb=(250, 20, 20), normal=(0, 0, 127))
+    g1 = frame()
+    for k in g0:
+        assert np.array_equal(g1[k], g0[k]), k
+    dyn.sync()
+    torch.cuda.synchronize()
+    g2 = frame()
+    o2 = oracle_frame()
+    for k in g2:
+        assert np.array_equal(g2[k], o2[k].reshape(-1)), k
+    assert not np.array_equal(g2["hit"], g0["hit"])
+    # the screen-space pipeline runs on the bound scene too
+    rgba = r.render_ssna()
+    r.frame_stats()
+    assert (rgba.cpu().numpy().view(np.uint32) >> 24).any()
+    # batching a renderer bound to an editable scene is refused
+    from yoxel import _lib as L
+    b = yoxel_mod.Batch()
+    out = torch.empty((64, 80), dtype=torch.int32, device="cuda")
+    with pytest.raises(L.YvError):
+        b.add_svo(r, out)

@@ -34,6 +34,9 @@ struct yv_renderer {
   uint32_t* d_node_data = nullptr;  // level-of-detail attribute per node, or null
   size_t cap_nodes = 0, cap_attrs = 0;  // allocated records of the three
   float detail = 0.f;  // SVORenderer::m_detailCoef; 0 = exact leaves
+  // SVORenderer::SetScene(DynamicSVO*): a non-owned editable scene whose
+  // device mirror (as of its last sync) is traced in place
+  const yv_svo_dynamic* dyn = nullptr;
   SvoDeviceScene scene;
   bool has_scene = false;
   uint64_t scene_bytes = 0;
@@ -73,6 +76,25 @@ static void free_scene(yv_renderer* r) {
   r->has_scene = false;
   r->scene = SvoDeviceScene();
   r->scene_bytes = 0;
+  r->dyn = nullptr;
+}
+
+// The scene the kernels see: the renderer's own device copy, or the
+// current synced state of a bound editable scene.
+static SvoDeviceScene scene_of(const yv_renderer* r) {
+  if (!r->dyn) return r->scene;
+  const yv_vox_node* nodes = nullptr;
+  const yv_leaf_attr* attrs = nullptr;
+  uint32_t count = 0, root = YV_EMPTY_NODE, nattrs = 0;
+  yv_svo_dynamic_device(r->dyn, &nodes, &count, &root, &attrs, &nattrs);
+  SvoDeviceScene sc;
+  sc.nodes = reinterpret_cast<const uint4*>(nodes);
+  sc.attrs = attrs;
+  sc.n_nodes = count;
+  sc.n_attrs = nattrs;
+  sc.root_word = (root & 0x80000000u) || !nodes ? YV_DW_NULL : root;
+  sc.ref_layout = 1;
+  return sc;
 }
 
 namespace yv {
@@ -87,6 +109,7 @@ yv_status renderer_scene_buffers(yv_renderer* r, uint32_t nn, uint32_t na, uint3
   if (r->frame_pending) cudaStreamSynchronize(r->last_stream);
   r->has_scene = false;
   r->scene = SvoDeviceScene();
+  r->dyn = nullptr;
   cudaFree(r->d_node_data);
   r->d_node_data = nullptr;
   const size_t want_n = nn ? nn : 1, want_a = na ? na : 1;
@@ -290,6 +313,16 @@ yv_status yv_get_detail_coef(const yv_renderer* r, float* coef) {
   return YV_OK;
 }
 
+yv_status yv_set_scene_dynamic(yv_renderer* r, const yv_svo_dynamic* s) {
+  if (!r || !s) return YV_ERR_INVALID_ARG;
+  YV_CUDA(cudaSetDevice(r->device), "cudaSetDevice");
+  if (r->frame_pending) cudaStreamSynchronize(r->last_stream);
+  free_scene(r);
+  r->dyn = s;
+  r->has_scene = true;
+  return YV_OK;
+}
+
 yv_status yv_load_scene_vox(yv_renderer* r, const char* path) {
   if (!r || !path) return YV_ERR_INVALID_ARG;
   yv_svo_host* h = nullptr;
@@ -370,7 +403,7 @@ yv_status yv_get_ray_basis(const yv_renderer* r, float dir0[3], float du[3], flo
 
 yv_status yv_get_device_scene_info(const yv_renderer* r, uint64_t* nodes, uint64_t* bytes) {
   if (!r || !nodes || !bytes) return YV_ERR_INVALID_ARG;
-  *nodes = r->scene.n_nodes;
+  *nodes = scene_of(r).n_nodes;
   *bytes = r->scene_bytes;
   return YV_OK;
 }
@@ -402,7 +435,7 @@ static void fill_frame_args(const yv_renderer* r, SvoFrameArgs& a) {
 namespace yv {
 bool renderer_view(const yv_renderer* r, yv_renderer_view* v) {
   if (!r) return false;
-  v->sc = r->scene;
+  v->sc = scene_of(r);
   fill_frame_args(r, v->fa);
   v->fov_deg = r->fov;
   return r->has_scene;
@@ -431,7 +464,7 @@ static yv_status enqueue_frame(yv_renderer* r, const yv_frame_outputs* out, cuda
   a.normal = static_cast<float*>(out->normal);
   a.counters = r->d_counters;
   int launches = 0;
-  YV_CUDA(launch_svo_frame(r->scene, a, r->cfg, s, &launches), "svo frame launch");
+  YV_CUDA(launch_svo_frame(scene_of(r), a, r->cfg, s, &launches), "svo frame launch");
   r->last_stream = s;
   r->last_pixels = (uint64_t)r->width * (uint64_t)r->height;
   r->last_shadows = a.shadows;

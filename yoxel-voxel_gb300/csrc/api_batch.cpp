@@ -152,6 +152,10 @@ yv_status yv_batch_add_svo(yv_batch* b, const yv_renderer* r, void* d_rgba) {
   if ((int)b->items.size() >= kMaxBatchItems) return YV_ERR_UNSUPPORTED;
   yv_renderer_view v;
   if (!renderer_view(r, &v)) return YV_ERR_NO_SCENE;
+  if (v.sc.ref_layout) {
+    set_last_error("yv_batch_add_svo: a renderer bound to an editable scene cannot be batched");
+    return YV_ERR_UNSUPPORTED;
+  }
   BatchItem it{};
   it.kind = kBatchSvo;
   it.width = v.fa.width;

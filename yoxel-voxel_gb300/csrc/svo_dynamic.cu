@@ -39,6 +39,8 @@ struct yv_svo_dynamic {
   uint32_t n_attrs = 0;
   uint32_t root = YV_EMPTY_NODE;
   int depth = 0;
+  // the state the device mirror holds (set by a sync)
+  uint32_t synced_root = YV_EMPTY_NODE, synced_nodes = 0, synced_attrs = 0;
   // page versions: host (bumped on edit) and the version last sent
   std::vector<uint32_t> ver_n, sent_n, ver_a, sent_a;
   yv_vox_node* d_nodes = nullptr;
@@ -361,18 +363,33 @@ yv_status yv_svo_dynamic_sync(yv_svo_dynamic* s, void* stream) {
   if (e == cudaSuccess)
     e = sync_array(s, reinterpret_cast<const uint8_t*>(s->attrs.data()), sizeof(yv_leaf_attr),
                    s->n_attrs, s->ver_a, s->sent_a, s->d_attrs, st);
-  return e == cudaSuccess ? YV_OK : dyn_fail(e, "sync");
+  if (e != cudaSuccess) return dyn_fail(e, "sync");
+  s->synced_root = s->root;
+  s->synced_nodes = s->n_nodes;
+  s->synced_attrs = s->n_attrs;
+  return YV_OK;
 }
 
-// The device mirror, for yv_render_svo_noalloc (valid after a sync).
+// The device mirror as of the last sync, for yv_render_svo_noalloc and the
+// renderer (SVORenderer::UpdateSVO hands the tree to the kernels after the
+// transfer, demo/SVORenderer.cpp:39-53).
 yv_status yv_svo_dynamic_device(const yv_svo_dynamic* s, const yv_vox_node** nodes,
                                 uint32_t* count, uint32_t* root, const yv_leaf_attr** attrs,
                                 uint32_t* nattrs) {
   if (!s || !nodes || !count || !root || !attrs || !nattrs) return YV_ERR_INVALID_ARG;
   *nodes = s->d_nodes;
+  *count = s->synced_nodes;
+  *root = s->synced_root;
+  *attrs = s->d_attrs;
+  *nattrs = s->synced_attrs;
+  return YV_OK;
+}
+
+yv_status yv_svo_dynamic_host_info(const yv_svo_dynamic* s, uint32_t* count, uint32_t* root,
+                                   uint32_t* nattrs) {
+  if (!s || !count || !root || !nattrs) return YV_ERR_INVALID_ARG;
   *count = s->n_nodes;
   *root = s->root;
-  *attrs = s->d_attrs;
   *nattrs = s->n_attrs;
   return YV_OK;
 }

@@ -52,10 +52,10 @@ cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t s) {
 
 cudaError_t scratch_free(void* p, cudaStream_t s) { return p ? cudaFreeAsync(p, s) : cudaSuccess; }
 
-template <int kMinBlocks, bool kStaged, bool kLod = false>
+template <int kMinBlocks, bool kStaged, bool kLod = false, bool kRef = false>
 static cudaError_t launch_with(const SvoDeviceScene& sc, const SvoFrameArgs& a, int bt,
                                uint32_t nsm, uint32_t refill, int per_sm, cudaStream_t stream) {
-  auto kern = svo_frame_kernel<kMinBlocks, false, kSvoRing, kStaged, kLod>;
+  auto kern = svo_frame_kernel<kMinBlocks, kRef, kSvoRing, kStaged, kLod>;
   const size_t smem = (size_t)nsm * 32u + (size_t)(bt / 32) * kSvoRing * 1024u;
   if (smem > 48u * 1024u) {
     static bool opted_in[64] = {false};
@@ -98,7 +98,11 @@ cudaError_t launch_svo_frame(const SvoDeviceScene& sc, const SvoFrameArgs& a,
   // 0 = default 4 (fastest on the 2048^3 frame with unstaged node reads)
   const int mb = cfg.blocks_per_sm <= 0 ? 4 : (cfg.blocks_per_sm > 4 ? 4 : cfg.blocks_per_sm);
   cudaError_t e;
-  if (a.lod_coef > 0.f && sc.node_data) {
+  if (sc.ref_layout) {
+    // a caller VoxNode pool (an editable scene's device mirror): checked
+    // traversal, the default launch shape
+    e = launch_with<3, false, false, true>(sc, a, bt, 0, refill, 0, stream);
+  } else if (a.lod_coef > 0.f && sc.node_data) {
     // level-of-detail frames: one instantiation, the default launch shape
     e = launch_with<4, false, true>(sc, a, bt, 0, refill, 0, stream);
   } else if (nsm == 0) {

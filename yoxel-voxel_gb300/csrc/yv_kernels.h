@@ -20,6 +20,9 @@ struct SvoDeviceScene {
   uint32_t n_nodes = 0;
   uint32_t n_attrs = 0;
   uint32_t root_word = 0x40000000u;
+  // host-side: 1 = `nodes` / `attrs` are a caller VoxNode pool (40-byte
+  // records, 8-byte attributes, pool ids as root and children)
+  uint32_t ref_layout = 0;
 };
 
 // One frame of the SVO renderer.

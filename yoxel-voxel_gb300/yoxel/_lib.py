@@ -137,6 +137,7 @@ _SIGS = {
     "yv_set_scene_host": (S, [P, P]),
     "yv_load_scene_vox": (S, [P, C.c_char_p]),
     "yv_set_scene_dense": (S, [P, P, P, C.c_int32, C.c_float, P]),
+    "yv_set_scene_dynamic": (S, [P, P]),
     "yv_set_view_pos": (S, [P, F3]),
     "yv_set_view_dir": (S, [P, F3]),
     "yv_set_view_up": (S, [P, F3]),
@@ -205,6 +206,7 @@ _SIGS = {
     "yv_svo_dynamic_host_nodes": (P, [P]),
     "yv_svo_dynamic_host_attrs": (P, [P]),
     "yv_svo_dynamic_download": (S, [P, P, P]),
+    "yv_svo_dynamic_host_info": (S, [P, C.POINTER(U32), C.POINTER(U32), C.POINTER(U32)]),
     "yv_render_svo_noalloc": (S, [P, U32, U32, P, U32, C.POINTER(Camera), C.POINTER(Light),
                                   C.c_int32, C.c_int32, C.POINTER(FrameOutputs), P]),
     "yv_ssna_defaults": (S, [P, C.POINTER(SsnaParams)]),

@@ -61,13 +61,20 @@ class DynamicSVO:
                                             C.byref(a), C.byref(na)), "yv_svo_dynamic_device")
         return n, cnt.value, root.value, a, na.value
 
+    def _host(self):
+        cnt, root, na = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        L.check(L.lib.yv_svo_dynamic_host_info(self._h, C.byref(cnt), C.byref(root),
+                                               C.byref(na)), "yv_svo_dynamic_host_info")
+        return cnt.value, root.value, na.value
+
     @property
     def root(self):
-        return self._device()[2]
+        """Root of the host pool (the device mirror takes it at the next sync)."""
+        return self._host()[1]
 
     def host_arrays(self):
         """Copies of the host pool: (nodes, root, attrs) structured arrays."""
-        _, cnt, root, _, na = self._device()
+        cnt, root, na = self._host()
         nodes = np.frombuffer((C.c_uint8 * (cnt * 40)).from_address(
             L.lib.yv_svo_dynamic_host_nodes(self._h)), dtype=NODE_DTYPE).copy()
         attrs = np.frombuffer((C.c_uint8 * (na * 8)).from_address(
@@ -75,8 +82,9 @@ class DynamicSVO:
         return nodes, root, attrs
 
     def download(self):
-        """The device mirror copied back: (nodes, attrs)."""
-        _, cnt, _, _, na = self._device()
+        """The device mirror copied back: (nodes, attrs), sized like the host
+        pool (equal to it after a sync)."""
+        cnt, _, na = self._host()
         nodes = np.zeros(cnt, NODE_DTYPE)
         attrs = np.zeros(na, ATTR_DTYPE)
         L.check(L.lib.yv_svo_dynamic_download(self._h, nodes.ctypes.data, attrs.ctypes.data),

@@ -72,6 +72,13 @@ class Renderer:
                 "SetSceneDense")
         self._scene = None
 
+    def SetSceneDynamic(self, dyn):
+        """SVORenderer::SetScene(DynamicSVO*): trace an editable scene's device
+        mirror in place (as of its last sync); the renderer keeps a
+        reference to it."""
+        L.check(L.lib.yv_set_scene_dynamic(self._h, dyn._h), "SetSceneDynamic")
+        self._scene = dyn
+
     def SetSceneArrays(self, nodes, root, attrs):
         from .svo import ATTR_DTYPE, NODE_DTYPE
         nodes = np.ascontiguousarray(nodes, dtype=NODE_DTYPE)
