@@ -240,6 +240,7 @@ yv_status yv_set_view_up(yv_renderer* r, const float up[3]);
 yv_status yv_set_resolution(yv_renderer* r, int width, int height);
 yv_status yv_get_resolution(const yv_renderer* r, int* width, int* height);
 yv_status yv_set_fov(yv_renderer* r, float fov_deg);
+yv_status yv_get_fov(const yv_renderer* r, float* fov_deg);  /* SVORenderer::GetFOV */
 yv_status yv_set_light(yv_renderer* r, const yv_light* light);
 /* SVORenderer::SetDetailCoef / GetDetailCoef (demo/SVORenderer.h:25-26):
  * level-of-detail cut-off.  With coef > 0 and a scene set from a host

@@ -160,6 +160,12 @@ class GPURenderer : public ISVORenderer {
   void SetFOV(float fov) override {
     if (r_) status_ = yv_set_fov(r_, fov);
   }
+  /* demo/SVORenderer.h:22 */
+  float GetFOV() const {
+    float f = 0.f;
+    if (r_) yv_get_fov(r_, &f);
+    return f;
+  }
   const Color32* RenderFrame() override {
     if (!r_ || !scene_ || !scene_->Handle()) {
       status_ = r_ ? YV_ERR_NO_SCENE : status_;

@@ -371,6 +371,11 @@ yv_status yv_set_fov(yv_renderer* r, float fov_deg) {
   r->fov = fov_deg;
   return YV_OK;
 }
+yv_status yv_get_fov(const yv_renderer* r, float* fov_deg) {
+  if (!r || !fov_deg) return YV_ERR_INVALID_ARG;
+  *fov_deg = r->fov;
+  return YV_OK;
+}
 yv_status yv_set_light(yv_renderer* r, const yv_light* light) {
   if (!r || !light || !finite3(light->dir)) return YV_ERR_INVALID_ARG;
   r->light = *light;

@@ -144,6 +144,7 @@ _SIGS = {
     "yv_set_resolution": (S, [P, I32, I32]),
     "yv_get_resolution": (S, [P, C.POINTER(I32), C.POINTER(I32)]),
     "yv_set_fov": (S, [P, C.c_float]),
+    "yv_get_fov": (S, [P, C.POINTER(C.c_float)]),
     "yv_set_detail_coef": (S, [P, C.c_float]),
     "yv_get_detail_coef": (S, [P, C.POINTER(C.c_float)]),
     "yv_set_light": (S, [P, C.POINTER(Light)]),

@@ -108,6 +108,11 @@ class Renderer:
         L.check(L.lib.yv_set_fov(self._h, float(fov)), "SetFOV")
         self._fov = float(np.float32(fov))
 
+    def GetFOV(self):
+        f = C.c_float()
+        L.check(L.lib.yv_get_fov(self._h, C.byref(f)), "GetFOV")
+        return f.value
+
     def SetDetailCoef(self, coef):
         """SVORenderer::SetDetailCoef: level-of-detail cut-off (0 = exact
         leaves; needs a scene with level-of-detail data)."""
@@ -302,6 +307,14 @@ class CudaRenderer:
         torch = _torch()
         self._r.SetViewPos(eyePos)
         self._r.SetViewDir(viewDir)
+        # trace_cuda.py:93 passes radians(1) / detailCoef as the cut-off
+        # angle; as the renderer's coefficient of radians(fov / 2) / width:
+        import math
+        if self.detailCoef > 0:
+            self._r.SetDetailCoef(math.radians(1.0) / self.detailCoef * self.resx /
+                                  math.radians(self._r.GetFOV() / 2))
+        else:
+            self._r.SetDetailCoef(0.0)
         if self._img is None:
             self._img = torch.empty((self.resy, self.resx), dtype=torch.int32, device="cuda")
         t0 = time.perf_counter()
