@@ -69,25 +69,29 @@ __device__ __forceinline__ float dens_clamped(const Grid& g, int x, int y, int z
 
 // Pass 1a: solid bits, one 32-voxel run of a row per warp and word (lane i
 // tests x = 32 w + i, a ballot packs the run): S[(z G + y) WR + w],
-// WR = max(1, G / 32) words per row; bits beyond the grid are 0.  Four
-// words per iteration keep four coalesced 128-byte loads in flight.
+// WR = max(1, G / 32) words per row (a power of two, as is G); bits beyond
+// the grid are 0.  Eight words per iteration keep eight coalesced 128-byte
+// loads in flight; word indices fit 32 bits (G^2 WR <= 2^28) and are split
+// with shifts.
 __global__ void solid_bits_kernel(Grid g, uint32_t WR, uint32_t* S) {
+  constexpr int kU = 8;
   const uint32_t lane = threadIdx.x & 31u;
-  const uint64_t total = (uint64_t)g.G * (uint64_t)g.G * WR;
-  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  for (uint64_t w0 = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; w0 < total;
-       w0 += 4 * nwarps) {
-    bool sol[4];
+  const int wsh = __ffs(WR) - 1;
+  const uint32_t total = (uint32_t)g.G * (uint32_t)g.G * WR;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w0 < total;
+       w0 += kU * nwarps) {
+    bool sol[kU];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const uint64_t wi = w0 + (uint64_t)u * nwarps;
-      const uint32_t x = (uint32_t)(wi % WR) * 32u + lane;
+    for (int u = 0; u < kU; ++u) {
+      const uint32_t wi = w0 + (uint32_t)u * nwarps;
+      const uint32_t x = ((wi & (WR - 1u)) << 5) + lane;
       sol[u] = wi < total && x < (uint32_t)g.G &&
-               __ldg(g.d + (wi / WR) * (uint64_t)g.G + x) > g.iso;
+               __ldg(g.d + (uint64_t)(wi >> wsh) * (uint64_t)g.G + x) > g.iso;
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const uint64_t wi = w0 + (uint64_t)u * nwarps;
+    for (int u = 0; u < kU; ++u) {
+      const uint32_t wi = w0 + (uint32_t)u * nwarps;
       const uint32_t m = __ballot_sync(0xFFFFFFFFu, sol[u]);
       if (lane == 0 && wi < total) S[wi] = m;
     }
@@ -99,15 +103,18 @@ __global__ void solid_bits_kernel(Grid g, uint32_t WR, uint32_t* S) {
 // solid and one of its 6 neighbours is not (bit shifts across the word and
 // its x neighbours, the words of the adjacent rows; outside the grid = not
 // solid).  Writes the class and the 2-bit voxel codes of the (up to) 16
-// regions the word covers.
+// regions the word covers, as one 16-byte and two 16-byte vector stores when
+// the word covers 16 regions.  Indices are split with shifts (WR and n are
+// powers of two).
 __global__ void classify_bits_kernel(const uint32_t* S, int G, uint32_t WR, uint32_t n,
                                      uint8_t* cls, uint16_t* codes) {
   const uint64_t total = (uint64_t)WR * n * n;
   const int nreg = n < 16u ? (int)n : 16;
+  const int wsh = __ffs(WR) - 1, nsh = __ffs(n) - 1;
   for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
        t += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t w = (uint32_t)(t % WR);
-    const uint32_t ry = (uint32_t)((t / WR) % n), rz = (uint32_t)(t / ((uint64_t)WR * n));
+    const uint32_t w = (uint32_t)(t & (WR - 1u));
+    const uint32_t ry = (uint32_t)((t >> wsh) & (n - 1u)), rz = (uint32_t)(t >> (wsh + nsh));
     uint32_t sol[2][2], surf[2][2];
 #pragma unroll
     for (int dz = 0; dz < 2; ++dz)
@@ -125,8 +132,10 @@ __global__ void classify_bits_kernel(const uint32_t* S, int G, uint32_t WR, uint
         sol[dz][dy] = W;
         surf[dz][dy] = W & ~(wl & wr & ym & yp & zm & zp);
       }
-    const uint64_t rbase = (uint64_t)16 * w + (uint64_t)n * (ry + (uint64_t)n * rz);
-    for (int k = 0; k < nreg; ++k) {
+    const uint64_t rbase = (uint64_t)16 * w + ((uint64_t)(ry + ((uint64_t)rz << nsh)) << nsh);
+    uint32_t cw[4] = {0u, 0u, 0u, 0u}, kw[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
       uint32_t code = 0;
       int n_empty = 0, n_full = 0;
 #pragma unroll
@@ -139,37 +148,49 @@ __global__ void classify_bits_kernel(const uint32_t* S, int G, uint32_t WR, uint
         n_full += so && !su;
         code |= c << (2 * ch);
       }
-      cls[rbase + k] = n_empty == 8 ? kClsEmpty : (n_full == 8 ? kClsFull : kClsNode);
-      codes[rbase + k] = (uint16_t)code;
+      const uint32_t cl = n_empty == 8 ? kClsEmpty : (n_full == 8 ? kClsFull : kClsNode);
+      cw[k >> 2] |= cl << (8 * (k & 3));
+      kw[k >> 1] |= code << (16 * (k & 1));
+    }
+    if (nreg == 16) {
+      // rbase is a multiple of 16: 16-byte aligned classes, 32-byte aligned codes
+      reinterpret_cast<uint4*>(cls + rbase)[0] = make_uint4(cw[0], cw[1], cw[2], cw[3]);
+      uint4* cp = reinterpret_cast<uint4*>(codes + rbase);
+      cp[0] = make_uint4(kw[0], kw[1], kw[2], kw[3]);
+      cp[1] = make_uint4(kw[4], kw[5], kw[6], kw[7]);
+    } else {
+      for (int k = 0; k < nreg; ++k) {
+        cls[rbase + k] = (uint8_t)(cw[k >> 2] >> (8 * (k & 3)));
+        codes[rbase + k] = (uint16_t)(kw[k >> 1] >> (16 * (k & 1)));
+      }
     }
   }
 }
 
 // Pass 2: class of each region of level k (n per axis) from its 8 children
 // at level k+1 (2n per axis).
+// Index of child ch of region r of a level with n = 2^s regions per axis,
+// in the level below (2n per axis).
+__device__ __forceinline__ uint64_t child_region(uint64_t r, uint32_t n, int ch) {
+  const int s = __ffs(n) - 1;
+  const uint64_t rx = r & (n - 1u), ry = (r >> s) & (n - 1u), rz = r >> (2 * s);
+  return (2 * rx + (ch & 1)) + ((2 * ry + ((ch >> 1) & 1)) << (s + 1)) +
+         ((2 * rz + (ch >> 2)) << (2 * s + 2));
+}
+
 __global__ void fold_level_kernel(const uint8_t* child, uint32_t n, uint8_t* cls) {
   const uint64_t total = (uint64_t)n * n * n;
-  const uint64_t m = 2ull * n;
   for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < total;
        r += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t rx = r % n, ry = (r / n) % n, rz = r / ((uint64_t)n * n);
     int n_empty = 0, n_full = 0;
 #pragma unroll
     for (int ch = 0; ch < 8; ++ch) {
-      const uint64_t c = (2 * rx + (ch & 1)) + m * ((2 * ry + ((ch >> 1) & 1)) +
-                                                    m * (2 * rz + (ch >> 2)));
-      const uint8_t k = child[c];
+      const uint8_t k = child[child_region(r, n, ch)];
       n_empty += k == kClsEmpty;
       n_full += k == kClsFull;
     }
     cls[r] = n_empty == 8 ? kClsEmpty : (n_full == 8 ? kClsFull : kClsNode);
   }
-}
-
-__device__ __forceinline__ uint64_t child_region(uint64_t r, uint32_t n, int ch) {
-  const uint64_t m = 2ull * n;
-  const uint64_t rx = r % n, ry = (r / n) % n, rz = r / ((uint64_t)n * n);
-  return (2 * rx + (ch & 1)) + m * ((2 * ry + ((ch >> 1) & 1)) + m * (2 * rz + (ch >> 2)));
 }
 
 // Mask of node children (level < bottom) or leaf children (bottom level).
@@ -253,7 +274,9 @@ __global__ void emit_bottom_kernel(Grid g, const uint64_t* list, uint32_t m, con
                                    yv_vox_node* out, yv_leaf_attr* attrs) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
     const uint64_t r = list[i];
-    const int rx = (int)(r % n), ry = (int)((r / n) % n), rz = (int)(r / ((uint64_t)n * n));
+    const int sh = __ffs(n) - 1;
+    const int rx = (int)(r & (n - 1u)), ry = (int)((r >> sh) & (n - 1u)),
+              rz = (int)(r >> (2 * sh));
     const uint32_t code = codes[r];
     yv_vox_node v;
     v.flags = 0;
