@@ -98,6 +98,43 @@ __global__ void solid_bits_kernel(Grid g, uint32_t WR, uint32_t* S) {
   }
 }
 
+// Pass 1a for rows of 128 voxels or more (G >= 128): one 128-voxel chunk
+// per warp and iteration, each lane a 16-byte load of 4 voxels; the lanes'
+// 4-bit groups are ORed into 32-bit words within groups of 8 lanes (3
+// shuffles), lane 8j writing word j of the chunk.  Same bits as above.
+__global__ void solid_bits_v4_kernel(Grid g, uint32_t WR, uint32_t* S) {
+  constexpr int kU = 4;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t CR = WR >> 2;  // chunks per row
+  const int csh = __ffs(CR) - 1;
+  const uint32_t total = (uint32_t)g.G * CR * (uint32_t)g.G;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const float4* d4 = reinterpret_cast<const float4*>(g.d);
+  for (uint32_t c0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c0 < total;
+       c0 += kU * nwarps) {
+    float4 v[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const uint32_t c = c0 + (uint32_t)u * nwarps;
+      v[u] = c < total ? __ldg(d4 + (((uint64_t)(c >> csh) * g.G + ((c & (CR - 1u)) << 7)) >> 2) +
+                               lane)
+                       : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const uint32_t c = c0 + (uint32_t)u * nwarps;
+      const uint32_t nib = (uint32_t)(v[u].x > g.iso) | ((uint32_t)(v[u].y > g.iso) << 1) |
+                           ((uint32_t)(v[u].z > g.iso) << 2) | ((uint32_t)(v[u].w > g.iso) << 3);
+      uint32_t word = nib << (4 * (lane & 7u));
+      word |= __shfl_xor_sync(0xFFFFFFFFu, word, 1);
+      word |= __shfl_xor_sync(0xFFFFFFFFu, word, 2);
+      word |= __shfl_xor_sync(0xFFFFFFFFu, word, 4);
+      if ((lane & 7u) == 0u && c < total)
+        S[((uint64_t)(c >> csh) * WR) + ((c & (CR - 1u)) << 2) + (lane >> 3)] = word;
+    }
+  }
+}
+
 // Pass 1b: bottom regions (2^3 voxels) from the bits.  One thread per word
 // and pair of rows in y and in z: a voxel is a surface voxel when it is
 // solid and one of its 6 neighbours is not (bit shifts across the word and
@@ -133,24 +170,22 @@ __global__ void classify_bits_kernel(const uint32_t* S, int G, uint32_t WR, uint
         surf[dz][dy] = W & ~(wl & wr & ym & yp & zm & zp);
       }
     const uint64_t rbase = (uint64_t)16 * w + ((uint64_t)(ry + ((uint64_t)rz << nsh)) << nsh);
+    // Region k holds bits 2k, 2k+1 of the four rows.  Bit-parallel over the
+    // 16 regions: bit 2k of `any` = some voxel solid, of `all_full` = all 8
+    // solid and not surface; only the other (node) regions need per-voxel
+    // codes (empty regions code 0, full ones 0x5555).
+    const uint32_t so_or = sol[0][0] | sol[0][1] | sol[1][0] | sol[1][1];
+    const uint32_t fu_and = (sol[0][0] & ~surf[0][0]) & (sol[0][1] & ~surf[0][1]) &
+                            (sol[1][0] & ~surf[1][0]) & (sol[1][1] & ~surf[1][1]);
+    const uint32_t any = (so_or | (so_or >> 1)) & 0x55555555u;
+    const uint32_t all_full = fu_and & (fu_and >> 1) & 0x55555555u;
     uint32_t cw[4] = {0u, 0u, 0u, 0u}, kw[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
-      uint32_t code = 0;
-      int n_empty = 0, n_full = 0;
-#pragma unroll
-      for (int ch = 0; ch < 8; ++ch) {
-        const int bit = 2 * k + (ch & 1);
-        const uint32_t so = (sol[ch >> 2][(ch >> 1) & 1] >> bit) & 1u;
-        const uint32_t su = (surf[ch >> 2][(ch >> 1) & 1] >> bit) & 1u;
-        const uint32_t c = !so ? kVoxEmpty : (su ? kVoxLeaf : kVoxFull);
-        n_empty += !so;
-        n_full += so && !su;
-        code |= c << (2 * ch);
-      }
-      const uint32_t cl = n_empty == 8 ? kClsEmpty : (n_full == 8 ? kClsFull : kClsNode);
+      const uint32_t b = 1u << (2 * k);
+      const uint32_t cl = !(any & b) ? kClsEmpty : ((all_full & b) ? kClsFull : kClsNode);
       cw[k >> 2] |= cl << (8 * (k & 3));
-      kw[k >> 1] |= code << (16 * (k & 1));
+      if (cl == kClsFull) kw[k >> 1] |= 0x5555u << (16 * (k & 1));
     }
     if (nreg == 16) {
       // rbase is a multiple of 16: 16-byte aligned classes, 32-byte aligned codes
@@ -159,16 +194,32 @@ __global__ void classify_bits_kernel(const uint32_t* S, int G, uint32_t WR, uint
       cp[0] = make_uint4(kw[0], kw[1], kw[2], kw[3]);
       cp[1] = make_uint4(kw[4], kw[5], kw[6], kw[7]);
     } else {
-      for (int k = 0; k < nreg; ++k) {
+#pragma unroll
+      for (int k = 0; k < 16; ++k) {
+        if (k >= nreg) break;
         cls[rbase + k] = (uint8_t)(cw[k >> 2] >> (8 * (k & 3)));
         codes[rbase + k] = (uint16_t)(kw[k >> 1] >> (16 * (k & 1)));
       }
     }
+    // per-voxel codes of the node regions (few), over the zeros just stored
+    uint32_t nodes_mask = any & ~all_full;
+    while (nodes_mask) {
+      const int k = (__ffs(nodes_mask) - 1) >> 1;
+      nodes_mask &= nodes_mask - 1u;
+      uint32_t code = 0;
+#pragma unroll
+      for (int ch = 0; ch < 8; ++ch) {
+        const int bit = 2 * k + (ch & 1);
+        const uint32_t so = (sol[ch >> 2][(ch >> 1) & 1] >> bit) & 1u;
+        const uint32_t su = (surf[ch >> 2][(ch >> 1) & 1] >> bit) & 1u;
+        const uint32_t c = !so ? kVoxEmpty : (su ? kVoxLeaf : kVoxFull);
+        code |= c << (2 * ch);
+      }
+      codes[rbase + k] = (uint16_t)code;
+    }
   }
 }
 
-// Pass 2: class of each region of level k (n per axis) from its 8 children
-// at level k+1 (2n per axis).
 // Index of child ch of region r of a level with n = 2^s regions per axis,
 // in the level below (2n per axis).
 __device__ __forceinline__ uint64_t child_region(uint64_t r, uint32_t n, int ch) {
@@ -178,6 +229,8 @@ __device__ __forceinline__ uint64_t child_region(uint64_t r, uint32_t n, int ch)
          ((2 * rz + (ch >> 2)) << (2 * s + 2));
 }
 
+// Pass 2: class of each region of level k (n per axis) from its 8 children
+// at level k+1 (2n per axis).
 __global__ void fold_level_kernel(const uint8_t* child, uint32_t n, uint8_t* cls) {
   const uint64_t total = (uint64_t)n * n * n;
   for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < total;
@@ -268,59 +321,80 @@ __device__ __forceinline__ int8_t quant_n(float v) {
   return (int8_t)(int)q;
 }
 
-// Pass 4b: bottom-level VoxNodes and their leaf attributes.
-__global__ void emit_bottom_kernel(Grid g, const uint64_t* list, uint32_t m, const uint16_t* codes,
-                                   uint32_t n, const uint32_t* offsets, uint32_t node_base,
-                                   yv_vox_node* out, yv_leaf_attr* attrs) {
+// Pass 4b: bottom-level VoxNodes (leaf indices from the scanned offsets).
+__global__ void emit_bottom_kernel(const uint64_t* list, uint32_t m, const uint16_t* codes,
+                                   const uint32_t* offsets, uint32_t node_base,
+                                   yv_vox_node* out) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
-    const uint64_t r = list[i];
-    const int sh = __ffs(n) - 1;
-    const int rx = (int)(r & (n - 1u)), ry = (int)((r >> sh) & (n - 1u)),
-              rz = (int)(r >> (2 * sh));
-    const uint32_t code = codes[r];
+    const uint32_t code = codes[list[i]];
     yv_vox_node v;
     v.flags = 0;
     v.data = 0;
     uint32_t next = offsets[i];
+#pragma unroll
     for (int ch = 0; ch < 8; ++ch) {
       const uint32_t c = (code >> (2 * ch)) & 3u;
       if (c != kVoxLeaf) {
         v.child[ch] = null_word(c == kVoxFull);
         v.flags |= 1u << (8 + ch);
-        continue;
-      }
-      const int x = 2 * rx + (ch & 1), y = 2 * ry + ((ch >> 1) & 1), z = 2 * rz + (ch >> 2);
-      yv_leaf_attr a;
-      if (g.rgb) {
-        const size_t o = 3 * vidx(g.G, x, y, z);
-        a.r = g.rgb[o];
-        a.g = g.rgb[o + 1];
-        a.b = g.rgb[o + 2];
       } else {
-        a.r = a.g = a.b = 255;
+        v.child[ch] = next++;
+        v.flags |= 1u << ch;
       }
-      a.a = 255;
-      const float fx = __fsub_rn(dens_clamped(g, x - 1, y, z), dens_clamped(g, x + 1, y, z));
-      const float fy = __fsub_rn(dens_clamped(g, x, y - 1, z), dens_clamped(g, x, y + 1, z));
-      const float fz = __fsub_rn(dens_clamped(g, x, y, z - 1), dens_clamped(g, x, y, z + 1));
-      const float len2 =
-          __fadd_rn(__fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy)), __fmul_rn(fz, fz));
-      float nx = 0.f, ny = 0.f, nz = 0.f;
-      if (len2 > 0.f && len2 <= 3.402823466e38f) {
-        const float len = __fsqrt_rn(len2);
-        nx = __fdiv_rn(fx, len);
-        ny = __fdiv_rn(fy, len);
-        nz = __fdiv_rn(fz, len);
-      }
-      a.nx = quant_n(nx);
-      a.ny = quant_n(ny);
-      a.nz = quant_n(nz);
-      a.nw = 0;
-      attrs[next] = a;
-      v.child[ch] = next++;
-      v.flags |= 1u << ch;
     }
     out[node_base + i] = v;
+  }
+}
+
+// Pass 4c: leaf attributes, one thread per (bottom node, child): the 8
+// lanes of a node handle neighbouring voxels, so the six density loads of
+// the central differences of a warp's leaves share sectors.
+__global__ void emit_leaves_kernel(Grid g, const uint64_t* list, uint32_t m,
+                                   const uint16_t* codes, uint32_t n, const uint32_t* offsets,
+                                   yv_leaf_attr* attrs) {
+  const uint64_t total = 8ull * m;
+  const int sh = __ffs(n) - 1;
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t i = (uint32_t)(t >> 3);
+    const int ch = (int)(t & 7u);
+    const uint64_t r = list[i];
+    const uint32_t code = codes[r];
+    if (((code >> (2 * ch)) & 3u) != kVoxLeaf) continue;
+    uint32_t before = 0;  // leaf children before ch
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      before += (q < ch && ((code >> (2 * q)) & 3u) == kVoxLeaf) ? 1u : 0u;
+    const int rx = (int)(r & (n - 1u)), ry = (int)((r >> sh) & (n - 1u)),
+              rz = (int)(r >> (2 * sh));
+    const int x = 2 * rx + (ch & 1), y = 2 * ry + ((ch >> 1) & 1), z = 2 * rz + (ch >> 2);
+    yv_leaf_attr a;
+    if (g.rgb) {
+      const size_t o = 3 * vidx(g.G, x, y, z);
+      a.r = g.rgb[o];
+      a.g = g.rgb[o + 1];
+      a.b = g.rgb[o + 2];
+    } else {
+      a.r = a.g = a.b = 255;
+    }
+    a.a = 255;
+    const float fx = __fsub_rn(dens_clamped(g, x - 1, y, z), dens_clamped(g, x + 1, y, z));
+    const float fy = __fsub_rn(dens_clamped(g, x, y - 1, z), dens_clamped(g, x, y + 1, z));
+    const float fz = __fsub_rn(dens_clamped(g, x, y, z - 1), dens_clamped(g, x, y, z + 1));
+    const float len2 =
+        __fadd_rn(__fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy)), __fmul_rn(fz, fz));
+    float nx = 0.f, ny = 0.f, nz = 0.f;
+    if (len2 > 0.f && len2 <= 3.402823466e38f) {
+      const float len = __fsqrt_rn(len2);
+      nx = __fdiv_rn(fx, len);
+      ny = __fdiv_rn(fy, len);
+      nz = __fdiv_rn(fz, len);
+    }
+    a.nx = quant_n(nx);
+    a.ny = quant_n(ny);
+    a.nz = quant_n(nz);
+    a.nw = 0;
+    attrs[offsets[i] + before] = a;
   }
 }
 
@@ -393,8 +467,12 @@ yv_status build_dense(const float* density, const uint8_t* rgb, int depth, float
   if ((e = codes.alloc(nb3 * 2, s)) != cudaSuccess ||
       (e = bits.alloc((uint64_t)G * G * WR * 4, s)) != cudaSuccess)
     return build_fail(e, "alloc");
-  solid_bits_kernel<<<grid_for((uint64_t)G * G * WR * 32 / 4), 256, 0, s>>>(
-      g, WR, bits.as<uint32_t>());
+  if (G >= 128)
+    solid_bits_v4_kernel<<<grid_for((uint64_t)G * G * WR * 8), 256, 0, s>>>(
+        g, WR, bits.as<uint32_t>());
+  else
+    solid_bits_kernel<<<grid_for((uint64_t)G * G * WR * 32 / 4), 256, 0, s>>>(
+        g, WR, bits.as<uint32_t>());
   classify_bits_kernel<<<grid_for((uint64_t)WR * nb * nb), 256, 0, s>>>(
       bits.as<uint32_t>(), G, WR, nb, cls[(size_t)depth - 1].as<uint8_t>(), codes.as<uint16_t>());
   for (int k = depth - 2; k >= 0; --k) {
@@ -468,9 +546,12 @@ yv_status build_dense(const float* density, const uint8_t* rgb, int depth, float
         res.nodes.as<yv_vox_node>());
   const int kb = depth - 1;
   emit_bottom_kernel<<<grid_for(m[(size_t)kb]), 256, 0, s>>>(
-      g, list[(size_t)kb].as<uint64_t>(), m[(size_t)kb], codes.as<uint16_t>(), 1u << kb,
-      offs[(size_t)kb].as<uint32_t>(), base[(size_t)kb], res.nodes.as<yv_vox_node>(),
-      res.attrs.as<yv_leaf_attr>());
+      list[(size_t)kb].as<uint64_t>(), m[(size_t)kb], codes.as<uint16_t>(),
+      offs[(size_t)kb].as<uint32_t>(), base[(size_t)kb], res.nodes.as<yv_vox_node>());
+  if (res.na)
+    emit_leaves_kernel<<<grid_for(8ull * m[(size_t)kb]), 256, 0, s>>>(
+        g, list[(size_t)kb].as<uint64_t>(), m[(size_t)kb], codes.as<uint16_t>(), 1u << kb,
+        offs[(size_t)kb].as<uint32_t>(), res.attrs.as<yv_leaf_attr>());
   if ((e = cudaGetLastError()) != cudaSuccess) return build_fail(e, "emit");
   return YV_OK;
 }
