@@ -76,11 +76,12 @@ int grid_for(uint64_t work) {
   return (int)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 
-// out[i] = sum of in[0..i), *total = sum of all.
+// out[i] = sum of in[0..i); *total = sum of all (read back with a stream
+// sync), or total = NULL when the caller knows it (no sync).
 cudaError_t exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32_t* total,
                            cudaStream_t s) {
   if (n == 0) {
-    *total = 0;
+    if (total) *total = 0;
     return cudaSuccess;
   }
   const uint32_t blocks = (n + kScanBlock - 1) / kScanBlock;
@@ -97,6 +98,7 @@ cudaError_t exclusive_scan(const uint32_t* in, uint32_t* out, uint32_t n, uint32
     return cudaGetLastError();
   }
   // one block: its sum is the total
+  if (!total) return cudaSuccess;
   e = cudaMemcpyAsync(total, sums.as<uint32_t>(), 4, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   return e;

@@ -143,8 +143,12 @@ __global__ void solid_bits_v4_kernel(Grid g, uint32_t WR, uint32_t* S) {
 // regions the word covers, as one 16-byte and two 16-byte vector stores when
 // the word covers 16 regions.  Indices are split with shifts (WR and n are
 // powers of two).
+// node_count / leaf_count (either may be null): node regions and leaf
+// (surface) voxels, added with one atomic per warp.
 __global__ void classify_bits_kernel(const uint32_t* S, int G, uint32_t WR, uint32_t n,
-                                     uint8_t* cls, uint16_t* codes) {
+                                     uint8_t* cls, uint16_t* codes, uint32_t* node_count,
+                                     uint32_t* leaf_count) {
+  uint32_t my_nodes = 0, my_leaves = 0;
   const uint64_t total = (uint64_t)WR * n * n;
   const int nreg = n < 16u ? (int)n : 16;
   const int wsh = __ffs(WR) - 1, nsh = __ffs(n) - 1;
@@ -203,6 +207,9 @@ __global__ void classify_bits_kernel(const uint32_t* S, int G, uint32_t WR, uint
     }
     // per-voxel codes of the node regions (few), over the zeros just stored
     uint32_t nodes_mask = any & ~all_full;
+    my_nodes += __popc(nodes_mask);
+    my_leaves += __popc(surf[0][0]) + __popc(surf[0][1]) + __popc(surf[1][0]) +
+                 __popc(surf[1][1]);
     while (nodes_mask) {
       const int k = (__ffs(nodes_mask) - 1) >> 1;
       nodes_mask &= nodes_mask - 1u;
@@ -218,6 +225,12 @@ __global__ void classify_bits_kernel(const uint32_t* S, int G, uint32_t WR, uint
       codes[rbase + k] = (uint16_t)code;
     }
   }
+  my_nodes = __reduce_add_sync(0xFFFFFFFFu, my_nodes);
+  my_leaves = __reduce_add_sync(0xFFFFFFFFu, my_leaves);
+  if ((threadIdx.x & 31u) == 0) {
+    if (node_count && my_nodes) atomicAdd(node_count, my_nodes);
+    if (leaf_count && my_leaves) atomicAdd(leaf_count, my_leaves);
+  }
 }
 
 // Index of child ch of region r of a level with n = 2^s regions per axis,
@@ -231,8 +244,11 @@ __device__ __forceinline__ uint64_t child_region(uint64_t r, uint32_t n, int ch)
 
 // Pass 2: class of each region of level k (n per axis) from its 8 children
 // at level k+1 (2n per axis).
-__global__ void fold_level_kernel(const uint8_t* child, uint32_t n, uint8_t* cls) {
+// count (may be null): node regions of the level, one atomic per warp.
+__global__ void fold_level_kernel(const uint8_t* child, uint32_t n, uint8_t* cls,
+                                  uint32_t* count) {
   const uint64_t total = (uint64_t)n * n * n;
+  uint32_t my_nodes = 0;
   for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < total;
        r += (uint64_t)gridDim.x * blockDim.x) {
     int n_empty = 0, n_full = 0;
@@ -242,8 +258,12 @@ __global__ void fold_level_kernel(const uint8_t* child, uint32_t n, uint8_t* cls
       n_empty += k == kClsEmpty;
       n_full += k == kClsFull;
     }
-    cls[r] = n_empty == 8 ? kClsEmpty : (n_full == 8 ? kClsFull : kClsNode);
+    const uint8_t c = n_empty == 8 ? kClsEmpty : (n_full == 8 ? kClsFull : kClsNode);
+    cls[r] = c;
+    my_nodes += c == kClsNode;
   }
+  my_nodes = __reduce_add_sync(0xFFFFFFFFu, my_nodes);
+  if (count && (threadIdx.x & 31u) == 0 && my_nodes) atomicAdd(count, my_nodes);
 }
 
 // Mask of node children (level < bottom) or leaf children (bottom level).
@@ -467,6 +487,13 @@ yv_status build_dense(const float* density, const uint8_t* rgb, int depth, float
   if ((e = codes.alloc(nb3 * 2, s)) != cudaSuccess ||
       (e = bits.alloc((uint64_t)G * G * WR * 4, s)) != cudaSuccess)
     return build_fail(e, "alloc");
+  // level sizes, counted by the classify and fold passes: hc[0] = root
+  // class, hc[k] = node regions of level k (k >= 1), hc[depth] = leaves
+  DevBuf dc;
+  if ((e = dc.alloc((size_t)(depth + 1) * 4, s)) != cudaSuccess ||
+      (e = cudaMemsetAsync(dc.p, 0, (size_t)(depth + 1) * 4, s)) != cudaSuccess)
+    return build_fail(e, "alloc");
+  uint32_t* dcp = dc.as<uint32_t>();
   if (G >= 128)
     solid_bits_v4_kernel<<<grid_for((uint64_t)G * G * WR * 8), 256, 0, s>>>(
         g, WR, bits.as<uint32_t>());
@@ -474,29 +501,45 @@ yv_status build_dense(const float* density, const uint8_t* rgb, int depth, float
     solid_bits_kernel<<<grid_for((uint64_t)G * G * WR * 32 / 4), 256, 0, s>>>(
         g, WR, bits.as<uint32_t>());
   classify_bits_kernel<<<grid_for((uint64_t)WR * nb * nb), 256, 0, s>>>(
-      bits.as<uint32_t>(), G, WR, nb, cls[(size_t)depth - 1].as<uint8_t>(), codes.as<uint16_t>());
+      bits.as<uint32_t>(), G, WR, nb, cls[(size_t)depth - 1].as<uint8_t>(), codes.as<uint16_t>(),
+      depth > 1 ? dcp + depth - 1 : nullptr, dcp + depth);
   for (int k = depth - 2; k >= 0; --k) {
     const uint32_t n = 1u << k;
     fold_level_kernel<<<grid_for((uint64_t)n * n * n), 256, 0, s>>>(
-        cls[(size_t)k + 1].as<uint8_t>(), n, cls[(size_t)k].as<uint8_t>());
+        cls[(size_t)k + 1].as<uint8_t>(), n, cls[(size_t)k].as<uint8_t>(),
+        k > 0 ? dcp + k : nullptr);
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return build_fail(e, "classify");
-  uint8_t root_cls = 0;
-  if ((e = cudaMemcpyAsync(&root_cls, cls[0].as<uint8_t>(), 1, cudaMemcpyDeviceToHost, s)) !=
-          cudaSuccess ||
+  // read back with one sync (the root class byte into hc[0])
+  if ((e = cudaMemcpyAsync(dc.p, cls[0].p, 1, cudaMemcpyDeviceToDevice, s)) != cudaSuccess)
+    return build_fail(e, "level sizes");
+  std::vector<uint32_t> hc((size_t)depth + 1, 0);
+  if ((e = cudaGetLastError()) != cudaSuccess ||
+      (e = cudaMemcpyAsync(hc.data(), dc.p, (size_t)(depth + 1) * 4, cudaMemcpyDeviceToHost,
+                           s)) != cudaSuccess ||
       (e = cudaStreamSynchronize(s)) != cudaSuccess)
-    return build_fail(e, "root class");
+    return build_fail(e, "level sizes");
+  const uint8_t root_cls = (uint8_t)(hc[0] & 0xFFu);
   if (root_cls != kClsNode) {
     res.root = root_cls == kClsFull ? YV_FULL_NODE : YV_EMPTY_NODE;
     return YV_OK;
   }
-  // breadth-first lists, level by level
+  // breadth-first lists, level by level, with no host round trip: the
+  // scanned totals are the level sizes counted above
   std::vector<DevBuf> list((size_t)depth), offs((size_t)depth);
   std::vector<uint32_t> m((size_t)depth, 0), base((size_t)depth + 1, 0);
+  m[0] = 1;
+  for (int k = 1; k < depth; ++k) m[(size_t)k] = hc[(size_t)k];
+  for (int k = 0; k < depth; ++k) {
+    base[(size_t)k + 1] = base[(size_t)k] + m[(size_t)k];
+    if ((uint64_t)base[(size_t)k] + m[(size_t)k] > YV_MAX_DEVICE_NODES) {
+      set_last_error("dense SVO build: more than 2^29 nodes");
+      return YV_ERR_UNSUPPORTED;
+    }
+  }
+  const uint32_t n_attrs = hc[(size_t)depth];
   if ((e = list[0].alloc(8, s)) != cudaSuccess) return build_fail(e, "alloc");
   if ((e = cudaMemsetAsync(list[0].p, 0, 8, s)) != cudaSuccess) return build_fail(e, "list");
-  m[0] = 1;
-  uint32_t n_attrs = 0;
   for (int k = 0; k < depth; ++k) {
     const bool bottom = k == depth - 1;
     const uint32_t n = 1u << k;
@@ -504,29 +547,17 @@ yv_status build_dense(const float* density, const uint8_t* rgb, int depth, float
     if ((e = counts.alloc((size_t)m[(size_t)k] * 4, s)) != cudaSuccess ||
         (e = offs[(size_t)k].alloc((size_t)m[(size_t)k] * 4, s)) != cudaSuccess)
       return build_fail(e, "alloc");
-    // (a node region holds a surface voxel, so every level below the root
-    // has nodes; an empty list would only skip its kernels)
     if (m[(size_t)k])
       count_kernel<<<grid_for(m[(size_t)k]), 256, 0, s>>>(
         list[(size_t)k].as<uint64_t>(), m[(size_t)k],
         bottom ? nullptr : cls[(size_t)k + 1].as<uint8_t>(), bottom ? codes.as<uint16_t>() : nullptr,
         n, counts.as<uint32_t>());
-    uint32_t total = 0;
     if ((e = cudaGetLastError()) != cudaSuccess ||
         (e = exclusive_scan(counts.as<uint32_t>(), offs[(size_t)k].as<uint32_t>(), m[(size_t)k],
-                            &total, s)) != cudaSuccess)
+                            nullptr, s)) != cudaSuccess)
       return build_fail(e, "scan");
-    base[(size_t)k + 1] = base[(size_t)k] + m[(size_t)k];
-    if ((uint64_t)base[(size_t)k + 1] > YV_MAX_DEVICE_NODES) {
-      set_last_error("dense SVO build: more than 2^29 nodes");
-      return YV_ERR_UNSUPPORTED;
-    }
-    if (bottom) {
-      n_attrs = total;
-      break;
-    }
-    m[(size_t)k + 1] = total;
-    if ((e = list[(size_t)k + 1].alloc((size_t)total * 8, s)) != cudaSuccess)
+    if (bottom) break;
+    if ((e = list[(size_t)k + 1].alloc((size_t)m[(size_t)k + 1] * 8, s)) != cudaSuccess)
       return build_fail(e, "alloc");
     expand_kernel<<<grid_for(m[(size_t)k]), 256, 0, s>>>(
         list[(size_t)k].as<uint64_t>(), m[(size_t)k], cls[(size_t)k + 1].as<uint8_t>(), n,
