@@ -83,7 +83,8 @@ CONFIGS = {
     "vbuild": dict(kind="vbuild", levels=3, precision=3, seed=1234,
                    workload="GPU brick-volume build from a dense 513^3 float32 lattice (4 "
                             "seeded sinusoid products - 0.4, clamped to [0, 1]): mark, N=4 tree, "
-                            "pack into the 8-byte fp16+RGB8 device pool"),
+                            "pack into the 8-byte fp16+RGB8 device pool, rebuilt in place every "
+                            "step (BrickPool::Update)"),
     "dynsync": dict(kind="dynsync", depth=8, edits=1000, seed=1234,
                     workload="editable SVO (200 seeded spheres in 256^3): 1000 random voxel "
                              "edits per step, then a sync of the changed 256-node pages into "
@@ -890,12 +891,11 @@ def run_vbuild(args, cfg):
     n = 8 * 4 ** levels + 1
     lat = wave_lattice(torch, n, cfg["seed"], "cuda")
     torch.cuda.synchronize()
-    keep = []
+    # BrickPool::Update: the pool is rebuilt in place every step
+    vol = yoxel.VolumeGPU.from_dense(lat, levels, cfg["precision"])
 
     def fn():
-        keep.append(yoxel.VolumeGPU.from_dense(lat, levels, cfg["precision"]))
-        if len(keep) > 1:
-            keep.pop(0)
+        vol.rebuild_dense(lat, levels)
 
     for _ in range(args.warmup):
         fn()

@@ -355,6 +355,13 @@ void      yv_volume_gpu_free(yv_volume_gpu* g);
 yv_status yv_volume_upload_dense(const float* density, const uint8_t* rgb,
                                  int32_t levels, int32_t precision, void* stream,
                                  yv_volume_gpu** out);
+/* BrickPool::Update in place: rebuilds `vol` (same precision) from a new
+ * lattice on `stream`, reusing its device arrays when they are large enough
+ * (growing them otherwise).  Work already queued that reads `vol` must be
+ * ordered before this call by the caller (same stream, or a sync). */
+yv_status yv_volume_rebuild_dense(yv_volume_gpu* vol, const float* density,
+                                  const uint8_t* rgb, int32_t levels,
+                                  void* stream);
 yv_status yv_volume_gpu_desc(const yv_volume_gpu* g, yv_volume_device* out);
 
 /* Pinhole camera (RendererBase fields, cell/renderer_base.h:13-21). */

@@ -71,3 +71,25 @@ def test_gpu_volume_build_empty_lattice(yoxel_mod, levels):
     host = yoxel_mod.BrickVolume.from_dense(levels, np.zeros((n, n, n), np.float32))
     g = yoxel_mod.BrickVolume.build_dense(torch.zeros((n, n, n), device="cuda"), levels)
     assert g.nbricks == 0 == host.nbricks and np.array_equal(g.grids, host.grids)
+
+
+@pytest.mark.parametrize("precision", [2, 3])
+def test_rebuild_in_place_renders_like_fresh_build(yoxel_mod, precision):
+    """BrickPool::Update: rebuilding a device pool in place from a new
+    lattice (smaller, then larger than the first) renders exactly like a
+    fresh build of that lattice."""
+    import torch
+    levels = 2
+    a = lattice(levels, 11, "blobs")
+    b = lattice(levels, 3, "specks")  # fewer bricks
+    c = lattice(levels, 12, "blobs")
+    cams = yoxel_mod.sphere_cameras(3)
+    vol = yoxel_mod.VolumeGPU.from_dense(torch.from_numpy(a).cuda(), levels, precision)
+    for nxt in (b, c, a):
+        t = torch.from_numpy(nxt).cuda()
+        vol.rebuild_dense(t, levels)
+        fresh = yoxel_mod.VolumeGPU.from_dense(t, levels, precision)
+        assert vol.desc().nbricks == fresh.desc().nbricks
+        x = yoxel_mod.render_volume(vol.desc(), cams, 40, 32)
+        y = yoxel_mod.render_volume(fresh.desc(), cams, 40, 32)
+        assert torch.equal(x.view(torch.int32), y.view(torch.int32))

@@ -20,6 +20,7 @@ struct yv_volume_gpu {
   int device = 0;
   yv_volume_device desc;
   void* mem[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  size_t cap[5] = {0, 0, 0, 0, 0};  // bytes allocated per array (reused by rebuilds)
 };
 
 namespace {
@@ -113,16 +114,28 @@ bool cams_ok(const yv_camera* c, int n) {
 
 namespace yv {
 
-yv_status volume_gpu_from_device(void* mem[5], const yv_volume_device& d, yv_volume_gpu** out) {
+yv_status volume_gpu_from_device(void* mem[5], const size_t bytes[5], const yv_volume_device& d,
+                                 yv_volume_gpu** out) {
   yv_volume_gpu* g = new (std::nothrow) yv_volume_gpu();
   if (!g) {
     for (int i = 0; i < 5; ++i) cudaFree(mem[i]);
     return YV_ERR_OUT_OF_MEMORY;
   }
   cudaGetDevice(&g->device);
-  for (int i = 0; i < 5; ++i) g->mem[i] = mem[i];
+  for (int i = 0; i < 5; ++i) {
+    g->mem[i] = mem[i];
+    g->cap[i] = mem[i] ? bytes[i] : 0;
+  }
   g->desc = d;
   *out = g;
+  return YV_OK;
+}
+
+yv_status volume_gpu_arrays(yv_volume_gpu* g, void*** mem, size_t** cap, yv_volume_device** d) {
+  if (!g) return YV_ERR_INVALID_ARG;
+  *mem = g->mem;
+  *cap = g->cap;
+  *d = &g->desc;
   return YV_OK;
 }
 
@@ -203,6 +216,7 @@ yv_status yv_volume_upload(const yv_volume_host* v, int32_t precision, yv_volume
   for (int i = 0; i < 5; ++i) {
     if (!bytes[i]) continue;
     cudaError_t e = cudaMalloc(&g->mem[i], bytes[i]);
+    if (e == cudaSuccess) g->cap[i] = bytes[i];
     if (e == cudaSuccess) e = cudaMemcpy(g->mem[i], src[i], bytes[i], cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
       yv_volume_gpu_free(g);

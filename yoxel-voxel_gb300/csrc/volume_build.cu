@@ -46,41 +46,52 @@ __device__ __forceinline__ uint64_t lat(const Lattice& g, int x, int y, int z) {
 }
 
 // Mark: one warp per brick cell, any nonzero value among its 9^3.
-__global__ void mark_cells_kernel(Lattice g, uint8_t* occ) {
+// Cell and level sizes are powers of two: index splits use shifts.
+// count: occupied cells, one atomic per warp.
+__global__ void mark_cells_kernel(Lattice g, uint8_t* occ, uint32_t* count) {
   const uint32_t lane = threadIdx.x & 31u;
+  const int nbs = __ffs(g.nb) - 1;
+  uint32_t my = 0;
   const uint64_t cells = (uint64_t)g.nb * g.nb * g.nb;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   for (uint64_t c = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; c < cells;
        c += nwarps) {
-    const int cx = (int)(c % g.nb), cy = (int)((c / g.nb) % g.nb),
-              cz = (int)(c / ((uint64_t)g.nb * g.nb));
+    const int cx = (int)(c & (uint64_t)(g.nb - 1)), cy = (int)((c >> nbs) & (uint64_t)(g.nb - 1)),
+              cz = (int)(c >> (2 * nbs));
     bool nz = false;
     for (int k = (int)lane; k < kVL3 && !nz; k += 32)
       nz = __ldg(g.d + lat(g, cx * kVB + k % kVL, cy * kVB + (k / kVL) % kVL,
                            cz * kVB + k / (kVL * kVL))) != 0.f;
     const uint32_t any = __ballot_sync(0xFFFFFFFFu, nz);
     if (lane == 0) occ[c] = any ? 1 : 0;
+    my += any ? 1u : 0u;
   }
+  if (lane == 0 && my) atomicAdd(count, my);
+}
+
+// Index of child c (x | y<<2 | z<<4) of node p of a level with n = 2^s
+// nodes per axis, in the level below (4n per axis).
+__device__ __forceinline__ uint64_t child64(uint64_t p, uint32_t n, int c) {
+  const int s = __ffs(n) - 1;
+  const uint64_t x = p & (n - 1u), y = (p >> s) & (n - 1u), z = p >> (2 * s);
+  return (4 * x + (c & 3)) + ((4 * y + ((c >> 2) & 3)) << (s + 2)) +
+         ((4 * z + (c >> 4)) << (2 * s + 4));
 }
 
 // Level l (n per axis) from level l+1 (4n per axis): OR of 64 children.
-__global__ void fold64_kernel(const uint8_t* child, uint32_t n, uint8_t* out) {
+// count: occupied nodes of the level, one atomic per warp.
+__global__ void fold64_kernel(const uint8_t* child, uint32_t n, uint8_t* out, uint32_t* count) {
   const uint64_t total = (uint64_t)n * n * n;
-  const uint64_t m = 4ull * n;
+  uint32_t my = 0;
   for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < total;
        p += (uint64_t)gridDim.x * blockDim.x) {
-    const uint64_t x = p % n, y = (p / n) % n, z = p / ((uint64_t)n * n);
     uint8_t a = 0;
-    for (int c = 0; c < 64 && !a; ++c)
-      a = child[(4 * x + (c & 3)) + m * ((4 * y + ((c >> 2) & 3)) + m * (4 * z + (c >> 4)))];
+    for (int c = 0; c < 64 && !a; ++c) a = child[child64(p, n, c)];
     out[p] = a;
+    my += a;
   }
-}
-
-__device__ __forceinline__ uint64_t child64(uint64_t p, uint32_t n, int c) {
-  const uint64_t m = 4ull * n;
-  const uint64_t x = p % n, y = (p / n) % n, z = p / ((uint64_t)n * n);
-  return (4 * x + (c & 3)) + m * ((4 * y + ((c >> 2) & 3)) + m * (4 * z + (c >> 4)));
+  my = __reduce_add_sync(0xFFFFFFFFu, my);
+  if ((threadIdx.x & 31u) == 0 && my) atomicAdd(count, my);
 }
 
 __global__ void count64_kernel(const uint64_t* list, uint32_t m, const uint8_t* child_any,
@@ -137,10 +148,11 @@ __global__ void pack_bricks_kernel(Lattice g, const uint64_t* cells, uint32_t nb
                                    int32_t* cell_xyz, int32_t* map) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int nbs = __ffs(g.nb) - 1;
   for (uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < nbricks; b += nwarps) {
     const uint64_t c = cells[b];
-    const int cx = (int)(c % g.nb), cy = (int)((c / g.nb) % g.nb),
-              cz = (int)(c / ((uint64_t)g.nb * g.nb));
+    const int cx = (int)(c & (uint64_t)(g.nb - 1)), cy = (int)((c >> nbs) & (uint64_t)(g.nb - 1)),
+              cz = (int)(c >> (2 * nbs));
     if (lane == 0) {
       cell_xyz[3 * (size_t)b] = cx;
       cell_xyz[3 * (size_t)b + 1] = cy;
@@ -225,13 +237,26 @@ yv_status build_volume_tree(const Lattice& g, int levels, cudaStream_t s, Volume
     if ((e = any[(size_t)l].alloc(n * n * n, s)) != cudaSuccess) return vbuild_fail(e, "alloc");
   }
   const uint64_t cells = (uint64_t)g.nb * g.nb * g.nb;
-  mark_cells_kernel<<<grid_for(cells * 32), 256, 0, s>>>(g, any[(size_t)levels].as<uint8_t>());
+  // occupied nodes per level (counted by the mark and fold passes, read
+  // back once): the breadth-first lists below need no host read per level
+  DevBuf dc;
+  if ((e = dc.alloc((size_t)(levels + 1) * 4, s)) != cudaSuccess ||
+      (e = cudaMemsetAsync(dc.p, 0, (size_t)(levels + 1) * 4, s)) != cudaSuccess)
+    return vbuild_fail(e, "alloc");
+  mark_cells_kernel<<<grid_for(cells * 32), 256, 0, s>>>(g, any[(size_t)levels].as<uint8_t>(),
+                                                         dc.as<uint32_t>() + levels);
   for (int l = levels - 1; l >= 0; --l) {
     const uint32_t n = 1u << (2 * l);
     fold64_kernel<<<grid_for((uint64_t)n * n * n), 256, 0, s>>>(
-        any[(size_t)l + 1].as<uint8_t>(), n, any[(size_t)l].as<uint8_t>());
+        any[(size_t)l + 1].as<uint8_t>(), n, any[(size_t)l].as<uint8_t>(),
+        dc.as<uint32_t>() + l);
   }
-  if ((e = cudaGetLastError()) != cudaSuccess) return vbuild_fail(e, "mark");
+  std::vector<uint32_t> occ((size_t)levels + 1, 0);
+  if ((e = cudaGetLastError()) != cudaSuccess ||
+      (e = cudaMemcpyAsync(occ.data(), dc.p, (size_t)(levels + 1) * 4, cudaMemcpyDeviceToHost,
+                           s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return vbuild_fail(e, "mark");
   // breadth-first lists: level 0 = the root (always a grid node)
   std::vector<DevBuf> list((size_t)levels + 1), offs((size_t)levels);
   std::vector<uint32_t> m((size_t)levels + 1, 0), base((size_t)levels + 1, 0);
@@ -249,11 +274,11 @@ yv_status build_volume_tree(const Lattice& g, int levels, cudaStream_t s, Volume
       count64_kernel<<<grid_for(m[(size_t)l]), 256, 0, s>>>(
           list[(size_t)l].as<uint64_t>(), m[(size_t)l], any[(size_t)l + 1].as<uint8_t>(), n,
           counts.as<uint32_t>());
-    uint32_t total = 0;
     if ((e = cudaGetLastError()) != cudaSuccess ||
         (e = exclusive_scan(counts.as<uint32_t>(), offs[(size_t)l].as<uint32_t>(),
-                            m[(size_t)l], &total, s)) != cudaSuccess)
+                            m[(size_t)l], nullptr, s)) != cudaSuccess)
       return vbuild_fail(e, "scan");
+    const uint32_t total = occ[(size_t)l + 1];  // the scanned total
     base[(size_t)l + 1] = base[(size_t)l] + m[(size_t)l];
     m[(size_t)l + 1] = total;
     if ((e = list[(size_t)l + 1].alloc((size_t)(total ? total : 1) * 8, s)) != cudaSuccess)
@@ -341,15 +366,20 @@ yv_status yv_volume_build_dense(const float* density, const uint8_t* rgb, int32_
                                 std::move(hcell), out);
 }
 
-yv_status yv_volume_upload_dense(const float* density, const uint8_t* rgb, int32_t levels,
-                                 int32_t precision, void* stream, yv_volume_gpu** out) {
-  if (!out) return YV_ERR_INVALID_ARG;
-  *out = nullptr;
+}  // extern "C"
+
+namespace yv {
+namespace {
+
+// Builds the device pool from a lattice into `into` (reusing its arrays
+// where they are large enough) or into a new volume (*out).
+yv_status upload_dense(const float* density, const uint8_t* rgb, int32_t levels,
+                       int32_t precision, cudaStream_t s, yv_volume_gpu* into,
+                       yv_volume_gpu** out) {
   Lattice g;
   if (!lattice_args(density, levels, &g, rgb) || precision < YV_PRECISION_F16 ||
       precision > YV_PRECISION_F16_PACKED)
     return YV_ERR_INVALID_ARG;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   VolumeTree t;
   yv_status st = build_volume_tree(g, levels, s, t);
   if (st != YV_OK) return st;
@@ -364,12 +394,27 @@ yv_status yv_volume_upload_dense(const float* density, const uint8_t* rgb, int32
   }
   // the device pool (owned by the yv_volume_gpu): grids, density, albedo,
   // neighbours up / down
-  void* mem[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   const size_t bytes[5] = {(size_t)t.ngrids * 256, dbytes, abytes, (size_t)t.nbricks * 28,
                            (size_t)t.nbricks * 28};
+  void* fresh[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  void** mem = fresh;
+  size_t* cap = nullptr;
+  yv_volume_device* desc = nullptr;
+  if (into) volume_gpu_arrays(into, &mem, &cap, &desc);
   cudaError_t e = cudaSuccess;
-  for (int i = 0; i < 5 && e == cudaSuccess; ++i)
-    if (bytes[i]) e = cudaMalloc(&mem[i], bytes[i]);
+  for (int i = 0; i < 5 && e == cudaSuccess; ++i) {
+    if (!bytes[i] || (cap && cap[i] >= bytes[i])) continue;
+    if (cap) {
+      // grow: the old array may still be read by queued work on `s`
+      e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) break;
+      cudaFree(mem[i]);
+      mem[i] = nullptr;
+      cap[i] = 0;
+    }
+    e = cudaMalloc(&mem[i], bytes[i]);
+    if (e == cudaSuccess && cap) cap[i] = bytes[i];
+  }
   DevBuf cxyz, map;
   if (e == cudaSuccess) e = cxyz.alloc((size_t)t.nbricks * 12, s);
   if (e == cudaSuccess) e = map.alloc(cells * 4, s);
@@ -385,9 +430,9 @@ yv_status yv_volume_upload_dense(const float* density, const uint8_t* rgb, int32
         static_cast<int32_t*>(mem[4]));
     e = cudaGetLastError();
   }
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {
-    for (void* p : mem) cudaFree(p);
+    if (!into)
+      for (void* p : fresh) cudaFree(p);
     return vbuild_fail(e, "device pool");
   }
   yv_volume_device d;
@@ -400,7 +445,39 @@ yv_status yv_volume_upload_dense(const float* density, const uint8_t* rgb, int32
   d.precision = precision;
   d.nbr_up = static_cast<const int32_t*>(mem[3]);
   d.nbr_dn = static_cast<const int32_t*>(mem[4]);
-  return volume_gpu_from_device(mem, d, out);
+  if (into) {
+    *desc = d;
+    return YV_OK;
+  }
+  // a new volume: its buffers are complete once the stream gets here
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) {
+    for (void* p : fresh) cudaFree(p);
+    return vbuild_fail(e, "device pool");
+  }
+  return volume_gpu_from_device(fresh, bytes, d, out);
+}
+
+}  // namespace
+}  // namespace yv
+
+extern "C" {
+
+yv_status yv_volume_upload_dense(const float* density, const uint8_t* rgb, int32_t levels,
+                                 int32_t precision, void* stream, yv_volume_gpu** out) {
+  if (!out) return YV_ERR_INVALID_ARG;
+  *out = nullptr;
+  return upload_dense(density, rgb, levels, precision, static_cast<cudaStream_t>(stream),
+                      nullptr, out);
+}
+
+yv_status yv_volume_rebuild_dense(yv_volume_gpu* vol, const float* density, const uint8_t* rgb,
+                                  int32_t levels, void* stream) {
+  if (!vol) return YV_ERR_INVALID_ARG;
+  yv_volume_device d;
+  yv_status st = yv_volume_gpu_desc(vol, &d);
+  if (st != YV_OK) return st;
+  return upload_dense(density, rgb, levels, d.precision, static_cast<cudaStream_t>(stream), vol,
+                      nullptr);
 }
 
 }  // extern "C"

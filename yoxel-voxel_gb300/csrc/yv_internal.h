@@ -99,7 +99,12 @@ yv_status volume_host_from_parts(int levels, std::vector<uint32_t>&& grids,
                                  std::vector<float>&& density, std::vector<uint8_t>&& albedo,
                                  std::vector<int32_t>&& cells, yv_volume_host** out);
 // A yv_volume_gpu that owns device buffers mem[0..4] (grids, density,
-// albedo, neighbours up, neighbours down) described by d (api_volume.cpp).
-yv_status volume_gpu_from_device(void* mem[5], const yv_volume_device& d, yv_volume_gpu** out);
+// albedo, neighbours up, neighbours down) of bytes[0..4] bytes, described by
+// d (api_volume.cpp).
+yv_status volume_gpu_from_device(void* mem[5], const size_t bytes[5], const yv_volume_device& d,
+                                 yv_volume_gpu** out);
+// The owned buffers, their allocated sizes and the descriptor of a volume
+// (for rebuilds in place).
+yv_status volume_gpu_arrays(yv_volume_gpu* g, void*** mem, size_t** cap, yv_volume_device** d);
 
 }  // namespace yv

@@ -170,6 +170,7 @@ _SIGS = {
     "yv_volume_gpu_free": (None, [P]),
     "yv_volume_build_dense": (S, [P, P, C.c_int32, P, C.POINTER(P)]),
     "yv_volume_upload_dense": (S, [P, P, C.c_int32, C.c_int32, P, C.POINTER(P)]),
+    "yv_volume_rebuild_dense": (S, [P, P, P, C.c_int32, P]),
     "yv_volume_gpu_desc": (S, [P, C.POINTER(VolumeDevice)]),
     "yv_volume_render": (S, [C.POINTER(VolumeDevice), C.POINTER(Camera), C.c_int32, C.c_int32,
                              C.c_int32, C.POINTER(MarchParams), P, P, P, P]),

@@ -181,6 +181,16 @@ class VolumeGPU:
                 "yv_volume_upload_dense")
         return cls(None, precision, h.value)
 
+    def rebuild_dense(self, density, levels, rgb=None, stream=None):
+        """BrickPool::Update in place: rebuild this device pool from a new
+        lattice on `stream`, reusing its device arrays where they fit."""
+        _check_lattice(density, levels, rgb)
+        L.check(L.lib.yv_volume_rebuild_dense(self._h, C.c_void_p(density.data_ptr()),
+                                              None if rgb is None else
+                                              C.c_void_p(rgb.data_ptr()), levels,
+                                              _stream(stream)), "yv_volume_rebuild_dense")
+        return self
+
     def __del__(self):
         h = getattr(self, "_h", None)
         if h is not None and h.value:
