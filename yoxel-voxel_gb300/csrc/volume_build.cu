@@ -11,7 +11,8 @@
 // grid node; bricks copy their 9^3 lattice values and RGB (white without an
 // rgb lattice); neighbour tables for the apron fold.
 //
-// Passes: one warp per brick cell marks it (ballot over its 729 values);
+// Passes: a cell is marked from per-row cell bits (one warp per lattice row,
+// coalesced loads and ballots) ORed over its 9 x 9 rows;
 // one pass per level ORs 64 child flags; top-down, an exclusive scan of the
 // per-node counts of occupied children expands level l's breadth-first list
 // into level l+1's and gives every node its first child id (bricks are the
@@ -45,28 +46,90 @@ __device__ __forceinline__ uint64_t lat(const Lattice& g, int x, int y, int z) {
   return ((uint64_t)z * g.L + (uint64_t)y) * g.L + (uint64_t)x;
 }
 
-// Mark: one warp per brick cell, any nonzero value among its 9^3.
 // Cell and level sizes are powers of two: index splits use shifts.
-// count: occupied cells, one atomic per warp.
-__global__ void mark_cells_kernel(Lattice g, uint8_t* occ, uint32_t* count) {
+
+// Mark, pass 1: per lattice row (y, z), one bit per brick cell cx: some
+// point of x in [8 cx, 8 cx + 8] (the cell's 8 points and its far apron
+// point) is nonzero.  One warp per row reads it in coalesced 32-point chunks
+// (eight loads in flight); the ballot of chunk j holds the points of cells
+// 4j..4j+3, and a cell's apron point is the first point of the next cell.
+// R[(z L + y) NW + w], NW = max(1, nb / 32) words per row.
+__global__ void mark_rows_kernel(Lattice g, uint32_t* R) {
+  constexpr int kU = 8;
   const uint32_t lane = threadIdx.x & 31u;
-  const int nbs = __ffs(g.nb) - 1;
-  uint32_t my = 0;
-  const uint64_t cells = (uint64_t)g.nb * g.nb * g.nb;
+  const uint64_t rows = g.L * g.L;
+  const uint32_t NW = g.nb >= 32 ? (uint32_t)g.nb / 32u : 1u;
+  const uint32_t chunks = (uint32_t)((g.L + 31) / 32);  // 4 nb / 32 + 1
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-  for (uint64_t c = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; c < cells;
-       c += nwarps) {
-    const int cx = (int)(c & (uint64_t)(g.nb - 1)), cy = (int)((c >> nbs) & (uint64_t)(g.nb - 1)),
-              cz = (int)(c >> (2 * nbs));
-    bool nz = false;
-    for (int k = (int)lane; k < kVL3 && !nz; k += 32)
-      nz = __ldg(g.d + lat(g, cx * kVB + k % kVL, cy * kVB + (k / kVL) % kVL,
-                           cz * kVB + k / (kVL * kVL))) != 0.f;
-    const uint32_t any = __ballot_sync(0xFFFFFFFFu, nz);
-    if (lane == 0) occ[c] = any ? 1 : 0;
-    my += any ? 1u : 0u;
+  for (uint64_t row = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; row < rows;
+       row += nwarps) {
+    const float* p = g.d + row * g.L;
+    uint32_t word = 0, prev = 0;  // cell bits being assembled, previous chunk's ballot
+    for (uint32_t j0 = 0; j0 < chunks; j0 += kU) {
+      float v[kU];
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const uint64_t x = (uint64_t)(j0 + u) * 32u + lane;
+        v[u] = (j0 + u < chunks && x < g.L) ? __ldg(p + x) : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < kU; ++u) {
+        const uint32_t j = j0 + (uint32_t)u;
+        if (j >= chunks) break;
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, v[u] != 0.f);
+        if (j > 0) {
+          // cells 4(j-1)..4(j-1)+3: own bytes of the previous chunk, apron =
+          // the first bit of the following byte (bit 0 of this chunk for
+          // the last one).  Bit 8k of `own` = byte k nonzero; the four
+          // bits 0, 8, 16, 24 are gathered into bits 24..27 by one multiply
+          // (no carries: the partial products below bit 24 are distinct).
+          uint32_t own = prev | (prev >> 4);
+          own |= own >> 2;
+          own |= own >> 1;
+          const uint32_t ap = (prev >> 8) | ((m & 1u) << 24);
+          const uint32_t c4 = (((own | ap) & 0x01010101u) * 0x01020408u) >> 24;
+          const uint32_t cbase = 4u * (j - 1);  // first cell of the group
+          if (cbase < (uint32_t)g.nb) {
+            word |= c4 << (cbase & 31u);
+            if ((cbase & 31u) == 28u || cbase + 4u >= (uint32_t)g.nb) {
+              if (lane == 0) R[row * NW + (cbase >> 5)] = word;
+              word = 0;
+            }
+          }
+        }
+        prev = m;
+      }
+    }
   }
-  if (lane == 0 && my) atomicAdd(count, my);
+}
+
+// Mark, pass 2: a cell is occupied when its bit is set in any of the 9 x 9
+// rows y in [8 cy, 8 cy + 8], z in [8 cz, 8 cz + 8].  One thread per row word
+// and (cy, cz); count = occupied cells, one atomic per warp.
+__global__ void mark_cells_from_rows_kernel(Lattice g, const uint32_t* R, uint8_t* occ,
+                                            uint32_t* count) {
+  const uint32_t NW = g.nb >= 32 ? (uint32_t)g.nb / 32u : 1u;
+  const int nbs = __ffs(g.nb) - 1;
+  const uint64_t total = (uint64_t)NW * g.nb * g.nb;
+  uint32_t my = 0;
+  for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+       t += (uint64_t)gridDim.x * blockDim.x) {
+    const int wsh = __ffs(NW) - 1;  // NW is a power of two
+    const uint32_t w = (uint32_t)(t & (NW - 1u));
+    const uint64_t yz = t >> wsh;
+    const uint32_t cy = (uint32_t)(yz & (uint64_t)(g.nb - 1)), cz = (uint32_t)(yz >> nbs);
+    uint32_t acc = 0;
+    for (int dz = 0; dz < 9; ++dz)
+      for (int dy = 0; dy < 9; ++dy)
+        acc |= R[(((uint64_t)(8 * cz + dz)) * g.L + (8 * cy + dy)) * NW + w];
+    const int nbits = g.nb >= 32 ? 32 : g.nb;
+    for (int b = 0; b < nbits; ++b)
+      occ[((uint64_t)cz << (2 * nbs)) + ((uint64_t)cy << nbs) + 32u * w + (uint32_t)b] =
+          (uint8_t)((acc >> b) & 1u);
+    my += (uint32_t)__popc(nbits == 32 ? acc : acc & ((1u << nbits) - 1u));
+  }
+  my = __reduce_add_sync(0xFFFFFFFFu, my);
+  if ((threadIdx.x & 31u) == 0 && my) atomicAdd(count, my);
 }
 
 // Index of child c (x | y<<2 | z<<4) of node p of a level with n = 2^s
@@ -159,39 +222,54 @@ __global__ void pack_bricks_kernel(Lattice g, const uint64_t* cells, uint32_t nb
       cell_xyz[3 * (size_t)b + 2] = cz;
       map[c] = (int32_t)b;
     }
-    for (int k = (int)lane; k < kVL3; k += 32) {
-      const uint64_t src = lat(g, cx * kVB + k % kVL, cy * kVB + (k / kVL) % kVL,
-                               cz * kVB + k / (kVL * kVL));
-      const float v = __ldg(g.d + src);
-      uint8_t r = 255, gg = 255, bb = 255;
-      if (g.rgb) {
-        r = g.rgb[3 * src];
-        gg = g.rgb[3 * src + 1];
-        bb = g.rgb[3 * src + 2];
+    // lattice point k = lane + 32 q; the loads of 8 points are issued before
+    // any is used
+    for (int q0 = 0; q0 < (kVL3 + 31) / 32; q0 += 8) {
+      float pv[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = (int)lane + 32 * (q0 + u);
+        pv[u] = k < kVL3 ? __ldg(g.d + lat(g, cx * kVB + k % kVL, cy * kVB + (k / kVL) % kVL,
+                                            cz * kVB + k / (kVL * kVL)))
+                         : 0.f;
       }
-      const size_t o = (size_t)b * kVL3 + (size_t)k;
-      if (format < 0) {
-        dens[o] = v;
-        rgb[3 * o] = r;
-        rgb[3 * o + 1] = gg;
-        rgb[3 * o + 2] = bb;
-      } else if (format == YV_PRECISION_F16) {
-        static_cast<uint16_t*>(d_out)[o] = f16_saturating(v);
-        static_cast<uchar4*>(a_out)[o] = make_uchar4(r, gg, bb, 255);
-      } else if (format == YV_PRECISION_F32) {
-        static_cast<float*>(d_out)[o] = v;
-        float* a = static_cast<float*>(a_out) + 3 * o;
-        a[0] = __fmul_rn((float)r, 1.0f / 255.0f);
-        a[1] = __fmul_rn((float)gg, 1.0f / 255.0f);
-        a[2] = __fmul_rn((float)bb, 1.0f / 255.0f);
-      } else if (format == YV_PRECISION_F32_PACKED) {
-        static_cast<float4*>(a_out)[o] =
-            make_float4(__fmul_rn((float)r, 1.0f / 255.0f), __fmul_rn((float)gg, 1.0f / 255.0f),
-                        __fmul_rn((float)bb, 1.0f / 255.0f), v);
-      } else {
-        static_cast<uint2*>(a_out)[o] =
-            make_uint2((uint32_t)f16_saturating(v) | ((uint32_t)r << 16) | ((uint32_t)gg << 24),
-                       (uint32_t)bb);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int k = (int)lane + 32 * (q0 + u);
+        if (k >= kVL3) break;
+        const uint64_t src = lat(g, cx * kVB + k % kVL, cy * kVB + (k / kVL) % kVL,
+                                 cz * kVB + k / (kVL * kVL));
+        const float v = pv[u];
+        uint8_t r = 255, gg = 255, bb = 255;
+        if (g.rgb) {
+          r = g.rgb[3 * src];
+          gg = g.rgb[3 * src + 1];
+          bb = g.rgb[3 * src + 2];
+        }
+        const size_t o = (size_t)b * kVL3 + (size_t)k;
+        if (format < 0) {
+          dens[o] = v;
+          rgb[3 * o] = r;
+          rgb[3 * o + 1] = gg;
+          rgb[3 * o + 2] = bb;
+        } else if (format == YV_PRECISION_F16) {
+          static_cast<uint16_t*>(d_out)[o] = f16_saturating(v);
+          static_cast<uchar4*>(a_out)[o] = make_uchar4(r, gg, bb, 255);
+        } else if (format == YV_PRECISION_F32) {
+          static_cast<float*>(d_out)[o] = v;
+          float* a = static_cast<float*>(a_out) + 3 * o;
+          a[0] = __fmul_rn((float)r, 1.0f / 255.0f);
+          a[1] = __fmul_rn((float)gg, 1.0f / 255.0f);
+          a[2] = __fmul_rn((float)bb, 1.0f / 255.0f);
+        } else if (format == YV_PRECISION_F32_PACKED) {
+          static_cast<float4*>(a_out)[o] =
+              make_float4(__fmul_rn((float)r, 1.0f / 255.0f), __fmul_rn((float)gg, 1.0f / 255.0f),
+                          __fmul_rn((float)bb, 1.0f / 255.0f), v);
+        } else {
+          static_cast<uint2*>(a_out)[o] =
+              make_uint2((uint32_t)f16_saturating(v) | ((uint32_t)r << 16) | ((uint32_t)gg << 24),
+                         (uint32_t)bb);
+        }
       }
     }
   }
@@ -236,15 +314,20 @@ yv_status build_volume_tree(const Lattice& g, int levels, cudaStream_t s, Volume
     const uint64_t n = 1ull << (2 * l);
     if ((e = any[(size_t)l].alloc(n * n * n, s)) != cudaSuccess) return vbuild_fail(e, "alloc");
   }
-  const uint64_t cells = (uint64_t)g.nb * g.nb * g.nb;
   // occupied nodes per level (counted by the mark and fold passes, read
   // back once): the breadth-first lists below need no host read per level
   DevBuf dc;
   if ((e = dc.alloc((size_t)(levels + 1) * 4, s)) != cudaSuccess ||
       (e = cudaMemsetAsync(dc.p, 0, (size_t)(levels + 1) * 4, s)) != cudaSuccess)
     return vbuild_fail(e, "alloc");
-  mark_cells_kernel<<<grid_for(cells * 32), 256, 0, s>>>(g, any[(size_t)levels].as<uint8_t>(),
-                                                         dc.as<uint32_t>() + levels);
+  {
+    const uint64_t NW = g.nb >= 32 ? (uint64_t)g.nb / 32 : 1;
+    DevBuf rows;
+    if ((e = rows.alloc(g.L * g.L * NW * 4, s)) != cudaSuccess) return vbuild_fail(e, "alloc");
+    mark_rows_kernel<<<grid_for(g.L * g.L * 32), 256, 0, s>>>(g, rows.as<uint32_t>());
+    mark_cells_from_rows_kernel<<<grid_for(NW * g.nb * g.nb), 256, 0, s>>>(
+        g, rows.as<uint32_t>(), any[(size_t)levels].as<uint8_t>(), dc.as<uint32_t>() + levels);
+  }
   for (int l = levels - 1; l >= 0; --l) {
     const uint32_t n = 1u << (2 * l);
     fold64_kernel<<<grid_for((uint64_t)n * n * n), 256, 0, s>>>(
