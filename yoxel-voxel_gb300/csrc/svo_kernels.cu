@@ -94,9 +94,10 @@ cudaError_t launch_svo_frame(const SvoDeviceScene& sc, const SvoFrameArgs& a,
   if (nsm > 4096) nsm = 4096;
   uint32_t refill = (uint32_t)(cfg.tile_rays <= 0 ? 32 : cfg.tile_rays);
   if (refill > 32) refill = 32;
-  // register budget: blocks_per_sm 2 (up to 128 regs), 3 (80), 4 (64);
-  // 0 = default 4 (fastest on the 2048^3 frame with unstaged node reads)
-  const int mb = cfg.blocks_per_sm <= 0 ? 4 : (cfg.blocks_per_sm > 4 ? 4 : cfg.blocks_per_sm);
+  // register budget: blocks_per_sm 2 (up to 128 regs), 3 (80), 4 (64), 5
+  // (51); 0 = default 5 (fastest on the 2048^3 frame with unstaged node
+  // reads: 0.991 ms against 1.003 at 4; 6 blocks spill)
+  const int mb = cfg.blocks_per_sm <= 0 ? 5 : (cfg.blocks_per_sm > 5 ? 5 : cfg.blocks_per_sm);
   cudaError_t e;
   if (sc.ref_layout) {
     // a caller VoxNode pool (an editable scene's device mirror): checked
@@ -104,21 +105,25 @@ cudaError_t launch_svo_frame(const SvoDeviceScene& sc, const SvoFrameArgs& a,
     e = launch_with<3, false, false, true>(sc, a, bt, 0, refill, 0, stream);
   } else if (a.lod_coef > 0.f && sc.node_data) {
     // level-of-detail frames: one instantiation, the default launch shape
-    e = launch_with<4, false, true>(sc, a, bt, 0, refill, 0, stream);
+    e = launch_with<5, false, true>(sc, a, bt, 0, refill, 0, stream);
   } else if (nsm == 0) {
     if (mb <= 2)
       e = launch_with<2, false>(sc, a, bt, nsm, refill, 0, stream);
     else if (mb == 3)
       e = launch_with<3, false>(sc, a, bt, nsm, refill, 0, stream);
-    else
+    else if (mb == 4)
       e = launch_with<4, false>(sc, a, bt, nsm, refill, 0, stream);
+    else
+      e = launch_with<5, false>(sc, a, bt, nsm, refill, 0, stream);
   } else {
     if (mb <= 2)
       e = launch_with<2, true>(sc, a, bt, nsm, refill, 0, stream);
     else if (mb == 3)
       e = launch_with<3, true>(sc, a, bt, nsm, refill, 0, stream);
-    else
+    else if (mb == 4)
       e = launch_with<4, true>(sc, a, bt, nsm, refill, 0, stream);
+    else
+      e = launch_with<5, true>(sc, a, bt, nsm, refill, 0, stream);
   }
   if (launches) *launches = 1;
   return e;

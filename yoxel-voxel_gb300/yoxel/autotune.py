@@ -15,7 +15,7 @@ import os
 
 DEFAULT_CACHE = os.path.join(os.path.expanduser("~"), ".cache", "yoxel", "autotune.json")
 
-SVO_SPACE = dict(block_threads=[128, 256], blocks_per_sm=[2, 3, 4], smem_nodes=[0, 73, 585],
+SVO_SPACE = dict(block_threads=[128, 256], blocks_per_sm=[3, 4, 5], smem_nodes=[0, 73, 585],
                  tile_rays=[24, 32])
 BATCH_SPACE = dict(block_threads=[128, 256], blocks_per_sm=[2, 3, 4])
 
