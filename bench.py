@@ -1009,6 +1009,15 @@ def run_dynsync(args, cfg):
     mean_sync = sum(sync_ms) / len(sync_ms)
     mean_frame = sum(frame_ms) / len(frame_ms)
     step_ms = mean_sync + mean_frame
+    # the frame kernel's algorithmic bytes: 40 B per node dereference, 8 B
+    # per pixel (RGBA8 + hit id), 8 B leaf attribute per hit
+    fo = dyn.render(pos, view, (0, 0, 1), 60.0, w, h, LIGHT)
+    torch.cuda.synchronize()
+    F = int(fo["fetches"].to(torch.int64).sum())
+    hits = int((fo["hit"] != -1).sum())
+    frame_bytes = 40 * F + 8 * w * h + 8 * hits
+    peaks, kind = measured_peaks()
+    achieved = frame_bytes / (mean_frame / 1e3) / 1e9
     line = _base_line(args, cfg, (w * h) / (step_ms / 1e3) / 1e6, step_ms, "f32")
     line["metric"] = "Mrays/s of the edit-sync-trace loop on 1 GB300"
     line["config"].update(scene_nodes=scene.node_count, edits_per_step=cfg["edits"])
@@ -1016,7 +1025,14 @@ def run_dynsync(args, cfg):
         "sync_ms_host_wall": round(mean_sync, 4), "frame_ms": round(mean_frame, 4),
         "bytes_per_sync": int(sum(moved) / len(moved)), "full_upload_bytes": full_bytes,
         "full_sync_ms": round(full_ms, 3),
-        "roofline": None, "e2e": None, "gpu_launches": None})
+        "roofline": {"bound": "hbm", "kernel": "svo_frame_kernel (caller pool: the mirror)",
+                     "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                     "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": None,
+                     "peak_source": kind, "algorithmic_bytes_per_frame": frame_bytes,
+                     "note": "the sync moves its pages host to device; the frame reads the "
+                             "mirror"},
+        # per step: one page scatter per array (nodes, attributes) + the frame
+        "e2e": None, "gpu_launches": 3 * args.steps})
     print(json.dumps(line), flush=True)
 
 

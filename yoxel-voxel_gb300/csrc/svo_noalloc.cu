@@ -111,16 +111,20 @@ extern "C" yv_status yv_render_svo_noalloc(const yv_vox_node* nodes, uint32_t co
   a.counters = scratch;
 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  auto kern = svo_frame_kernel<3, true, 0, false>;
+  // checked traversal of the caller's pool with the 4-frame shared-memory
+  // ring (dynamic shared memory, 4 KB per warp: no allocation)
+  constexpr int kRing = 4;
+  constexpr size_t kSmem = (256 / 32) * kRing * 1024;
+  auto kern = svo_frame_kernel<3, true, kRing, false>;
   int resident = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, 256, 0);
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kern, 256, kSmem);
   if (e == cudaSuccess && resident <= 0) e = cudaErrorInvalidConfiguration;
   // the counters start every frame at zero: the array keeps the last call's
   // contents
   if (e == cudaSuccess)
     e = cudaMemsetAsync(scratch, 0, kSvoCounterWords * sizeof(uint32_t), s);
   if (e == cudaSuccess) {
-    kern<<<device_sm_count() * resident, 256, 0, s>>>(sc, a, 0u, 32u);
+    kern<<<device_sm_count() * resident, 256, kSmem, s>>>(sc, a, 0u, 32u);
     e = cudaGetLastError();
   }
   if (e != cudaSuccess) {
