@@ -11,6 +11,16 @@ namespace {
 // per-lane gradient accumulators live in registers (a shared-memory copy
 // measured 1.25x slower).
 constexpr int kBackwardMinBlocks = 3;
+// Register budget of the forward march per lattice format: the fp16 +
+// 8-bit colour formats (0, 3) run at 3 resident blocks (74 registers for the
+// 8-byte format: 1.19 ms on the 1024^2 frame of a 512^3 volume, against 1.26
+// ms at 4 blocks / 64 registers and 1.43 ms at 5 / 48 with spills); the fp32
+// formats (1, 2) at 4 (the 64-camera 128^3 forward: 3.19 ms at 4 blocks,
+// 3.29 ms at 3).
+template <int P>
+struct ForwardBlocks {
+  static constexpr int value = (P == 0 || P == 3) ? 3 : 4;
+};
 
 // tile mapping: warp w of the grid -> 8x4 pixel tile of one camera image
 __device__ __forceinline__ bool ray_of_thread(const VolumeArgs& a, uint32_t tile, int& cam,
@@ -32,8 +42,10 @@ __device__ __forceinline__ uint32_t stage_grids(const VolumeArgs& a, uint32_t* s
   return nsg;
 }
 
-template <int P>
-__global__ void __launch_bounds__(256) volume_forward_kernel(VolumeArgs a) {
+// kMinBlocks: resident blocks of 256 per SM the register allocation is
+// sized for.
+template <int P, int kMinBlocks>
+__global__ void __launch_bounds__(256, kMinBlocks) volume_forward_kernel(VolumeArgs a) {
   __shared__ uint32_t sg[kSmemGrids * 64];
   const uint32_t nsg = stage_grids(a, sg);
   const uint32_t n_tiles = (uint32_t)a.ncams * (uint32_t)(((a.width + 7) >> 3) * ((a.height + 3) >> 2));
@@ -208,10 +220,10 @@ cudaError_t launch_volume_forward(const VolumeArgs& a, cudaStream_t s) {
   const uint32_t blocks = (tiles + 7) / 8;
   if (blocks == 0) return cudaSuccess;
   switch (a.v.precision) {
-    case 0: volume_forward_kernel<0><<<blocks, 256, 0, s>>>(a); break;
-    case 1: volume_forward_kernel<1><<<blocks, 256, 0, s>>>(a); break;
-    case 2: volume_forward_kernel<2><<<blocks, 256, 0, s>>>(a); break;
-    case 3: volume_forward_kernel<3><<<blocks, 256, 0, s>>>(a); break;
+    case 0: volume_forward_kernel<0, ForwardBlocks<0>::value><<<blocks, 256, 0, s>>>(a); break;
+    case 1: volume_forward_kernel<1, ForwardBlocks<1>::value><<<blocks, 256, 0, s>>>(a); break;
+    case 2: volume_forward_kernel<2, ForwardBlocks<2>::value><<<blocks, 256, 0, s>>>(a); break;
+    case 3: volume_forward_kernel<3, ForwardBlocks<3>::value><<<blocks, 256, 0, s>>>(a); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
