@@ -126,6 +126,27 @@ def test_ssna_matches_oracle(yoxel_mod, spheres, case):
         assert (got[1][hits] != z0[hits]).mean() > 0.05
 
 
+@pytest.mark.parametrize("passes", [3, 24])
+def test_passes_beyond_the_nearest_depth_are_skipped_exactly(yoxel_mod, spheres, passes):
+    """The nearest hit lies between the pass limits: the leading passes blur,
+    the rest are skipped by the kernels (the limits fall below the frame's
+    smallest depth), and the result is still the oracle's."""
+    r, pos = make_renderer(yoxel_mod, spheres, dist=0.9)
+    p = r.ssna_params()
+    fine_voxel(p)
+    p.blur_passes = passes
+    tr = unlit_trace(r)
+    hits = (tr["rgba"] >> 24) != 0
+    z0 = O.depth(tr["rgba"], tr["hit_t"], *r.ray_basis())
+    zl = O.zlimits(passes, p.voxel_size, float(np.float32(FOV)), W)
+    zmin = z0[hits].min()
+    if passes == 24:
+        assert zl[0] >= zmin > zl[-1]  # some passes run, some do not
+    got = run_ssna(r, p)
+    want = oracle_frame(r, pos, tr, p)
+    assert_close(got, want)
+
+
 def test_frame_normal_output_is_the_leaf_normal(yoxel_mod, spheres):
     r, _ = make_renderer(yoxel_mod, spheres)
     tr = unlit_trace(r)

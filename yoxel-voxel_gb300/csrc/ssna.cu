@@ -35,8 +35,9 @@
 // Launch shape: every pass works on 32x32-pixel tiles with 256 threads, 4
 // pixels a thread, and issues all of a thread's global loads before it uses
 // any, so the depth-buffer passes (8 MB in, 8 MB out at 1920x1080, L2
-// resident) are not bound by load latency.  A pass whose limit blurs no pixel
-// is a copy.
+// resident) are not bound by load latency.  The depth pass also finds the
+// frame's smallest hit depth, and a blur pass whose limit lies below it
+// returns without work.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -57,6 +58,7 @@ constexpr int kTile = 32;              // kTile x kTile pixels per block
 constexpr int kRowsPer = kTile / kTY;  // pixels (rows) per thread
 constexpr int kHalo = 2;
 constexpr int kSm = kTile + 2 * kHalo;  // shared tile side of the blur
+constexpr int kMaxPasses = 64;         // blur passes a frame may ask for
 
 struct BlurWeights {
   float k[25];  // [oy + 2][ox + 2]
@@ -91,33 +93,39 @@ __device__ __forceinline__ float dot3(const float a[3], const float b[3]) {
                    __fmul_rn(a[2], b[2]));
 }
 
+// zmin: the smallest hit depth of the frame (bits of a non-negative float,
+// which order like the floats), for skipping blur passes that blur nothing.
 __global__ void __launch_bounds__(kTX* kTY)
     depth_kernel(const uint32_t* __restrict__ albedo, const float* __restrict__ hit_t, View v,
-                 float* __restrict__ z) {
+                 float* __restrict__ z, uint32_t* __restrict__ zmin) {
   const int x = blockIdx.x * kTile + threadIdx.x;
   const int y0 = blockIdx.y * kTile + threadIdx.y;
-  if (x >= v.width) return;
+  uint32_t my_min = 0x7F7FFFFFu;  // FLT_MAX
   uint32_t a[kRowsPer];
   float t[kRowsPer];
 #pragma unroll
   for (int r = 0; r < kRowsPer; ++r) {
     const int y = y0 + r * kTY;
     const size_t off = (size_t)y * (size_t)v.width + (size_t)x;
-    a[r] = y < v.height ? __ldg(albedo + off) : 0u;
-    t[r] = y < v.height ? __ldg(hit_t + off) : 0.f;
+    a[r] = (x < v.width && y < v.height) ? __ldg(albedo + off) : 0u;
+    t[r] = (x < v.width && y < v.height) ? __ldg(hit_t + off) : 0.f;
   }
 #pragma unroll
   for (int r = 0; r < kRowsPer; ++r) {
     const int y = y0 + r * kTY;
-    if (y >= v.height) continue;
+    if (x >= v.width || y >= v.height) continue;
     float out = kFar;
     if (a[r] >> 24) {
       float u[3];
       ray_u(v, x, y, u);
       out = __fdiv_rn(t[r], __fsqrt_rn(dot3(u, u)));
+      const uint32_t b = __float_as_uint(fmaxf(out, 0.f));
+      my_min = b < my_min ? b : my_min;
     }
     z[(size_t)y * (size_t)v.width + (size_t)x] = out;
   }
+  my_min = __reduce_min_sync(0xFFFFFFFFu, my_min);
+  if ((threadIdx.x & 31u) == 0) atomicMin(zmin, my_min);
 }
 
 // Blurred depth of pixel (x, y) of a w x h frame; at(dx, dy) is the depth of
@@ -166,9 +174,22 @@ __device__ __forceinline__ float blur_pixel(At at, int x, int y, int w, int h, f
   return blur_taps<true>(at, d, x, y, w, h, thr, pad_thr, bw);
 }
 
+// Whether a blur pass with limit zlimit can change a pixel of a frame whose
+// smallest hit depth is zm.  Every blurred depth is a weighted mean of depths
+// and depths moved away from the eye (edge_pad >= 0), so the buffer's
+// smallest depth falls only by rounding (about 51 ulp a pass, 2e-4 relative
+// over 64 passes); a pass with zlimit below zm (1 - 2^-10) blurs nothing.
+// The passes that run are a prefix of the schedule: the limits decrease.
+__device__ __forceinline__ bool pass_runs(float zm, float zlimit) {
+  return zlimit >= __fmul_rn(zm, 1.f - 1.f / 1024.f);
+}
+
+// A pass that blurs nothing returns at once; its buffers keep their roles.
 __global__ void __launch_bounds__(kTX* kTY)
     blur_kernel(const float* __restrict__ zin, float* __restrict__ zout, int w, int h,
-                float zlimit, float thr, float pad_thr, BlurWeights bw) {
+                float zlimit, float thr, float pad_thr, BlurWeights bw,
+                const uint32_t* __restrict__ zmin) {
+  if (!pass_runs(__uint_as_float(__ldg(zmin)), zlimit)) return;
   __shared__ float tile[kSm][kSm];
   constexpr int kLoads = (kSm * kSm + kTX * kTY - 1) / (kTX * kTY);
   const int x0 = blockIdx.x * kTile - kHalo, y0 = blockIdx.y * kTile - kHalo;
@@ -303,11 +324,23 @@ __device__ __forceinline__ uint32_t shade_pixel(uint32_t alb, float zc, const fl
   return out;
 }
 
+// The final depth is in za after an even number of passes that ran, zb
+// after an odd number (pass_runs decides each).
+struct PassLimits {
+  float z[kMaxPasses];
+  int n;
+};
+
 __global__ void __launch_bounds__(kTX* kTY)
-    shade_kernel(const uint32_t* __restrict__ albedo, const float* __restrict__ z,
+    shade_kernel(const uint32_t* __restrict__ albedo, const float* __restrict__ za,
+                 const float* __restrict__ zb, PassLimits pl, const uint32_t* __restrict__ zmin,
                  const float* __restrict__ stored_n, View v, Shading sh,
                  uint32_t* __restrict__ rgba, float* __restrict__ depth_out,
                  float* __restrict__ normal_out) {
+  const float zm = __uint_as_float(__ldg(zmin));
+  int ran = 0;
+  for (int i = 0; i < pl.n; ++i) ran += pass_runs(zm, pl.z[i]) ? 1 : 0;
+  const float* __restrict__ z = (ran & 1) ? zb : za;
   const int x = blockIdx.x * kTile + threadIdx.x;
   const int y0 = blockIdx.y * kTile + threadIdx.y;
   const int w = v.width, h = v.height;
@@ -436,11 +469,13 @@ yv_status yv_render_ssna(yv_renderer* r, const yv_ssna_params* p, void* device_r
   const View v = make_view(rv);
   const size_t px = (size_t)v.width * (size_t)v.height;
   const int passes = p->ssna ? p->blur_passes : 0;
-  DevBuf alb, ht, nrm, za, zb;
+  DevBuf alb, ht, nrm, za, zb, zmin;
   cudaError_t e;
   if ((e = alb.alloc(px * 4, s)) != cudaSuccess || (e = ht.alloc(px * 4, s)) != cudaSuccess ||
       (e = nrm.alloc(px * 12, s)) != cudaSuccess || (e = za.alloc(px * 4, s)) != cudaSuccess ||
-      (passes > 0 && (e = zb.alloc(px * 4, s)) != cudaSuccess))
+      (e = zb.alloc(passes > 0 ? px * 4 : 16, s)) != cudaSuccess ||
+      (e = zmin.alloc(4, s)) != cudaSuccess ||
+      (e = cudaMemsetAsync(zmin.p, 0x7F, 4, s)) != cudaSuccess)  // 3.4e38: above every depth
     return ssna_fail(e, "scratch");
   yv_frame_outputs fo;
   std::memset(&fo, 0, sizeof(fo));
@@ -475,19 +510,24 @@ yv_status yv_render_ssna(yv_renderer* r, const yv_ssna_params* p, void* device_r
   const dim3 blk(kTX, kTY);
   const dim3 grd((unsigned)((v.width + kTile - 1) / kTile),
                  (unsigned)((v.height + kTile - 1) / kTile));
-  depth_kernel<<<grd, blk, 0, s>>>(alb.as<uint32_t>(), ht.as<float>(), v, za.as<float>());
+  depth_kernel<<<grd, blk, 0, s>>>(alb.as<uint32_t>(), ht.as<float>(), v, za.as<float>(),
+                                   zmin.as<uint32_t>());
   if ((e = cudaGetLastError()) != cudaSuccess) return ssna_fail(e, "depth launch");
+  PassLimits pl;
+  pl.n = passes;
   float* src = za.as<float>();
   float* dst = zb.as<float>();
   for (int i = 0; i < passes; ++i) {
-    const float zlimit = (float)(5.0 * p->voxel_size / (pix * 3.0 * (i + 1)));
-    blur_kernel<<<grd, blk, 0, s>>>(src, dst, v.width, v.height, zlimit, thr, pad_thr, bw);
+    pl.z[i] = (float)(5.0 * p->voxel_size / (pix * 3.0 * (i + 1)));
+    blur_kernel<<<grd, blk, 0, s>>>(src, dst, v.width, v.height, pl.z[i], thr, pad_thr, bw,
+                                    zmin.as<uint32_t>());
     if ((e = cudaGetLastError()) != cudaSuccess) return ssna_fail(e, "blur launch");
     float* t = src;
     src = dst;
     dst = t;
   }
-  shade_kernel<<<grd, blk, 0, s>>>(alb.as<uint32_t>(), src, nrm.as<float>(), v, sh,
+  shade_kernel<<<grd, blk, 0, s>>>(alb.as<uint32_t>(), za.as<float>(), zb.as<float>(), pl,
+                                   zmin.as<uint32_t>(), nrm.as<float>(), v, sh,
                                    static_cast<uint32_t*>(device_rgba),
                                    static_cast<float*>(device_depth),
                                    static_cast<float*>(device_normals));
