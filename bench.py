@@ -38,6 +38,7 @@ UNIT = "Mrays/s"
 POOL_FORMATS = {0: "fp16 density + RGBA8 albedo", 1: "fp32 density + fp32 RGB albedo",
                 2: "packed float4 (r, g, b, density)",
                 3: "packed 8 B (fp16 density, RGB8)"}
+SEED = 1234  # default seed of every synthetic workload
 LIGHT = (np.array([0.3, 0.5, 0.8]) / np.linalg.norm([0.3, 0.5, 0.8])).astype(np.float32)
 
 
@@ -201,6 +202,24 @@ def profile_traffic(name):
     return float(m.group(1)) if m else None
 
 
+def cfg_seed(cfg):
+    """The workload's scene seed (1234 unless --seed set another)."""
+    if "scene" in cfg:
+        return cfg["scene"][1]["seed"]
+    return cfg.get("seed", SEED)
+
+
+def with_seed(cfg, seed):
+    """A copy of cfg whose scene, volume or batch specs use `seed`."""
+    import copy
+    c = copy.deepcopy(cfg)
+    if "scene" in c:
+        c["scene"][1]["seed"] = seed
+    else:
+        c["seed"] = seed
+    return c
+
+
 def make_scene(cfg):
     import yoxel
     kind, kw = cfg["scene"]
@@ -254,7 +273,7 @@ def run_reference(args, cfg):
     else:
         import yoxel
         from oracle import pyoracle
-        vol = yoxel.BrickVolume.noise(cfg["levels"], 0.4, 1.4, 1234)
+        vol = yoxel.BrickVolume.noise(cfg["levels"], 0.4, 1.4, cfg_seed(cfg))
         den = vol.density.astype(np.float16).astype(np.float32)
         alb = vol.albedo_u8.astype(np.float32) * np.float32(1.0 / 255.0)
         pos, view = camera()
@@ -282,7 +301,7 @@ def run_reference(args, cfg):
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1000 * sum(secs) / len(secs), 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": cfg["workload"], "config": args.config},
+        "config": {"workload": cfg["workload"], "config": args.config, "seed": cfg_seed(cfg)},
         "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads,
                          "kind": "port", "sample": sample},
         "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -411,7 +430,7 @@ def run_svo(args, cfg):
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(mean_step_s * 1000, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": cfg["workload"], "config": args.config,
+        "config": {"workload": cfg["workload"], "config": args.config, "seed": cfg_seed(cfg),
                    "primary_rays_per_step": npix, "shadow_rays_per_step": shadow_rays,
                    "scene_nodes": dev_nodes, "scene_device_bytes": dev_bytes,
                    "l2": "flushed between steps (256 MiB write); scene > L2",
@@ -479,7 +498,7 @@ def _base_line(args, cfg, value, ms, dtype):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
             "data": "synthetic",
             "config": {"workload": cfg["workload"], "config": args.config,
-                       "l2": "flushed between steps (256 MiB write)"}}
+                       "seed": cfg_seed(cfg), "l2": "flushed between steps (256 MiB write)"}}
 
 
 def run_brick(args, cfg):
@@ -489,7 +508,7 @@ def run_brick(args, cfg):
     from yoxel import workloads as W
     torch.cuda.set_device(dist_env()[2])
     t_scene = time.perf_counter()
-    vol = yoxel.BrickVolume.noise(cfg["levels"], 0.4, 1.4, 1234)
+    vol = yoxel.BrickVolume.noise(cfg["levels"], 0.4, 1.4, cfg_seed(cfg))
     t_scene = time.perf_counter() - t_scene
     prec = cfg["precision"] if args.precision is None else args.precision
     gv = vol.upload(prec)
@@ -571,9 +590,9 @@ def run_train(args, cfg):
     import torch
     import yoxel
     torch.cuda.set_device(dist_env()[2])
-    vol = yoxel.BrickVolume.noise(cfg["levels"], 0.4, 1.4, 1234)
+    vol = yoxel.BrickVolume.noise(cfg["levels"], 0.4, 1.4, cfg_seed(cfg))
     tv = vol.to_torch()
-    g = torch.Generator(device="cuda").manual_seed(1234)
+    g = torch.Generator(device="cuda").manual_seed(cfg_seed(cfg))
     # target volume: the first + N(0, 0.1), owners perturbed then aprons synced
     tgt_d = (tv["density"] + 0.1 * torch.randn(tv["density"].shape, generator=g,
                                                device="cuda")).clamp_(0, 1)
@@ -678,7 +697,7 @@ def run_batch(args, cfg):
     from yoxel import autotune
     from yoxel import workloads as W
     torch.cuda.set_device(dist_env()[2])
-    specs = W.cfg5_specs(1234, cfg["n"])
+    specs = W.cfg5_specs(cfg_seed(cfg), cfg["n"])
     batch = yoxel.Batch()
     keep = []
     t_scene = time.perf_counter()
@@ -1165,10 +1184,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", type=int, default=None, choices=[0, 1, 2, 3],
                     help="brick pool format for the brick workload (default: the config's)")
+    ap.add_argument("--seed", type=int, default=SEED,
+                    help="seed of the synthetic scene, volume or batch (default 1234; other "
+                         "seeds give the run-to-run variance over scenes)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    cfg = CONFIGS[args.config]
+    cfg = with_seed(CONFIGS[args.config], args.seed)
     import importlib.util
     spec = importlib.util.spec_from_file_location("_gentry", os.path.join(ROOT, "__graft_entry__.py"))
     ge = importlib.util.module_from_spec(spec)

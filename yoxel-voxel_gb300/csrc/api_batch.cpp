@@ -98,6 +98,17 @@ BatchLaunch launch_desc(const yv_batch* b) {
   l.nitems = (int)b->items.size();
   l.total_ids = b->total_ids;
   l.counters = b->d_counters;
+  // the batch kernel is compiled per brick lattice format: a batch whose
+  // volumes share one (or that has none) runs the kernel carrying only that
+  // march
+  l.brick_precision = 3;
+  bool first = true;
+  for (const BatchItem& it : b->items) {
+    if (it.kind != kBatchBrick) continue;
+    if (first) l.brick_precision = it.vol.precision;
+    else if (l.brick_precision != it.vol.precision) l.brick_precision = -1;
+    first = false;
+  }
   return l;
 }
 

@@ -25,7 +25,9 @@ namespace {
 // 1 KB x kBatchRing per warp.
 constexpr int kBatchRing = 4;
 
-template <int kMinBlocks>
+// kP: the lattice format of every brick item (its march alone is compiled
+// in), or -1 for a batch mixing formats (all four marches).
+template <int kMinBlocks, int kP>
 __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
   __shared__ BatchItem items[kMaxBatchItems];
   extern __shared__ uint4 ring_smem[];
@@ -52,6 +54,14 @@ __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
   for (;;) {
     const uint32_t busy = __ballot_sync(0xFFFFFFFFu, mode == kPrimary || mode == kShadow);
     if (busy == 0) {
+      // Every lane is idle: the SVO state of its last ray is dead.  Saying
+      // so keeps it out of the registers while a brick tile is marched.
+      tr = Trace{};
+      dx = dy = dz = 0.f;
+      hitw = 0xFFFFFFFFu;
+      fp = 0;
+      ht = 0.f;
+      attr = make_uint4(0u, 0u, 0u, 0u);
       // the whole warp takes the next 8x4 tile of the queue
       uint32_t base = 0;
       if (lane == 0) base = atomicAdd(&b.counters[0], 32u);
@@ -79,7 +89,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
           pixel_ray(it.vcam, x, y, o, d);
           NoVis nv;
           RayOut r;
-          switch (it.vol.precision) {
+          switch (kP >= 0 ? kP : it.vol.precision) {
             case 0: march<0>(it.vol, nullptr, 0u, o, d, nv, r); break;
             case 1: march<1>(it.vol, nullptr, 0u, o, d, nv, r); break;
             case 2: march<2>(it.vol, nullptr, 0u, o, d, nv, r); break;
@@ -143,9 +153,9 @@ __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
   if (err) atomicOr(&b.counters[1], err);
 }
 
-template <int kMinBlocks>
+template <int kMinBlocks, int kP>
 cudaError_t launch_batch_with(const BatchLaunch& b, int bt, cudaStream_t s) {
-  auto kern = batch_kernel<kMinBlocks>;
+  auto kern = batch_kernel<kMinBlocks, kP>;
   const size_t smem = (size_t)(bt / 32) * kBatchRing * 1024u;
   static bool opted_in[64] = {false};
   int dev = 0;
@@ -169,17 +179,28 @@ cudaError_t launch_batch_with(const BatchLaunch& b, int bt, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+template <int kP>
+cudaError_t launch_by_budget(const BatchLaunch& b, int mb, int bt, cudaStream_t s) {
+  if (mb <= 2) return launch_batch_with<2, kP>(b, bt, s);
+  if (mb == 3) return launch_batch_with<3, kP>(b, bt, s);
+  return launch_batch_with<4, kP>(b, bt, s);
+}
+
 }  // namespace
 
 cudaError_t launch_batch(const BatchLaunch& b, const LaunchCfg& cfg, cudaStream_t s) {
   if (b.nitems <= 0) return cudaSuccess;
   int bt = cfg.block_threads;
   if (bt < 32 || bt > 256 || (bt & 31)) bt = 256;
-  // register budget per blocks_per_sm: 2 -> no spills (default), 3, 4
+  // register budget per blocks_per_sm: 2 (default), 3, 4
   const int mb = cfg.blocks_per_sm <= 0 ? 2 : (cfg.blocks_per_sm > 4 ? 4 : cfg.blocks_per_sm);
-  if (mb <= 2) return launch_batch_with<2>(b, bt, s);
-  if (mb == 3) return launch_batch_with<3>(b, bt, s);
-  return launch_batch_with<4>(b, bt, s);
+  switch (b.brick_precision) {
+    case 0: return launch_by_budget<0>(b, mb, bt, s);
+    case 1: return launch_by_budget<1>(b, mb, bt, s);
+    case 2: return launch_by_budget<2>(b, mb, bt, s);
+    case 3: return launch_by_budget<3>(b, mb, bt, s);
+    default: return launch_by_budget<-1>(b, mb, bt, s);
+  }
 }
 
 }  // namespace yv

@@ -35,6 +35,7 @@ struct BatchLaunch {
   int nitems;
   uint32_t total_ids;
   uint32_t* counters;      // device scratch: [0] queue, [1] status
+  int brick_precision;     // lattice format shared by every brick item, -1 if mixed
 };
 
 // Enqueues counter reset + the persistent batch kernel.
