@@ -97,3 +97,52 @@ def test_autotuner_picks_and_caches(yoxel_mod, tmp_path, monkeypatch):
     batch, outs, keep = build_batch(yoxel_mod, torch)
     bb, bt = autotune.tune_batch(batch, "mixed5", reps=1)
     assert bb in [json.loads(k) for k in bt]
+
+
+@pytest.mark.parametrize("blocks_per_sm", [2, 3, 4])
+@pytest.mark.parametrize("formats", [(0, 0), (1, 1), (2, 2), (3, 3), (3, 0), ()])
+def test_every_batch_kernel_variant_matches_separate_launches(yoxel_mod, formats,
+                                                              blocks_per_sm):
+    """The batch kernel is compiled per register budget and per brick lattice
+    format (one format shared by every volume, or all four for a mixed
+    batch; an SVO-only batch takes the 8-byte format's kernel): every
+    variant gives the per-scene frames bit for bit."""
+    import torch
+    from yoxel import workloads as W
+    batch = yoxel_mod.Batch()
+    keep, outs = [], []
+    s = W.spheres(6, seed=21, n_spheres=30)
+    r = yoxel_mod.Renderer()
+    r.SetScene(s)
+    pos, view = W.camera((0.9, 0.4, 0.5))
+    r.SetViewPos(pos)
+    r.SetViewDir(view)
+    r.SetResolution(88, 72)
+    r.SetFOV(60.0)
+    r.SetLight(W.LIGHT, 0.15, 0.85, True)
+    o = torch.zeros((72, 88), dtype=torch.int32, device="cuda")
+    batch.add_svo(r, o)
+    keep += [s, r]
+    outs.append(o)
+    for i, prec in enumerate(formats):
+        v = yoxel_mod.BrickVolume.noise(1 + i, 0.4, 1.4, 31 + i)
+        g = v.upload(prec)
+        pos, view = W.camera((0.4, 1.0, 0.3 + 0.3 * i))
+        o = torch.zeros((60, 84, 4), dtype=torch.float32, device="cuda")
+        batch.add_volume(g.desc(), (pos, view, (0, 0, 1), 60.0), 84, 60, o, alpha_scale=1.3)
+        keep += [v, g]
+        outs.append(o)
+    batch.set_launch_config(block_threads=128, blocks_per_sm=blocks_per_sm)
+    results = {}
+    for mode in ("separate", "graph"):
+        for o in outs:
+            o.fill_(-1) if o.dtype == torch.int32 else o.fill_(float("nan"))
+        if mode == "separate":
+            batch.render_separate()
+        else:
+            batch.render(graph=True)
+        torch.cuda.synchronize()
+        results[mode] = [o.clone() for o in outs]
+    for a, b in zip(results["separate"], results["graph"]):
+        assert torch.equal(a.view(torch.int32), b.view(torch.int32))
+    assert (results["graph"][0] != 0).any()
