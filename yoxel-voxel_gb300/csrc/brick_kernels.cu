@@ -22,16 +22,22 @@ struct ForwardBlocks {
   static constexpr int value = (P == 0 || P == 3) ? 3 : 4;
 };
 
-// tile mapping: warp w of the grid -> 8x4 pixel tile of one camera image
+// tile mapping: warp w of the grid -> 8x4 pixel tile of one camera image;
+// the 8 warps of a block take a 2x4-tile (16x16-pixel) square
+__host__ __device__ __forceinline__ uint32_t tile_ids(const VolumeArgs& a) {
+  const uint32_t tx = (uint32_t)((a.width + 7) >> 3), ty = (uint32_t)((a.height + 3) >> 2);
+  return (uint32_t)a.ncams * ((tx + 1) >> 1) * ((ty + 3) >> 2) * 8u;
+}
 __device__ __forceinline__ bool ray_of_thread(const VolumeArgs& a, uint32_t tile, int& cam,
                                               int& x, int& y) {
-  const int tx = (a.width + 7) >> 3, ty = (a.height + 3) >> 2;
-  const uint32_t per_cam = (uint32_t)(tx * ty);
+  const uint32_t tx = (uint32_t)((a.width + 7) >> 3), ty = (uint32_t)((a.height + 3) >> 2);
+  const uint32_t stx = (tx + 1) >> 1, sty = (ty + 3) >> 2;
+  const uint32_t per_cam = stx * sty * 8u;
   cam = (int)(tile / per_cam);
-  const uint32_t t = tile % per_cam;
+  const uint32_t r = tile % per_cam, st = r >> 3, w = r & 7u;
   const int lane = threadIdx.x & 31;
-  x = (int)(t % (uint32_t)tx) * 8 + (lane & 7);
-  y = (int)(t / (uint32_t)tx) * 4 + (lane >> 3);
+  x = (int)(((st % stx) * 2u + (w & 1u)) * 8u) + (lane & 7);
+  y = (int)(((st / stx) * 4u + (w >> 1)) * 4u) + (lane >> 3);
   return cam < a.ncams && x < a.width && y < a.height;
 }
 
@@ -48,7 +54,7 @@ template <int P, int kMinBlocks>
 __global__ void __launch_bounds__(256, kMinBlocks) volume_forward_kernel(VolumeArgs a) {
   __shared__ uint32_t sg[kSmemGrids * 64];
   const uint32_t nsg = stage_grids(a, sg);
-  const uint32_t n_tiles = (uint32_t)a.ncams * (uint32_t)(((a.width + 7) >> 3) * ((a.height + 3) >> 2));
+  const uint32_t n_tiles = tile_ids(a);
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   bool bad = false;
   for (uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile < n_tiles;
@@ -145,7 +151,7 @@ template <int P, int kMinBlocks>
 __global__ void __launch_bounds__(256, kMinBlocks) volume_backward_kernel(VolumeArgs a) {
   __shared__ uint32_t sg[kSmemGrids * 64];
   const uint32_t nsg = stage_grids(a, sg);
-  const uint32_t n_tiles = (uint32_t)a.ncams * (uint32_t)(((a.width + 7) >> 3) * ((a.height + 3) >> 2));
+  const uint32_t n_tiles = tile_ids(a);
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   bool bad = false;
   for (uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile < n_tiles;
@@ -216,7 +222,7 @@ __global__ void fold_scatter_kernel(VolumeArgs a, int channels, float* g) {
 }  // namespace
 
 cudaError_t launch_volume_forward(const VolumeArgs& a, cudaStream_t s) {
-  const uint32_t tiles = (uint32_t)a.ncams * (uint32_t)(((a.width + 7) >> 3) * ((a.height + 3) >> 2));
+  const uint32_t tiles = tile_ids(a);
   const uint32_t blocks = (tiles + 7) / 8;
   if (blocks == 0) return cudaSuccess;
   switch (a.v.precision) {
@@ -230,7 +236,7 @@ cudaError_t launch_volume_forward(const VolumeArgs& a, cudaStream_t s) {
 }
 
 cudaError_t launch_volume_backward(const VolumeArgs& a, cudaStream_t s) {
-  const uint32_t tiles = (uint32_t)a.ncams * (uint32_t)(((a.width + 7) >> 3) * ((a.height + 3) >> 2));
+  const uint32_t tiles = tile_ids(a);
   const uint32_t blocks = (tiles + 7) / 8;
   if (blocks == 0) return cudaSuccess;
   // only fp32 (learnable) volumes have an adjoint
