@@ -52,8 +52,13 @@ __device__ __forceinline__ uint32_t stage_grids(const VolumeArgs& a, uint32_t* s
 // sized for.
 template <int P, int kMinBlocks>
 __global__ void __launch_bounds__(256, kMinBlocks) volume_forward_kernel(VolumeArgs a) {
-  __shared__ uint32_t sg[kSmemGrids * 64];
-  const uint32_t nsg = stage_grids(a, sg);
+  // the fp32 formats read the grid nodes through L1 with all of L1 (1389 ->
+  // 1434 Mrays/s on the 64-camera 128^3 workload); the 8-byte and fp16
+  // formats stage them (their 512^3 trees read three levels per cell)
+  constexpr bool kStage = !(P == 1 || P == 2);
+  __shared__ uint32_t sgs[kStage ? kSmemGrids * 64 : 1];
+  const uint32_t nsg = kStage ? stage_grids(a, sgs) : 0u;
+  const uint32_t* sg = kStage ? sgs : nullptr;
   const uint32_t n_tiles = tile_ids(a);
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   bool bad = false;
@@ -225,7 +230,7 @@ __global__ void fold_scatter_kernel(VolumeArgs a, int channels, float* g) {
 // The march reads the lattice through L1, so the kernels ask for the
 // smallest shared-memory carveout their resident blocks fit in (16.6 KB of
 // staged grid nodes each, + 1 KB reserved): 25 % (a 64 KB configuration)
-// for 3 blocks, 31 % (100 KB) for 4, none for the adjoint, which stages
+// for 3 blocks, none for the fp32 forwards and the adjoint, which stage
 // nothing.  The rest is L1: on the 64-camera 128^3 workload forward 1365 ->
 // 1388 Mrays/s and adjoint 6.65 -> 6.49 ms against the driver's default
 // choice; cfg3 unchanged.
@@ -237,8 +242,8 @@ void prefer_l1() {
   const cudaFuncAttribute k = cudaFuncAttributePreferredSharedMemoryCarveout;
   const cudaError_t e[6] = {
       cudaFuncSetAttribute(volume_forward_kernel<0, ForwardBlocks<0>::value>, k, 25),
-      cudaFuncSetAttribute(volume_forward_kernel<1, ForwardBlocks<1>::value>, k, 31),
-      cudaFuncSetAttribute(volume_forward_kernel<2, ForwardBlocks<2>::value>, k, 31),
+      cudaFuncSetAttribute(volume_forward_kernel<1, ForwardBlocks<1>::value>, k, 0),
+      cudaFuncSetAttribute(volume_forward_kernel<2, ForwardBlocks<2>::value>, k, 0),
       cudaFuncSetAttribute(volume_forward_kernel<3, ForwardBlocks<3>::value>, k, 25),
       cudaFuncSetAttribute(volume_backward_kernel<1, kBackwardMinBlocks>, k, 0),
       cudaFuncSetAttribute(volume_backward_kernel<2, kBackwardMinBlocks>, k, 0)};
