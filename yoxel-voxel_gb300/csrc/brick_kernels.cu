@@ -41,24 +41,13 @@ __device__ __forceinline__ bool ray_of_thread(const VolumeArgs& a, uint32_t tile
   return cam < a.ncams && x < a.width && y < a.height;
 }
 
-__device__ __forceinline__ uint32_t stage_grids(const VolumeArgs& a, uint32_t* sg) {
-  const uint32_t nsg = a.v.ngrids < (uint32_t)kSmemGrids ? a.v.ngrids : (uint32_t)kSmemGrids;
-  for (uint32_t i = threadIdx.x; i < nsg * 64; i += blockDim.x) sg[i] = __ldg(a.v.grids + i);
-  __syncthreads();
-  return nsg;
-}
-
 // kMinBlocks: resident blocks of 256 per SM the register allocation is
 // sized for.
 template <int P, int kMinBlocks>
 __global__ void __launch_bounds__(256, kMinBlocks) volume_forward_kernel(VolumeArgs a) {
-  // the fp32 formats read the grid nodes through L1 with all of L1 (1389 ->
-  // 1434 Mrays/s on the 64-camera 128^3 workload); the 8-byte and fp16
-  // formats stage them (their 512^3 trees read three levels per cell)
-  constexpr bool kStage = !(P == 1 || P == 2);
-  __shared__ uint32_t sgs[kStage ? kSmemGrids * 64 : 1];
-  const uint32_t nsg = kStage ? stage_grids(a, sgs) : 0u;
-  const uint32_t* sg = kStage ? sgs : nullptr;
+  // grid nodes are read through L1 (see prefer_l1)
+  const uint32_t* sg = nullptr;
+  const uint32_t nsg = 0;
   const uint32_t n_tiles = tile_ids(a);
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   bool bad = false;
@@ -153,9 +142,7 @@ struct GradVis {
 
 // kMinBlocks: register budget (resident blocks of 256 per SM).
 template <int P, int kMinBlocks>
-// The grid nodes are read through L1, not staged in shared memory: the
-// kernel then runs with all of the SM's L1 (6.49 -> 6.42 ms on the
-// 64-camera 128^3 workload).
+// grid nodes are read through L1 (see prefer_l1)
 __global__ void __launch_bounds__(256, kMinBlocks) volume_backward_kernel(VolumeArgs a) {
   const uint32_t* sg = nullptr;
   const uint32_t nsg = 0;
@@ -227,13 +214,13 @@ __global__ void fold_scatter_kernel(VolumeArgs a, int channels, float* g) {
   }
 }
 
-// The march reads the lattice through L1, so the kernels ask for the
-// smallest shared-memory carveout their resident blocks fit in (16.6 KB of
-// staged grid nodes each, + 1 KB reserved): 25 % (a 64 KB configuration)
-// for 3 blocks, none for the fp32 forwards and the adjoint, which stage
-// nothing.  The rest is L1: on the 64-camera 128^3 workload forward 1365 ->
-// 1388 Mrays/s and adjoint 6.65 -> 6.49 ms against the driver's default
-// choice; cfg3 unchanged.
+// The march reads the lattice and the grid nodes through L1, and the
+// kernels use no shared memory, so they ask for the largest L1 (carveout 0).
+// Measured against staging the root and level-1 grid nodes (16.6 KB a
+// block) under the driver's default carveout: 64-camera 128^3 forward
+// 1365 -> 1434 Mrays/s and adjoint 6.65 -> 6.40 ms; 512^3 fp16 + RGB8
+// frame 875 -> 907 Mrays/s (the lowest carveout that still held the staged
+// nodes gave half of these gains).
 void prefer_l1() {
   static bool done[64] = {false};
   int dev = 0;
@@ -241,10 +228,10 @@ void prefer_l1() {
   if (dev < 0 || dev >= 64 || done[dev]) return;
   const cudaFuncAttribute k = cudaFuncAttributePreferredSharedMemoryCarveout;
   const cudaError_t e[6] = {
-      cudaFuncSetAttribute(volume_forward_kernel<0, ForwardBlocks<0>::value>, k, 25),
+      cudaFuncSetAttribute(volume_forward_kernel<0, ForwardBlocks<0>::value>, k, 0),
       cudaFuncSetAttribute(volume_forward_kernel<1, ForwardBlocks<1>::value>, k, 0),
       cudaFuncSetAttribute(volume_forward_kernel<2, ForwardBlocks<2>::value>, k, 0),
-      cudaFuncSetAttribute(volume_forward_kernel<3, ForwardBlocks<3>::value>, k, 25),
+      cudaFuncSetAttribute(volume_forward_kernel<3, ForwardBlocks<3>::value>, k, 0),
       cudaFuncSetAttribute(volume_backward_kernel<1, kBackwardMinBlocks>, k, 0),
       cudaFuncSetAttribute(volume_backward_kernel<2, kBackwardMinBlocks>, k, 0)};
   // a hint: a refusal keeps the default configuration and is not reported

@@ -40,7 +40,6 @@ constexpr int kL = 9;
 constexpr int kL3 = 729;
 constexpr uint32_t kEmpty = 0x80000000u;
 constexpr uint32_t kBrick = 0x40000000u;
-constexpr int kSmemGrids = 65;  // root + up to 64 level-1 grid nodes
 
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
@@ -201,7 +200,8 @@ __device__ __forceinline__ void eval_sample(const VolumeView& a, int b, float lx
 }
 
 // Tree descent for brick cell `cell` (ntree/ntree/nodes.h:56-99 offsets).
-// Top grid nodes come from shared memory.  Returns brick id, -1 if empty,
+// Grid nodes below nsg come from sg (a shared-memory copy; the kernels pass
+// none and read every node through L1).  Returns brick id, -1 if empty,
 // -2 if the pool is malformed.
 __device__ __forceinline__ int lookup(const VolumeView& a, const uint32_t* sg, uint32_t nsg,
                                       const int* cell) {
