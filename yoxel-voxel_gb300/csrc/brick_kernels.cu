@@ -7,7 +7,7 @@
 namespace yv {
 namespace {
 
-// Register budget of the adjoint (resident blocks of 256 per SM): its 32
+// Register budget of the adjoint (resident blocks of 256 per SM): its 16
 // per-lane gradient accumulators live in registers (a shared-memory copy
 // measured 1.25x slower).
 constexpr int kBackwardMinBlocks = 3;
@@ -16,7 +16,8 @@ constexpr int kBackwardMinBlocks = 3;
 // 8-byte format: 1.19 ms on the 1024^2 frame of a 512^3 volume, against 1.26
 // ms at 4 blocks / 64 registers and 1.43 ms at 5 / 48 with spills); the fp32
 // formats (1, 2) at 4 (the 64-camera 128^3 forward: 3.19 ms at 4 blocks,
-// 3.29 ms at 3).
+// 3.29 ms at 3).  Measured while the grid nodes were staged in shared
+// memory.
 template <int P>
 struct ForwardBlocks {
   static constexpr int value = (P == 0 || P == 3) ? 3 : 4;
