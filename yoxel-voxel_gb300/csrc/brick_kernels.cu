@@ -17,7 +17,8 @@ constexpr int kBackwardMinBlocks = 3;
 // ms at 4 blocks / 64 registers and 1.43 ms at 5 / 48 with spills); the fp32
 // formats (1, 2) at 4 (the 64-camera 128^3 forward: 3.19 ms at 4 blocks,
 // 3.29 ms at 3).  Measured while the grid nodes were staged in shared
-// memory.
+// memory; re-measured for the 8-byte format without staging: 904 / 843 /
+// 754 Mrays/s at 3 / 4 / 5 blocks.
 template <int P>
 struct ForwardBlocks {
   static constexpr int value = (P == 0 || P == 3) ? 3 : 4;
