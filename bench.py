@@ -590,20 +590,9 @@ def run_train(args, cfg):
     import torch
     import yoxel
     torch.cuda.set_device(dist_env()[2])
-    vol = yoxel.BrickVolume.noise(cfg["levels"], 0.4, 1.4, cfg_seed(cfg))
-    tv = vol.to_torch()
-    g = torch.Generator(device="cuda").manual_seed(cfg_seed(cfg))
-    # target volume: the first + N(0, 0.1), owners perturbed then aprons synced
-    tgt_d = (tv["density"] + 0.1 * torch.randn(tv["density"].shape, generator=g,
-                                               device="cuda")).clamp_(0, 1)
-    tgt_a = (tv["albedo"] + 0.1 * torch.randn(tv["albedo"].shape, generator=g,
-                                              device="cuda")).clamp_(0, 1)
-    import ctypes as C
-    from yoxel import _lib as L
-    L.check(L.lib.yv_volume_sync_aprons(C.byref(yoxel.torch_desc(tv, tgt_d, tgt_a)),
-                                        C.c_void_p(tgt_d.data_ptr()),
-                                        C.c_void_p(tgt_a.data_ptr()), None), "sync")
-    cams = yoxel.cameras(yoxel.sphere_cameras(cfg["cams"]))
+    from yoxel import workloads as W
+    vol, tv, tgt_d, tgt_a, cam_list = W.cfg4_problem(cfg["levels"], cfg["cams"], cfg_seed(cfg))
+    cams = yoxel.cameras(cam_list)
     w, h = cfg["width"], cfg["height"]
     a_s, st = cfg["alpha_scale"], cfg["step_vox"]
     target = yoxel.render_volume(yoxel.torch_desc(tv, tgt_d, tgt_a), cams, w, h, a_s, st)
@@ -698,50 +687,30 @@ def run_batch(args, cfg):
     from yoxel import workloads as W
     torch.cuda.set_device(dist_env()[2])
     specs = W.cfg5_specs(cfg_seed(cfg), cfg["n"])
-    batch = yoxel.Batch()
-    keep = []
+    prec = cfg["precision"] if args.precision is None else args.precision
     t_scene = time.perf_counter()
+    batch, items = W.cfg5_batch(specs, prec)
     rays = 0
     alg = 0      # algorithmic bytes of one batch (SVO: 40 B/fetch + 8 B/pixel + 8 B/hit;
     outs = []    # bricks: 8 corners x format bytes per sample + refs + 16 B/pixel)
-    for sp in specs:
-        res = sp["res"]
-        pos, view = W.camera(sp["cam_dir"])
-        if sp["kind"] == "svo":
-            s = W.spheres(sp["depth"], seed=sp["seed"])
-            r = yoxel.Renderer()
-            r.SetScene(s)
-            r.SetViewPos(pos)
-            r.SetViewDir(view)
-            r.SetResolution(res, res)
-            r.SetFOV(60.0)
-            r.SetLight(LIGHT, 0.15, 0.85, False)
-            out = torch.empty((res, res), dtype=torch.int32, device="cuda")
-            batch.add_svo(r, out)
+    for it in items:
+        res = it["res"]
+        if it["kind"] == "svo":
             # algorithmic bytes of this scene from its own counters (one render)
-            o = r.render_outputs()
+            o = it["renderer"].render_outputs()
             alg += (40 * int(o["fetches"].to(torch.int64).sum()) + 8 * res * res +
                     8 * int(o["stats"]["hits"]))
-            keep += [r, out]
-            outs.append(out)
-            del s, o
+            del o
         else:
-            v = yoxel.BrickVolume.noise(W.brick_levels_for_depth(sp["depth"]), 0.4, 1.4,
-                                        sp["seed"])
-            prec = cfg["precision"] if args.precision is None else args.precision
-            gv = v.upload(prec)
-            out = torch.empty((res, res, 4), dtype=torch.float32, device="cuda")
-            cam = (pos, view, (0, 0, 1), 60.0)
-            batch.add_volume(gv.desc(), cam, res, res, out)
             ns = torch.zeros((1, res, res), dtype=torch.int32, device="cuda")
             nb = torch.zeros((1, res, res), dtype=torch.int32, device="cuda")
-            yoxel.render_volume(gv.desc(), [cam], res, res, samples=ns, bricks=nb)
+            gv = it["gpu_volume"]
+            yoxel.render_volume(gv.desc(), [it["cam"]], res, res, samples=ns, bricks=nb)
             per_corner = 5 if prec in (0, 3) else 16
             alg += (8 * per_corner * int(ns.to(torch.int64).sum()) +
-                    4 * v.levels * int(nb.to(torch.int64).sum()) + 16 * res * res)
-            keep += [gv, out]
-            outs.append(out)
-            del v, ns, nb
+                    4 * it["volume"].levels * int(nb.to(torch.int64).sum()) + 16 * res * res)
+            del ns, nb
+        outs.append(it["out"])
         rays += res * res
     t_scene = time.perf_counter() - t_scene
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")

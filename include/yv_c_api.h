@@ -266,6 +266,24 @@ yv_status yv_render_frame(yv_renderer* r, uint32_t* host_rgba,
 yv_status yv_render_frame_async(yv_renderer* r, const yv_frame_outputs* out,
                                 void* stream);
 
+/* Tiles [tile_begin, tile_end) of the frame only: the frame is cut into
+ * 8x4-pixel tiles numbered row-major (yv_get_tile_count), and just the
+ * pixels of the given range are traced and written (outputs are full-frame
+ * device buffers as for yv_render_frame_async).  The work split of the
+ * reference's threaded renderer, which gives each thread a band of rows
+ * (TreadedRenderer::RenderFrame, cell/ppu_renderer.cpp:121-144), and of its
+ * SPU renderer, which gives each SPE a stride of 16x16 tiles
+ * (cell/spu/trace_spu.cpp:162-177): a frame split into tile ranges over
+ * several GPUs (or calls) and merged gives the full frame bit for bit.
+ * yv_renderer_frame_stats then counts the range's pixels. */
+#define YV_TILE_W 8
+#define YV_TILE_H 4
+yv_status yv_render_frame_tiles(yv_renderer* r, uint32_t tile_begin,
+                                uint32_t tile_end, const yv_frame_outputs* out,
+                                void* stream);
+yv_status yv_get_tile_count(const yv_renderer* r, uint32_t* tiles_x,
+                            uint32_t* tiles_y);
+
 /* Synchronises the last frame's stream and returns its counters. */
 yv_status yv_renderer_frame_stats(yv_renderer* r, yv_frame_stats* stats);
 
@@ -428,6 +446,13 @@ yv_status yv_batch_clear(yv_batch* b);
 /* Adds the renderer's current scene, camera, light and resolution (a
  * snapshot; the renderer must outlive the batch); output: device RGBA8. */
 yv_status yv_batch_add_svo(yv_batch* b, const yv_renderer* r, void* d_rgba);
+/* The same with any of the renderer's per-pixel device outputs
+ * (yv_frame_outputs: rgba, hit ids, hit t, fetch counts, shadow fetch
+ * counts, normals), so a batched frame reports the hit voxel of every ray
+ * ((node << 3) | child, TraceResult of cell/ppu_renderer.cpp:8-13) as a
+ * per-scene launch does. */
+yv_status yv_batch_add_svo_outputs(yv_batch* b, const yv_renderer* r,
+                                   const yv_frame_outputs* out);
 /* Adds one camera of a device volume; output: device RGBA float4. */
 yv_status yv_batch_add_volume(yv_batch* b, const yv_volume_device* vol,
                               const yv_camera* cam, int32_t width,
@@ -459,7 +484,8 @@ yv_status yv_batch_info(const yv_batch* b, uint32_t* n_items, uint64_t* rays);
  * `stream` first, so calls that overlap on the GPU (other streams, other
  * threads) race and must be serialised by the caller.  Asynchronous: returns
  * launch errors only; malformed pools are contained by the kernel's bounds
- * checks (validate the host copy with yv_svo_validate).  Frames needing more
+ * checks (validate the host copy with yv_svo_validate), and the frame's
+ * device status is read with yv_render_svo_noalloc_status.  Frames needing more
  * than 2^31 rays (8x4-tile padded) or pools over 2^29 nodes return
  * YV_ERR_INVALID_ARG. */
 yv_status yv_render_svo_noalloc(const yv_vox_node* nodes, uint32_t count,
@@ -468,6 +494,15 @@ yv_status yv_render_svo_noalloc(const yv_vox_node* nodes, uint32_t count,
                                 const yv_light* light, int32_t width,
                                 int32_t height, const yv_frame_outputs* out,
                                 void* stream);
+/* Device status of the last allocation-free frame on the current device:
+ * waits for `stream` (the stream of that frame), reads the status word of
+ * the static scratch array and returns YV_ERR_BAD_POOL (a child index outside
+ * the pool, or a leaf attribute index outside attrs), YV_ERR_ITERATION_CAP
+ * (a ray reached the fetch cap or the 16-level depth cap: a cycle or a
+ * too-deep pool) or YV_OK; device_bits (optional) receives the raw bits.
+ * Allocates nothing.  The word belongs to whichever call ran last on the
+ * device, so it must be read before the next allocation-free frame starts. */
+yv_status yv_render_svo_noalloc_status(void* stream, uint32_t* device_bits);
 
 /* ------------------------------------------------------------------------ */
 /* Editable SVO with incremental device sync (DynamicSVO,                   */

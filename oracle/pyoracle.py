@@ -49,10 +49,22 @@ def load_library(build_if_missing=True):
         "orc_brick_render_f64": (I, [P, U, P, P, U, I, P, P, P, P, I, I, D, D, I, I, P, P, P]),
         "orc_brick_render_f32": (I, [P, U, P, P, U, I, P, P, P, P, I, I, F, F, I, I, P, P, P]),
         "orc_brick_render_f64_f32ray": (I, [P, U, P, P, U, I, P, P, P, P, I, I, D, D, I, I,
-                                            P, P, P]),
+                                            P, P, P, P]),
         "orc_brick_render_mt_f32": (I, [I, P, U, P, P, U, I, P, P, P, P, I, I, F, F, P, P, P]),
         "orc_brick_backward_f64": (I, [P, U, P, P, U, I, P, P, P, P, I, I, D, D, P, P, P]),
         "orc_svo_build_dense": (I, [P, P, I, F, P, U, P, U, P, P, P]),
+        "orc_svo_hits_f64_mt": (I, [I, P, U, U, P, P, P, D, I, I, P, P]),
+        "orc_svo_hits_f64_f32ray_mt": (I, [I, P, U, U, P, P, P, P, I, I, P, P]),
+        "orc_brick_backward_f64_f32ray_mt": (I, [I, P, U, P, P, U, I, P, P, P, P, I, I, D, D,
+                                                 P, P, P]),
+        "orc_brick_render_f64_f32ray_mt": (I, [I, P, U, P, P, U, I, P, P, P, P, I, I, D, D,
+                                               P, P, P, P]),
+        "orc_brick_backward_f64_mt": (I, [I, P, U, P, P, U, I, P, P, P, P, I, I, D, D, P, P,
+                                          P]),
+        "orc_brick_render_f64_rect": (I, [P, U, P, P, U, I, P, P, P, P, I, I, D, D, I, I, I, I,
+                                          P, P]),
+        "orc_brick_render_f64_f32ray_rect": (I, [P, U, P, P, U, I, P, P, P, P, I, I, D, D, I, I,
+                                                 I, I, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -162,11 +174,18 @@ def svo_render(nodes_u32, root, attrs_u8, pos, dir_, up, fov, width, height, lig
 
 
 @_keeps
-def svo_hits_f64(nodes_u32, root, pos, dir_, up, fov, width, height, rows=None):
+def svo_hits_f64(nodes_u32, root, pos, dir_, up, fov, width, height, rows=None, threads=1):
     nodes_u32 = np.ascontiguousarray(nodes_u32, dtype=np.uint32)
     n = width * height
     hit = np.full(n, 0xFFFFFFFF, np.uint32)
     t = np.zeros(n, np.float64)
+    if threads > 1 and rows is None:
+        st = lib().orc_svo_hits_f64_mt(int(threads), _p(nodes_u32), len(nodes_u32) // 10, root,
+                                       _p(f64(pos)), _p(f64(dir_)), _p(f64(up)), float(fov),
+                                       width, height, _p(hit), _p(t))
+        if st != 0:
+            raise RuntimeError(f"oracle f64 hits failed: {st}")
+        return hit.reshape(height, width), t.reshape(height, width)
     y0, y1 = (0, height) if rows is None else rows
     st = lib().orc_svo_hits_f64(_p(nodes_u32), len(nodes_u32) // 10, root, _p(f64(pos)),
                                 _p(f64(dir_)), _p(f64(up)), float(fov), width, height, y0, y1,
@@ -174,6 +193,43 @@ def svo_hits_f64(nodes_u32, root, pos, dir_, up, fov, width, height, rows=None):
     if st != 0:
         raise RuntimeError(f"oracle f64 hits failed: {st}")
     return hit.reshape(height, width), t.reshape(height, width)
+
+
+@_keeps
+def svo_hits_f64_f32ray(nodes_u32, root, pos, dir_, up, fov, width, height, threads=1):
+    """FP64 traversal of the FP32 primary rays (hits differ from the float
+    traversal only where a rounding tie inside the traversal decides)."""
+    nodes_u32 = np.ascontiguousarray(nodes_u32, dtype=np.uint32)
+    d0, du, dv = init_ray_dir_f32(dir_, up, fov, width, height)
+    n = width * height
+    hit = np.full(n, 0xFFFFFFFF, np.uint32)
+    t = np.zeros(n, np.float64)
+    st = lib().orc_svo_hits_f64_f32ray_mt(max(1, int(threads)), _p(nodes_u32),
+                                          len(nodes_u32) // 10, root, _p(f32(pos)), _p(d0),
+                                          _p(du), _p(dv), width, height, _p(hit), _p(t))
+    if st != 0:
+        raise RuntimeError(f"oracle f64 hits failed: {st}")
+    return hit.reshape(height, width), t.reshape(height, width)
+
+
+@_keeps
+def brick_backward_f64_f32ray(grids, density, albedo, levels, pos, dir_, up, fov, width,
+                              height, grad_rgba, alpha_scale=1.0, step_vox=0.5, threads=1):
+    """FP64 adjoint along the FP32 primary rays (the rays the CUDA path
+    casts); pool layout, apron slots holding their own share."""
+    g, d, a = _vol_arrays(grids, density, albedo)
+    d0, du, dv = init_ray_dir_f32(dir_, up, fov, width, height)
+    gr = np.ascontiguousarray(np.asarray(grad_rgba, np.float64).reshape(-1))
+    gd = np.zeros(len(d), np.float64)
+    ga = np.zeros(len(a), np.float64)
+    st = lib().orc_brick_backward_f64_f32ray_mt(max(1, int(threads)), _p(g), len(g) // 64,
+                                                _p(d), _p(a), len(d) // 729, levels,
+                                                _p(f32(pos)), _p(d0), _p(du), _p(dv), width,
+                                                height, float(alpha_scale), float(step_vox),
+                                                _p(gr), _p(gd), _p(ga))
+    if st != 0:
+        raise RuntimeError(f"oracle brick backward failed: {st}")
+    return gd, ga
 
 
 @_keeps
@@ -262,14 +318,23 @@ def brick_render_f32_mt(grids, density, albedo, levels, pos, dir_, up, fov, widt
 
 @_keeps
 def brick_backward_f64(grids, density, albedo, levels, pos, dir_, up, fov, width, height,
-                       grad_rgba, alpha_scale=1.0, step_vox=0.5):
+                       grad_rgba, alpha_scale=1.0, step_vox=0.5, threads=1):
     """FP64 adjoint: returns (grad_density (nb*729), grad_albedo (nb*729*3))
-    in pool layout, apron slots holding their own share."""
+    in pool layout, apron slots holding their own share.  threads > 1: row-
+    parallel, per-thread accumulators summed in thread order."""
     g, d, a = _vol_arrays(grids, density, albedo)
     d0, du, dv = init_ray_dir_f64(dir_, up, fov, width, height)
     gr = np.ascontiguousarray(np.asarray(grad_rgba, np.float64).reshape(-1))
     gd = np.zeros(len(d), np.float64)
     ga = np.zeros(len(a), np.float64)
+    if threads > 1:
+        st = lib().orc_brick_backward_f64_mt(int(threads), _p(g), len(g) // 64, _p(d), _p(a),
+                                             len(d) // 729, levels, _p(f64(pos)), _p(d0),
+                                             _p(du), _p(dv), width, height, float(alpha_scale),
+                                             float(step_vox), _p(gr), _p(gd), _p(ga))
+        if st != 0:
+            raise RuntimeError(f"oracle brick backward failed: {st}")
+        return gd, ga
     st = lib().orc_brick_backward_f64(_p(g), len(g) // 64, _p(d), _p(a), len(d) // 729, levels,
                                       _p(f64(pos)), _p(d0), _p(du), _p(dv), width, height,
                                       float(alpha_scale), float(step_vox), _p(gr), _p(gd), _p(ga))
@@ -280,22 +345,77 @@ def brick_backward_f64(grids, density, albedo, levels, pos, dir_, up, fov, width
 
 @_keeps
 def brick_render_f64_f32ray(grids, density, albedo, levels, pos, dir_, up, fov, width, height,
-                            alpha_scale=1.0, step_vox=0.5, rows=None):
+                            alpha_scale=1.0, step_vox=0.5, rows=None, threads=1, ties=False):
     """FP64 march of the FP32-generated primary rays (the rays the CUDA path
-    casts), so the comparison measures the march arithmetic alone."""
+    casts), so the comparison measures the march arithmetic alone.  Returns
+    (rgba, samples, bricks), and with ties=True also the per-ray flag of a
+    sample set or early exit decided by a rounding tie (yv_oracle.h)."""
     g, d, a = _vol_arrays(grids, density, albedo)
     d0, du, dv = init_ray_dir_f32(dir_, up, fov, width, height)
     rgba = np.zeros(width * height * 4, np.float64)
     ns = np.zeros(width * height, np.uint32)
     nb = np.zeros(width * height, np.uint32)
-    y0, y1 = (0, height) if rows is None else rows
-    st = lib().orc_brick_render_f64_f32ray(_p(g), len(g) // 64, _p(d), _p(a), len(d) // 729,
-                                           levels, _p(f32(pos)), _p(d0), _p(du), _p(dv), width,
-                                           height, float(alpha_scale), float(step_vox), y0, y1,
-                                           _p(rgba), _p(ns), _p(nb))
+    tf = np.zeros(width * height, np.uint8)
+    if threads > 1 and rows is None:
+        st = lib().orc_brick_render_f64_f32ray_mt(int(threads), _p(g), len(g) // 64, _p(d),
+                                                  _p(a), len(d) // 729, levels, _p(f32(pos)),
+                                                  _p(d0), _p(du), _p(dv), width, height,
+                                                  float(alpha_scale), float(step_vox),
+                                                  _p(rgba), _p(ns), _p(nb), _p(tf))
+    else:
+        y0, y1 = (0, height) if rows is None else rows
+        st = lib().orc_brick_render_f64_f32ray(_p(g), len(g) // 64, _p(d), _p(a),
+                                               len(d) // 729, levels, _p(f32(pos)), _p(d0),
+                                               _p(du), _p(dv), width, height,
+                                               float(alpha_scale), float(step_vox), y0, y1,
+                                               _p(rgba), _p(ns), _p(nb), _p(tf))
     if st != 0:
         raise RuntimeError(f"oracle brick render failed: {st}")
-    return rgba.reshape(height, width, 4), ns.reshape(height, width), nb.reshape(height, width)
+    out = (rgba.reshape(height, width, 4), ns.reshape(height, width), nb.reshape(height, width))
+    return out + (tf.reshape(height, width).astype(bool),) if ties else out
+
+
+class BrickWindow:
+    """FP64 march of pixel windows of one camera over a volume whose arrays
+    are modified in place between calls (central differences).  Holds the
+    float32 copies the oracle reads; `density` / `albedo` are those arrays."""
+
+    def __init__(self, grids, density, albedo, levels, pos, dir_, up, fov, width, height,
+                 alpha_scale=1.0, step_vox=0.5, f32ray=False):
+        self.g, self.density, self.albedo = _vol_arrays(grids, density, albedo)
+        self.density = self.density.copy()
+        self.albedo = self.albedo.copy()
+        self.levels, self.width, self.height = levels, width, height
+        # f32ray: the FP32 primary rays (as the CUDA path casts them), promoted
+        self.f32ray = bool(f32ray)
+        if self.f32ray:
+            self.pos = f32(pos)
+            self.d0, self.du, self.dv = init_ray_dir_f32(dir_, up, fov, width, height)
+        else:
+            self.pos = f64(pos)
+            self.d0, self.du, self.dv = init_ray_dir_f64(dir_, up, fov, width, height)
+        self.alpha_scale, self.step_vox = float(alpha_scale), float(step_vox)
+        self.rgba = np.zeros(width * height * 4, np.float64)
+        self.samples = np.zeros(width * height, np.uint32)
+
+    def render(self, x0, x1, y0, y1):
+        """(y1-y0, x1-x0, 4) radiance of the window; the samples each ray took
+        are left in self.samples (full-frame, row-major)."""
+        fn = (lib().orc_brick_render_f64_f32ray_rect if self.f32ray
+              else lib().orc_brick_render_f64_rect)
+        st = fn(
+            self.g.ctypes.data, len(self.g) // 64, self.density.ctypes.data,
+            self.albedo.ctypes.data, len(self.density) // 729, self.levels,
+            self.pos.ctypes.data, self.d0.ctypes.data, self.du.ctypes.data,
+            self.dv.ctypes.data, self.width, self.height, self.alpha_scale, self.step_vox,
+            x0, x1, y0, y1, self.rgba.ctypes.data, self.samples.ctypes.data)
+        if st != 0:
+            raise RuntimeError(f"oracle brick window failed: {st}")
+        return self.rgba.reshape(self.height, self.width, 4)[y0:y1, x0:x1].copy()
+
+    def window_samples(self, x0, x1, y0, y1):
+        """Samples per ray of the last render of the window."""
+        return self.samples.reshape(self.height, self.width)[y0:y1, x0:x1].copy()
 
 
 def svo_build_dense(density, depth, iso=0.0, rgb=None):

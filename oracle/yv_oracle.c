@@ -389,7 +389,7 @@ int orc_brick_render_f64_f32ray(const uint32_t* grids, uint32_t ngrids,
                                 const float dv[3], int width, int height,
                                 double alpha_scale, double step_vox, int y0,
                                 int y1, double* rgba, uint32_t* samples,
-                                uint32_t* bricks) {
+                                uint32_t* bricks, uint8_t* ties) {
   brick_ctx_f64 c;
   if (brick_ctx_init_f64(&c, grids, ngrids, density, albedo, nbricks, levels,
                          alpha_scale, step_vox))
@@ -412,6 +412,7 @@ int orc_brick_render_f64_f32ray(const uint32_t* grids, uint32_t ngrids,
         for (int i = 0; i < 4; ++i) rgba[off * 4 + (size_t)i] = out[i];
       if (samples) samples[off] = ns;
       if (bricks) bricks[off] = nbk;
+      if (ties) ties[off] = (uint8_t)c.tie;
     }
   return 0;
 }
@@ -485,4 +486,360 @@ int orc_brick_backward_f64(const uint32_t* grids, uint32_t ngrids,
       if (st) return st;
     }
   return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Row-parallel drivers for full-size checks (POSIX threads, interleaved    */
+/* rows; every thread owns its own context and, for the adjoint, its own    */
+/* gradient accumulators, summed in thread order at the end, so the result  */
+/* depends only on nthreads)                                                */
+/* ------------------------------------------------------------------------ */
+typedef int (*row_fn)(void* ctx, int y, int tid);
+typedef struct {
+  row_fn fn;
+  void* ctx;
+  int tid, nthreads, height, status;
+} row_job;
+
+static void* row_main(void* arg) {
+  row_job* j = (row_job*)arg;
+  for (int y = j->tid; y < j->height && !j->status; y += j->nthreads)
+    j->status = j->fn(j->ctx, y, j->tid);
+  return NULL;
+}
+
+static int run_rows(int nthreads, int height, row_fn fn, void* ctx) {
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  row_job* jobs = (row_job*)calloc((size_t)nthreads, sizeof(row_job));
+  pthread_t* th = (pthread_t*)calloc((size_t)nthreads, sizeof(pthread_t));
+  char* created = (char*)calloc((size_t)nthreads, 1);
+  if (!jobs || !th || !created) {
+    free(jobs);
+    free(th);
+    free(created);
+    return 7;
+  }
+  int st = 0;
+  for (int i = 0; i < nthreads; ++i) {
+    jobs[i].fn = fn;
+    jobs[i].ctx = ctx;
+    jobs[i].tid = i;
+    jobs[i].nthreads = nthreads;
+    jobs[i].height = height;
+    created[i] = pthread_create(&th[i], NULL, row_main, &jobs[i]) == 0;
+  }
+  for (int i = 0; i < nthreads; ++i) {
+    if (created[i])
+      pthread_join(th[i], NULL);
+    else
+      row_main(&jobs[i]);
+    if (jobs[i].status && !st) st = jobs[i].status;
+  }
+  free(jobs);
+  free(th);
+  free(created);
+  return st;
+}
+
+/* ---- FP64 traversal of the FP32 primary rays: directions generated as
+ * the float path generates them (InitRayDir, RenderRect, AdjustDir in
+ * float), promoted, then traced in double; rays whose hit differs from the
+ * float traversal are the rays a rounding tie inside the traversal decides */
+int orc_svo_hits_f64_f32ray(const uint32_t* nodes, uint32_t count, uint32_t root,
+                            const float pos[3], const float dir0[3], const float du[3],
+                            const float dv[3], int width, int height, int y0, int y1,
+                            uint32_t* hit, double* hit_t) {
+  if (y0 < 0) y0 = 0;
+  if (y1 > height) y1 = height;
+  const double o[3] = {pos[0], pos[1], pos[2]};
+  for (int y = y0; y < y1; ++y)
+    for (int x = 0; x < width; ++x) {
+      size_t off = (size_t)y * (size_t)width + (size_t)x;
+      float df[3];
+      pixel_dir_f32(dir0, du, dv, x, y, df);
+      adjust_dir_f32(df);
+      double d[3] = {df[0], df[1], df[2]};
+      trace_ctx_f64 c = {nodes, count, 0, 0, 0};
+      hit_rec_f64 h;
+      int ok = trace_one_f64(&c, root, o, d, &h, 0);
+      if (c.err) return c.err;
+      if (hit) hit[off] = ok ? ((h.node << 3) | (uint32_t)h.child) : 0xFFFFFFFFu;
+      if (hit_t) hit_t[off] = ok ? h.t : 0.0;
+    }
+  return 0;
+}
+
+typedef struct {
+  const uint32_t* nodes;
+  uint32_t count, root;
+  const float *pos, *dir0, *du, *dv;
+  int width, height;
+  uint32_t* hit;
+  double* hit_t;
+} hits32_job;
+
+static int hits32_row(void* ctx, int y, int tid) {
+  (void)tid;
+  hits32_job* j = (hits32_job*)ctx;
+  return orc_svo_hits_f64_f32ray(j->nodes, j->count, j->root, j->pos, j->dir0, j->du, j->dv,
+                                 j->width, j->height, y, y + 1, j->hit, j->hit_t);
+}
+
+/* ---- FP64 primary hits on threads ---- */
+typedef struct {
+  const uint32_t* nodes;
+  uint32_t count, root;
+  const double *pos, *dir, *up;
+  double fov;
+  int width, height;
+  uint32_t* hit;
+  double* hit_t;
+} hits_job;
+
+static int hits_row(void* ctx, int y, int tid) {
+  (void)tid;
+  hits_job* j = (hits_job*)ctx;
+  return orc_svo_hits_f64(j->nodes, j->count, j->root, j->pos, j->dir, j->up, j->fov,
+                          j->width, j->height, y, y + 1, j->hit, j->hit_t);
+}
+
+int orc_svo_hits_f64_f32ray_mt(int nthreads, const uint32_t* nodes, uint32_t count,
+                               uint32_t root, const float pos[3], const float dir0[3],
+                               const float du[3], const float dv[3], int width, int height,
+                               uint32_t* hit, double* hit_t) {
+  hits32_job j = {nodes, count, root, pos, dir0, du, dv, width, height, hit, hit_t};
+  return run_rows(nthreads, height, hits32_row, &j);
+}
+
+int orc_svo_hits_f64_mt(int nthreads, const uint32_t* nodes, uint32_t count,
+                        uint32_t root, const double pos[3], const double dir[3],
+                        const double up[3], double fov_deg, int width,
+                        int height, uint32_t* hit, double* hit_t) {
+  hits_job j = {nodes, count, root, pos, dir, up, fov_deg, width, height, hit, hit_t};
+  return run_rows(nthreads, height, hits_row, &j);
+}
+
+/* ---- FP64 march of the FP32 primary rays on threads ---- */
+typedef struct {
+  const uint32_t* grids;
+  uint32_t ngrids;
+  const float *density, *albedo;
+  uint32_t nbricks;
+  int levels;
+  const float *pos, *dir0, *du, *dv;
+  int width, height;
+  double alpha_scale, step_vox;
+  double* rgba;
+  uint32_t *samples, *bricks;
+  uint8_t* ties;
+} march32_job;
+
+static int march32_row(void* ctx, int y, int tid) {
+  (void)tid;
+  march32_job* j = (march32_job*)ctx;
+  return orc_brick_render_f64_f32ray(j->grids, j->ngrids, j->density, j->albedo, j->nbricks,
+                                     j->levels, j->pos, j->dir0, j->du, j->dv, j->width,
+                                     j->height, j->alpha_scale, j->step_vox, y, y + 1,
+                                     j->rgba, j->samples, j->bricks, j->ties);
+}
+
+int orc_brick_render_f64_f32ray_mt(int nthreads, const uint32_t* grids, uint32_t ngrids,
+                                   const float* density, const float* albedo,
+                                   uint32_t nbricks, int levels, const float pos[3],
+                                   const float dir0[3], const float du[3],
+                                   const float dv[3], int width, int height,
+                                   double alpha_scale, double step_vox, double* rgba,
+                                   uint32_t* samples, uint32_t* bricks, uint8_t* ties) {
+  march32_job j = {grids, ngrids, density, albedo, nbricks, levels, pos, dir0, du, dv,
+                   width, height, alpha_scale, step_vox, rgba, samples, bricks, ties};
+  return run_rows(nthreads, height, march32_row, &j);
+}
+
+/* ---- FP64 march of a pixel window [x0, x1) x [y0, y1) (FP64 rays, as
+ * orc_brick_render_f64 and the FP64 adjoint cast them) ---- */
+int orc_brick_render_f64_rect(const uint32_t* grids, uint32_t ngrids,
+                              const float* density, const float* albedo,
+                              uint32_t nbricks, int levels, const double pos[3],
+                              const double dir0[3], const double du[3],
+                              const double dv[3], int width, int height,
+                              double alpha_scale, double step_vox, int x0, int x1,
+                              int y0, int y1, double* rgba, uint32_t* samples) {
+  brick_ctx_f64 c;
+  if (brick_ctx_init_f64(&c, grids, ngrids, density, albedo, nbricks, levels,
+                         alpha_scale, step_vox))
+    return 1;
+  if (x0 < 0) x0 = 0;
+  if (y0 < 0) y0 = 0;
+  if (x1 > width) x1 = width;
+  if (y1 > height) y1 = height;
+  for (int y = y0; y < y1; ++y)
+    for (int x = x0; x < x1; ++x) {
+      size_t off = (size_t)y * (size_t)width + (size_t)x;
+      double d[3];
+      pixel_dir_f64(dir0, du, dv, x, y, d);
+      adjust_dir_f64(d);
+      double out[4];
+      uint32_t ns = 0;
+      int st = brick_march_f64(&c, pos, d, out, &ns, 0, 0, 0);
+      if (st) return st;
+      for (int i = 0; i < 4; ++i) rgba[off * 4 + (size_t)i] = out[i];
+      if (samples) samples[off] = ns;
+    }
+  return 0;
+}
+
+int orc_brick_render_f64_f32ray_rect(const uint32_t* grids, uint32_t ngrids,
+                                     const float* density, const float* albedo,
+                                     uint32_t nbricks, int levels, const float pos[3],
+                                     const float dir0[3], const float du[3],
+                                     const float dv[3], int width, int height,
+                                     double alpha_scale, double step_vox, int x0, int x1,
+                                     int y0, int y1, double* rgba, uint32_t* samples) {
+  brick_ctx_f64 c;
+  if (brick_ctx_init_f64(&c, grids, ngrids, density, albedo, nbricks, levels,
+                         alpha_scale, step_vox))
+    return 1;
+  if (x0 < 0) x0 = 0;
+  if (y0 < 0) y0 = 0;
+  if (x1 > width) x1 = width;
+  if (y1 > height) y1 = height;
+  const double o[3] = {pos[0], pos[1], pos[2]};
+  for (int y = y0; y < y1; ++y)
+    for (int x = x0; x < x1; ++x) {
+      size_t off = (size_t)y * (size_t)width + (size_t)x;
+      float df[3];
+      pixel_dir_f32(dir0, du, dv, x, y, df);
+      adjust_dir_f32(df);
+      double d[3] = {df[0], df[1], df[2]};
+      double out[4];
+      uint32_t ns = 0;
+      int st = brick_march_f64(&c, o, d, out, &ns, 0, 0, 0);
+      if (st) return st;
+      for (int i = 0; i < 4; ++i) rgba[off * 4 + (size_t)i] = out[i];
+      if (samples) samples[off] = ns;
+    }
+  return 0;
+}
+
+/* ---- FP64 adjoint on threads ---- */
+typedef struct {
+  brick_ctx_f64 proto;
+  const double *pos, *dir0, *du, *dv;
+  /* FP32 rays (orc_brick_backward_f64_f32ray_mt): float basis, or NULL */
+  const float *fdir0, *fdu, *fdv;
+  int width;
+  double alpha_scale;
+  const double* grad_rgba;
+  double** gd;  /* per-thread accumulators */
+  double** ga;
+} bwd_job;
+
+static int bwd_row(void* ctx, int y, int tid) {
+  bwd_job* j = (bwd_job*)ctx;
+  brick_ctx_f64 c = j->proto;
+  for (int x = 0; x < j->width; ++x) {
+    size_t off = (size_t)y * (size_t)j->width + (size_t)x;
+    double d[3];
+    if (j->fdir0) {
+      float df[3];
+      pixel_dir_f32(j->fdir0, j->fdu, j->fdv, x, y, df);
+      adjust_dir_f32(df);
+      d[0] = df[0];
+      d[1] = df[1];
+      d[2] = df[2];
+    } else {
+      pixel_dir_f64(j->dir0, j->du, j->dv, x, y, d);
+      adjust_dir_f64(d);
+    }
+    double out[4];
+    int st = brick_march_f64(&c, j->pos, d, out, 0, 0, 0, 0);
+    if (st) return st;
+    bwd_user u = {j->grad_rgba + off * 4, out, j->alpha_scale, j->gd[tid], j->ga[tid]};
+    double out2[4];
+    st = brick_march_f64(&c, j->pos, d, out2, 0, 0, bwd_sample, &u);
+    if (st) return st;
+  }
+  return 0;
+}
+
+static int backward_mt(int nthreads, bwd_job* jp, const uint32_t* grids, uint32_t ngrids,
+                       const float* density, const float* albedo, uint32_t nbricks,
+                       int levels, int width, int height, double alpha_scale,
+                       double step_vox, const double* grad_rgba, double* grad_density,
+                       double* grad_albedo);
+
+int orc_brick_backward_f64_mt(int nthreads, const uint32_t* grids, uint32_t ngrids,
+                              const float* density, const float* albedo,
+                              uint32_t nbricks, int levels, const double pos[3],
+                              const double dir0[3], const double du[3],
+                              const double dv[3], int width, int height,
+                              double alpha_scale, double step_vox,
+                              const double* grad_rgba, double* grad_density,
+                              double* grad_albedo) {
+  bwd_job j;
+  memset(&j, 0, sizeof(j));
+  j.pos = pos;
+  j.dir0 = dir0;
+  j.du = du;
+  j.dv = dv;
+  return backward_mt(nthreads, &j, grids, ngrids, density, albedo, nbricks, levels, width,
+                     height, alpha_scale, step_vox, grad_rgba, grad_density, grad_albedo);
+}
+
+int orc_brick_backward_f64_f32ray_mt(int nthreads, const uint32_t* grids, uint32_t ngrids,
+                                     const float* density, const float* albedo,
+                                     uint32_t nbricks, int levels, const float pos[3],
+                                     const float dir0[3], const float du[3],
+                                     const float dv[3], int width, int height,
+                                     double alpha_scale, double step_vox,
+                                     const double* grad_rgba, double* grad_density,
+                                     double* grad_albedo) {
+  bwd_job j;
+  memset(&j, 0, sizeof(j));
+  const double o[3] = {pos[0], pos[1], pos[2]};
+  j.pos = o;
+  j.fdir0 = dir0;
+  j.fdu = du;
+  j.fdv = dv;
+  return backward_mt(nthreads, &j, grids, ngrids, density, albedo, nbricks, levels, width,
+                     height, alpha_scale, step_vox, grad_rgba, grad_density, grad_albedo);
+}
+
+static int backward_mt(int nthreads, bwd_job* jp, const uint32_t* grids, uint32_t ngrids,
+                       const float* density, const float* albedo, uint32_t nbricks,
+                       int levels, int width, int height, double alpha_scale,
+                       double step_vox, const double* grad_rgba, double* grad_density,
+                       double* grad_albedo) {
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  bwd_job j = *jp;
+  if (brick_ctx_init_f64(&j.proto, grids, ngrids, density, albedo, nbricks, levels,
+                         alpha_scale, step_vox))
+    return 1;
+  const size_t nd = (size_t)nbricks * 729u, na = nd * 3u;
+  j.width = width;
+  j.alpha_scale = alpha_scale;
+  j.grad_rgba = grad_rgba;
+  j.gd = (double**)calloc((size_t)nthreads, sizeof(double*));
+  j.ga = (double**)calloc((size_t)nthreads, sizeof(double*));
+  int st = (j.gd && j.ga) ? 0 : 7;
+  for (int i = 0; i < nthreads && !st; ++i) {
+    j.gd[i] = (double*)calloc(nd ? nd : 1, sizeof(double));
+    j.ga[i] = (double*)calloc(na ? na : 1, sizeof(double));
+    if (!j.gd[i] || !j.ga[i]) st = 7;
+  }
+  if (!st) st = run_rows(nthreads, height, bwd_row, &j);
+  if (!st)
+    for (int i = 0; i < nthreads; ++i) {
+      for (size_t k = 0; k < nd; ++k) grad_density[k] += j.gd[i][k];
+      for (size_t k = 0; k < na; ++k) grad_albedo[k] += j.ga[i][k];
+    }
+  for (int i = 0; i < nthreads; ++i) {
+    if (j.gd) free(j.gd[i]);
+    if (j.ga) free(j.ga[i]);
+  }
+  free(j.gd);
+  free(j.ga);
+  return st;
 }

@@ -122,7 +122,13 @@ int orc_brick_render_f64(const uint32_t* grids, uint32_t ngrids,
                          const double dv[3], int width, int height,
                          double alpha_scale, double step_vox, int y0, int y1,
                          double* rgba, uint32_t* samples, uint32_t* bricks);
-/* FP64 march of the FP32-generated primary rays (float camera basis). */
+/* FP64 march of the FP32-generated primary rays (float camera basis).
+ * ties (optional): 1 where the ray's sample set or its early exit is decided
+ * by a rounding tie - a sample within 1e-6 (relative) of a cell boundary,
+ * two exit planes of a cell within 1e-6 of each other, the entry cell's
+ * coordinate within 1e-6 of an integer, or the opacity within 1e-5 of the
+ * 0.99 early-exit threshold after a sample - so that an FP32 march may take
+ * a different sample set. */
 int orc_brick_render_f64_f32ray(const uint32_t* grids, uint32_t ngrids,
                                 const float* density, const float* albedo,
                                 uint32_t nbricks, int levels, const float pos[3],
@@ -130,7 +136,7 @@ int orc_brick_render_f64_f32ray(const uint32_t* grids, uint32_t ngrids,
                                 const float dv[3], int width, int height,
                                 double alpha_scale, double step_vox, int y0,
                                 int y1, double* rgba, uint32_t* samples,
-                                uint32_t* bricks);
+                                uint32_t* bricks, uint8_t* ties);
 int orc_brick_render_f32(const uint32_t* grids, uint32_t ngrids,
                          const float* density, const float* albedo,
                          uint32_t nbricks, int levels, const float pos[3],
@@ -157,6 +163,72 @@ int orc_brick_backward_f64(const uint32_t* grids, uint32_t ngrids,
                            double alpha_scale, double step_vox,
                            const double* grad_rgba, double* grad_density,
                            double* grad_albedo);
+
+/* Row-parallel forms of the checks above, for full-size frames: interleaved
+ * rows on nthreads POSIX threads, each with its own context.  The adjoint
+ * keeps per-thread gradient accumulators and adds them into grad_density /
+ * grad_albedo in thread order (deterministic for a given nthreads). */
+int orc_svo_hits_f64_mt(int nthreads, const uint32_t* nodes, uint32_t count,
+                        uint32_t root, const double pos[3], const double dir[3],
+                        const double up[3], double fov_deg, int width,
+                        int height, uint32_t* hit, double* hit_t);
+int orc_brick_render_f64_f32ray_mt(int nthreads, const uint32_t* grids, uint32_t ngrids,
+                                   const float* density, const float* albedo,
+                                   uint32_t nbricks, int levels, const float pos[3],
+                                   const float dir0[3], const float du[3],
+                                   const float dv[3], int width, int height,
+                                   double alpha_scale, double step_vox, double* rgba,
+                                   uint32_t* samples, uint32_t* bricks, uint8_t* ties);
+int orc_brick_backward_f64_mt(int nthreads, const uint32_t* grids, uint32_t ngrids,
+                              const float* density, const float* albedo,
+                              uint32_t nbricks, int levels, const double pos[3],
+                              const double dir0[3], const double du[3],
+                              const double dv[3], int width, int height,
+                              double alpha_scale, double step_vox,
+                              const double* grad_rgba, double* grad_density,
+                              double* grad_albedo);
+/* The same checks over the FP32 primary rays (float camera basis, as the
+ * CUDA path generates them) promoted to double: the FP64 traversal of those
+ * rays (its hits differ from the float traversal only where a rounding tie
+ * inside the traversal decides the hit) and the FP64 adjoint of the march
+ * along them. */
+int orc_svo_hits_f64_f32ray(const uint32_t* nodes, uint32_t count, uint32_t root,
+                            const float pos[3], const float dir0[3], const float du[3],
+                            const float dv[3], int width, int height, int y0, int y1,
+                            uint32_t* hit, double* hit_t);
+int orc_svo_hits_f64_f32ray_mt(int nthreads, const uint32_t* nodes, uint32_t count,
+                               uint32_t root, const float pos[3], const float dir0[3],
+                               const float du[3], const float dv[3], int width, int height,
+                               uint32_t* hit, double* hit_t);
+int orc_brick_backward_f64_f32ray_mt(int nthreads, const uint32_t* grids, uint32_t ngrids,
+                                     const float* density, const float* albedo,
+                                     uint32_t nbricks, int levels, const float pos[3],
+                                     const float dir0[3], const float du[3],
+                                     const float dv[3], int width, int height,
+                                     double alpha_scale, double step_vox,
+                                     const double* grad_rgba, double* grad_density,
+                                     double* grad_albedo);
+/* FP64 march (FP64 rays, as orc_brick_render_f64) of the pixel window
+ * [x0, x1) x [y0, y1) only; rgba (4 doubles per pixel) and samples (optional,
+ * samples taken per ray) are full-frame arrays, pixels outside the window
+ * are left untouched.  Used for central
+ * differences, where a lattice point reaches only the rays of a few pixels. */
+int orc_brick_render_f64_rect(const uint32_t* grids, uint32_t ngrids,
+                              const float* density, const float* albedo,
+                              uint32_t nbricks, int levels, const double pos[3],
+                              const double dir0[3], const double du[3],
+                              const double dv[3], int width, int height,
+                              double alpha_scale, double step_vox, int x0, int x1,
+                              int y0, int y1, double* rgba, uint32_t* samples);
+
+/* The same window over the FP32 primary rays promoted to double. */
+int orc_brick_render_f64_f32ray_rect(const uint32_t* grids, uint32_t ngrids,
+                                     const float* density, const float* albedo,
+                                     uint32_t nbricks, int levels, const float pos[3],
+                                     const float dir0[3], const float du[3],
+                                     const float dv[3], int width, int height,
+                                     double alpha_scale, double step_vox, int x0, int x1,
+                                     int y0, int y1, double* rgba, uint32_t* samples);
 
 /* SVO build from a dense density grid (yv_oracle_build.c): 2^depth grid,
  * solid = density > iso, canonical breadth-first pool (nodes: 10 uint32 per

@@ -247,6 +247,12 @@ typedef struct {
   REAL dt;         /* world-space step = step_vox / S */
   REAL inv_dt;
   int err;
+  /* set by brick_march when the ray's sample set or its early exit is
+   * decided by a rounding tie: a sample within TIE_T (relative) of a cell
+   * boundary, two exit planes of a cell within TIE_T of each other, the
+   * entry cell's coordinate within TIE_T of an integer, or the opacity
+   * within TIE_A of the early-exit threshold after a sample */
+  int tie;
 } FN(brick_ctx);
 
 /* Tree descent for brick cell c (ntree/ntree/nodes.h:56-99 child offsets
@@ -319,10 +325,22 @@ typedef void (*FN(sample_fn))(void* user, const uint32_t* idx, const REAL* w,
                               REAL sigma, const REAL* col, REAL alpha,
                               REAL acc_a_before, const REAL* acc_c_before);
 
+#ifndef YV_ORC_TIES
+#define YV_ORC_TIES
+#define TIE_T 1e-6
+#define TIE_A 1e-5
+#endif
+static inline int FN(near_rel)(REAL a, REAL b) {
+  REAL d = a - b, m = a < 0 ? -a : a;
+  if (d < 0) d = -d;
+  return d <= (REAL)TIE_T * (m > (REAL)1e-3 ? m : (REAL)1e-3);
+}
+
 static int FN(brick_march)(FN(brick_ctx) * c, const REAL* o, const REAL* d,
                            REAL* out, uint32_t* n_samples,
                            uint32_t* n_bricks, FN(sample_fn) fn, void* user) {
   REAL inv[3], t1[3], t2[3];
+  c->tie = 0;
   for (int i = 0; i < 4; ++i) out[i] = 0;
   for (int i = 0; i < 3; ++i) {
     inv[i] = (REAL)1 / d[i];
@@ -339,6 +357,10 @@ static int FN(brick_march)(FN(brick_ctx) * c, const REAL* o, const REAL* d,
   for (int i = 0; i < 3; ++i) {
     REAL q = (o[i] + t_enter * d[i]) / h;
     int k = (int)FLOOR(q);
+    /* near an interior cell plane (the entry face itself is clamped) */
+    if ((k > 0 && k < c->nb && FN(near_rel)(q, (REAL)k)) ||
+        (k + 1 < c->nb && FN(near_rel)(q, (REAL)(k + 1))))
+      c->tie = 1;
     if (k < 0) k = 0;
     if (k > c->nb - 1) k = c->nb - 1;
     cell[i] = k;
@@ -358,13 +380,19 @@ static int FN(brick_march)(FN(brick_ctx) * c, const REAL* o, const REAL* d,
     if (tx[1] < tx[e]) e = 1;
     if (tx[2] < tx[e]) e = 2;
     REAL t_out = tx[e];
+    for (int i = 0; i < 3; ++i)
+      if (i != e && FN(near_rel)(tx[i], t_out)) c->tie = 1;
     int b = FN(brick_lookup)(c, cell);
     if (c->err) return c->err;
     if (b >= 0) {
       ++nbk;
       int64_t k = (int64_t)CEIL(t_in * c->inv_dt);
+      /* the sample just before the cell's first one may fall inside it in
+       * another precision */
+      if (FN(near_rel)((REAL)(k - 1) * c->dt, t_in)) c->tie = 1;
       for (;; ++k) {
         REAL t = (REAL)k * c->dt;
+        if (FN(near_rel)(t, t_in) || FN(near_rel)(t, t_out)) c->tie = 1;
         if (!(t < t_out)) break;
         REAL l[3];  /* brick-local lattice coordinates */
         for (int i = 0; i < 3; ++i)
@@ -386,6 +414,10 @@ static int FN(brick_march)(FN(brick_ctx) * c, const REAL* o, const REAL* d,
         for (int ch = 0; ch < 3; ++ch) acc_c[ch] += wgt * col[ch];
         acc_a += wgt;
         ++ns;
+        {
+          REAL da = acc_a - (REAL)0.99f;
+          if (da < (REAL)TIE_A && da > -(REAL)TIE_A) c->tie = 1;
+        }
         if (acc_a > (REAL)0.99f) {
           done = 1;
           break;

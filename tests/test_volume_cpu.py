@@ -187,3 +187,36 @@ def test_oracle_adjoint_matches_central_differences(oracle, small):
     assert len(refs) > 60 and np.abs(refs).max() > 0 and kinks < len(refs)
     rel = np.linalg.norm(errs) / np.linalg.norm(refs)
     assert rel < 1e-4, rel
+
+
+def test_oracle_adjoint_matches_central_differences_cfg4_volume(oracle, yoxel_mod):
+    """The FP64 adjoint on the full 128^3 differentiable volume (seed 1234)
+    with 4 of its 64 cameras at 256^2 and a seeded dL/drgba, against FP64
+    central differences on 150 seeded lattice points (density and albedo),
+    kinks left out (volume_util.central_differences)."""
+    import os
+    from volume_util import central_differences, gradient_at
+    vol = yoxel_mod.BrickVolume.noise(2, 0.4, 1.4, 1234)
+    cams = [yoxel_mod.sphere_cameras(64)[i] for i in (0, 16, 32, 48)]
+    den = vol.density.astype(np.float32)
+    alb = vol.albedo_u8.astype(np.float32) * np.float32(1.0 / 255.0)
+    w = h = 256
+    rng = np.random.default_rng(11)
+    grads = [rng.standard_normal((h, w, 4)) for _ in cams]
+    threads = max(1, os.cpu_count() or 1)
+    rd = np.zeros(vol.nbricks * 729)
+    ra = np.zeros(vol.nbricks * 729 * 3)
+    for c, g in zip(cams, grads):
+        a, b = oracle.brick_backward_f64(vol.grids, den, alb, vol.levels, *c, w, h, g,
+                                         threads=threads)
+        rd += a
+        ra += b
+    pts = owned_points(vol, np.random.default_rng(1234), 150)
+    fds, kinks = central_differences(oracle, vol, den, alb, cams, grads, w, h, pts)
+    for kind, ch, rg in (("d", 1, rd), ("a", 3, ra)):
+        fd = np.array([f for (_, f, _) in fds[kind]])
+        an = np.array([gradient_at(rg, sl, ch, 0 if kind == "d" else 1)
+                       for (_, _, sl) in fds[kind]])
+        assert len(fd) > 100 and np.abs(fd).max() > 0
+        assert np.linalg.norm(an - fd) / np.linalg.norm(fd) < 1e-4, kind
+    assert kinks < 40

@@ -4,6 +4,7 @@
 // svo_kernels.cu.  No CUDA error aborts: every failure is a yv_status.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -427,6 +428,8 @@ static void fill_frame_args(const yv_renderer* r, SvoFrameArgs& a) {
   a.shadows = r->light.shadows ? 1 : 0;
   a.width = r->width;
   a.height = r->height;
+  a.id_begin = 0;
+  a.id_end = frame_ray_ids(r->width, r->height);
   // SVORenderer::Render: rp.detailCoef = m_detailCoef * (fov / 2 in
   // radians) / width (demo/SVORenderer.cpp:104), in double, rounded once
   a.lod_coef = (r->detail > 0.f && r->scene.node_data)
@@ -449,13 +452,32 @@ bool renderer_view(const yv_renderer* r, yv_renderer_view* v) {
 
 extern "C" {
 
+// Pixels of the frame inside 8x4 tiles [tb, te) (row-major tiles; edge
+// tiles are clipped to the frame).
+static uint64_t tile_range_pixels(int width, int height, uint32_t tb, uint32_t te) {
+  const uint32_t tiles_x = (uint32_t)((width + 7) / 8);
+  uint64_t n = 0;
+  for (uint32_t t = tb; t < te; ++t) {
+    const int x0 = (int)(t % tiles_x) * 8, y0 = (int)(t / tiles_x) * 4;
+    n += (uint64_t)std::min(8, width - x0) * (uint64_t)std::min(4, height - y0);
+  }
+  return n;
+}
+
 // `unlit`: the light is replaced by ambient 1, diffuse 0 and no shadow rays,
-// so rgba carries the hit leaves' albedo.
+// so rgba carries the hit leaves' albedo.  Tiles [tb, te) of the frame
+// (te = UINT32_MAX: the whole frame).
 static yv_status enqueue_frame(yv_renderer* r, const yv_frame_outputs* out, cudaStream_t s,
-                               bool unlit = false) {
+                               bool unlit = false, uint32_t tb = 0,
+                               uint32_t te = 0xFFFFFFFFu) {
   if (!r->has_scene) return YV_ERR_NO_SCENE;
   SvoFrameArgs a;
   fill_frame_args(r, a);
+  const uint32_t ntiles = a.id_end / 32u;
+  if (te > ntiles) te = ntiles;
+  if (tb > te) tb = te;
+  a.id_begin = tb * 32u;
+  a.id_end = te * 32u;
   if (unlit) {
     a.ambient = 1.0f;
     a.diffuse = 0.0f;
@@ -471,7 +493,8 @@ static yv_status enqueue_frame(yv_renderer* r, const yv_frame_outputs* out, cuda
   int launches = 0;
   YV_CUDA(launch_svo_frame(scene_of(r), a, r->cfg, s, &launches), "svo frame launch");
   r->last_stream = s;
-  r->last_pixels = (uint64_t)r->width * (uint64_t)r->height;
+  r->last_pixels = (tb == 0 && te == ntiles) ? (uint64_t)r->width * (uint64_t)r->height
+                                             : tile_range_pixels(r->width, r->height, tb, te);
   r->last_shadows = a.shadows;
   r->last_launches = (uint32_t)launches;
   r->frame_pending = true;
@@ -494,6 +517,23 @@ yv_status yv_render_frame_async(yv_renderer* r, const yv_frame_outputs* out, voi
   if (!r || !out) return YV_ERR_INVALID_ARG;
   YV_CUDA(cudaSetDevice(r->device), "cudaSetDevice");
   return enqueue_frame(r, out, static_cast<cudaStream_t>(stream));
+}
+
+yv_status yv_render_frame_tiles(yv_renderer* r, uint32_t tile_begin, uint32_t tile_end,
+                                const yv_frame_outputs* out, void* stream) {
+  if (!r || !out || tile_begin > tile_end) return YV_ERR_INVALID_ARG;
+  if (!r->has_scene) return YV_ERR_NO_SCENE;
+  const uint32_t ntiles = frame_ray_ids(r->width, r->height) / 32u;
+  if (tile_end > ntiles) return YV_ERR_INVALID_ARG;
+  YV_CUDA(cudaSetDevice(r->device), "cudaSetDevice");
+  return enqueue_frame(r, out, static_cast<cudaStream_t>(stream), false, tile_begin, tile_end);
+}
+
+yv_status yv_get_tile_count(const yv_renderer* r, uint32_t* tiles_x, uint32_t* tiles_y) {
+  if (!r || !tiles_x || !tiles_y) return YV_ERR_INVALID_ARG;
+  *tiles_x = (uint32_t)((r->width + 7) / 8);
+  *tiles_y = (uint32_t)((r->height + 3) / 4);
+  return YV_OK;
 }
 
 yv_status yv_renderer_frame_stats(yv_renderer* r, yv_frame_stats* stats) {

@@ -160,6 +160,18 @@ yv_status yv_batch_clear(yv_batch* b) {
 
 yv_status yv_batch_add_svo(yv_batch* b, const yv_renderer* r, void* d_rgba) {
   if (!b || !r || !d_rgba) return YV_ERR_INVALID_ARG;
+  yv_frame_outputs o;
+  std::memset(&o, 0, sizeof(o));
+  o.rgba = d_rgba;
+  return yv_batch_add_svo_outputs(b, r, &o);
+}
+
+yv_status yv_batch_add_svo_outputs(yv_batch* b, const yv_renderer* r,
+                                   const yv_frame_outputs* out) {
+  if (!b || !r || !out ||
+      !(out->rgba || out->hit || out->hit_t || out->fetches || out->shadow_fetches ||
+        out->normal))
+    return YV_ERR_INVALID_ARG;
   if ((int)b->items.size() >= kMaxBatchItems) return YV_ERR_UNSUPPORTED;
   yv_renderer_view v;
   if (!renderer_view(r, &v)) return YV_ERR_NO_SCENE;
@@ -175,7 +187,12 @@ yv_status yv_batch_add_svo(yv_batch* b, const yv_renderer* r, void* d_rgba) {
   it.tiles = it.tiles_x * (uint32_t)((it.height + 3) / 4);
   it.svo = v.sc;
   it.fa = v.fa;
-  it.fa.rgba = static_cast<uint32_t*>(d_rgba);
+  it.fa.rgba = static_cast<uint32_t*>(out->rgba);
+  it.fa.hit = static_cast<uint32_t*>(out->hit);
+  it.fa.hit_t = static_cast<float*>(out->hit_t);
+  it.fa.fetches = static_cast<uint32_t*>(out->fetches);
+  it.fa.shadow_fetches = static_cast<uint32_t*>(out->shadow_fetches);
+  it.fa.normal = static_cast<float*>(out->normal);
   b->items.push_back(it);
   b->dirty = true;
   return YV_OK;

@@ -9,7 +9,9 @@
 //  * in an occupied cell, samples sit at the global multiples t = k*dt
 //    (trace.cu:47), dt = step_vox lattice cells;
 //  * sample = software FP32 trilinear of density and albedo inside the brick
-//    (the 9^3 apron lattice keeps all 8 corners in the brick);
+//    (the 9^3 apron lattice keeps all 8 corners in the brick), at a position
+//    carried as a float pair (sample_coord) so the trilinear fractions are
+//    accurate to ulp(1);
 //  * alpha = saturate(alpha_scale * density), front-to-back pre-multiplied
 //    accumulation C += (1-A)*alpha*albedo, A += (1-A)*alpha (trace.cu:58),
 //    stop once A > 0.99 (trace.cu:59).
@@ -146,18 +148,42 @@ __device__ __forceinline__ uint32_t corner_offset(int j) {
   return (uint32_t)(((j >> 2) * kL + ((j >> 1) & 1)) * kL + (j & 1));
 }
 
-// lx, ly, lz: brick-local lattice coordinates of the sample, in [0, 8].
+// a + b as an exact float pair s + r (Knuth's TwoSum).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& r) {
+  s = fadd(a, b);
+  const float bb = fsub(s, a);
+  r = fadd(fsub(a, fsub(s, bb)), fsub(b, bb));
+}
+
+// Brick-local lattice coordinate t D + (Lh + Ll) of a sample (in [0, 8]),
+// Lh + Ll the brick-local origin o S - 8c as an exact pair (two_sum: o S is
+// exact, but o S - 8c can need one bit more when it grows a binade), as a
+// float pair l + e: p = t D rounded, e = its exact rounding error (one fma)
+// plus Ll, l = p + Lh.  Once the origin is more than two bricks away, p and
+// -Lh agree to a factor of two and l is exact (Sterbenz), so the fractional
+// position inside the trilinear cell, (l - k) + e, is accurate to ulp(1)
+// instead of ulp(8) or ulp(o S).  (Rounded once to ulp(8), and o S - 8c to
+// ulp(o S), sample points on steep density edges moved low-opacity rays by
+// up to 5e-5 relative.)
+__device__ __forceinline__ void sample_coord(float t, float D, float Lh, float Ll, float& l,
+                                             float& e) {
+  const float p = fmul(t, D);
+  e = fadd(ffma(t, D, -p), Ll);
+  l = fadd(p, Lh);
+}
+
+// l + e: brick-local lattice coordinates of the sample (sample_coord), in
+// [0, 8].
 template <int P>
-__device__ __forceinline__ void eval_sample(const VolumeView& a, int b, float lx, float ly,
-                                            float lz, SampleCtx& s) {
-  float l[3] = {lx, ly, lz};
+__device__ __forceinline__ void eval_sample(const VolumeView& a, int b, const float* l,
+                                            const float* e, SampleCtx& s) {
   int i0[3];
   float f[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     int k = __float2int_rd(l[i]);
     k = k < 0 ? 0 : (k > 7 ? 7 : k);
-    float fi = fsub(l[i], small_int_f(k));
+    float fi = fadd(fsub(l[i], small_int_f(k)), e[i]);
     fi = fi < 0.f ? 0.f : (fi > 1.f ? 1.f : fi);
     i0[i] = k;
     f[i] = fi;
@@ -296,18 +322,22 @@ __device__ __forceinline__ void march(const VolumeView& a, const uint32_t* sg, u
     }
     if (b >= 0) {
       ++r.bricks;
-      // Q - 8c is exact (8c is a multiple of ulp(Q)), so fma(t, D, Q - 8c)
-      // rounds the brick-local coordinate in [0, 8] once: the sample point
-      // is accurate to ulp(8) instead of ulp(|Q|).
-      const float L0 = fsub(kColor ? Q[0] : fmul(o[0], a.S), (float)(8 * cell[0]));
-      const float L1 = fsub(kColor ? Q[1] : fmul(o[1], a.S), (float)(8 * cell[1]));
-      const float L2 = fsub(kColor ? Q[2] : fmul(o[2], a.S), (float)(8 * cell[2]));
+      // the brick-local origin Q - 8c as an exact pair: the brick-local
+      // coordinate t D + (Q - 8c) in [0, 8] is formed without the rounding
+      // of |Q| (sample_coord)
+      float Lh[3], Ll[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+        two_sum(kColor ? Q[i] : fmul(o[i], a.S), -(float)(8 * cell[i]), Lh[i], Ll[i]);
       int k = __float2int_ru(fmul(t_in, a.inv_dt));
       for (int it = 0; it < 1 << 16; ++it, ++k) {
         const float t = fmul((float)k, a.dt);
         if (!(t < t_out)) break;
         SampleCtx s;
-        eval_sample<P>(a, b, ffma(t, D[0], L0), ffma(t, D[1], L1), ffma(t, D[2], L2), s);
+        float lc[3], le[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) sample_coord(t, D[i], Lh[i], Ll[i], lc[i], le[i]);
+        eval_sample<P>(a, b, lc, le, s);
         const float T = fsub(1.f, A);
         const float w = fmul(T, s.alpha);
         vis(s, T, w, A, C0, C1, C2);

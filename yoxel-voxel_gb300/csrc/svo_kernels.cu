@@ -1,5 +1,6 @@
 // svo_kernels.cu - launcher of the sparse-voxel-octree frame kernel
 // (device code in svo_trace.cuh) for the library's device node layout.
+#include <atomic>
 #include <mutex>
 
 #include "svo_trace.cuh"
@@ -7,16 +8,18 @@
 namespace yv {
 
 int device_sm_count() {
-  static int cached[64] = {0};
+  // entry points may run on several host threads: the cache is atomic (a
+  // race only repeats the same attribute query)
+  static std::atomic<int> cached[64];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 1;
-  if (cached[dev] == 0) {
-    int n = 0;
+  int n = cached[dev].load(std::memory_order_relaxed);
+  if (n == 0) {
     if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
       n = 1;
-    cached[dev] = n;
+    cached[dev].store(n, std::memory_order_relaxed);
   }
-  return cached[dev];
+  return n;
 }
 
 // Frames of the per-lane shared-memory stack ring.

@@ -102,6 +102,8 @@ extern "C" yv_status yv_render_svo_noalloc(const yv_vox_node* nodes, uint32_t co
   a.shadows = light->shadows ? 1 : 0;
   a.width = width;
   a.height = height;
+  a.id_begin = 0;
+  a.id_end = (uint32_t)ids;
   a.rgba = static_cast<uint32_t*>(out->rgba);
   a.hit = static_cast<uint32_t*>(out->hit);
   a.hit_t = static_cast<float*>(out->hit_t);
@@ -132,5 +134,28 @@ extern "C" yv_status yv_render_svo_noalloc(const yv_vox_node* nodes, uint32_t co
     cudaGetLastError();
     return YV_ERR_CUDA;
   }
+  return YV_OK;
+}
+
+extern "C" yv_status yv_render_svo_noalloc_status(void* stream, uint32_t* device_bits) {
+  uint32_t* scratch = nullptr;
+  yv_status st = scratch_address(&scratch);
+  if (st != YV_OK) return st;
+  // word 1 of the scratch is the frame's status; a pageable host word makes
+  // the copy complete before cudaMemcpyAsync returns, and nothing is
+  // allocated
+  uint32_t bits = 0;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemcpyAsync(&bits, scratch + 1, sizeof(bits), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    set_last_error(std::string("yv_render_svo_noalloc_status: ") + cudaGetErrorString(e));
+    cudaGetLastError();
+    return YV_ERR_CUDA;
+  }
+  if (device_bits) *device_bits = bits;
+  if (bits & YV_DEV_ERR_POOL) return YV_ERR_BAD_POOL;
+  if (bits & (YV_DEV_ERR_ITER | YV_DEV_ERR_DEPTH)) return YV_ERR_ITERATION_CAP;
+  if (bits & YV_DEV_ERR_TIMEOUT) return YV_ERR_TIMEOUT;
   return YV_OK;
 }

@@ -15,9 +15,12 @@
 //    the slowest ray of a tile and the shadow rays of some lanes overlap the
 //    primary rays of others.  Consecutive ray ids map to 8x4 pixel tiles, so
 //    lanes refilled together trace neighbouring pixels;
-//  * node records are 32 B (one L2 sector) read with two 128-bit loads; the
-//    breadth-first first `smem_nodes` records (the top tree levels, touched
-//    by every ray) are staged once per block in shared memory;
+//  * node records are 32 B (one L2 sector); a traversal step reads the one
+//    32-bit child word it tests (the sector stays in L1 while the ray is in
+//    the node).  Staging the breadth-first first `smem_nodes` records (the
+//    top tree levels) in shared memory is a separately compiled variant the
+//    launch configuration can ask for; reading every record through L1
+//    measured as fast or faster, so it is off by default;
 //  * the recursion of RecTrace becomes an explicit per-lane stack of
 //    (node id, child, slab box) frames, so a pop restores the parent's exact
 //    float values: every operation is an explicit round-to-nearest intrinsic
@@ -402,7 +405,7 @@ __global__ void __launch_bounds__(256, kMinBlocks)
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t lt_mask = (1u << lane) - 1u;
   const uint32_t tiles_x = (uint32_t)((a.width + 7) >> 3);
-  const uint32_t n_ids = tiles_x * (uint32_t)((a.height + 3) >> 2) * 32u;
+  const uint32_t n_ids = a.id_end;
   uint32_t err = 0, my_hits = 0, my_shadowed = 0;
 
   uint32_t mode = kIdle, off = 0;
@@ -421,7 +424,7 @@ __global__ void __launch_bounds__(256, kMinBlocks)
       if (lane == leader) base = atomicAdd(&a.counters[0], (uint32_t)__popc(idle));
       base = __shfl_sync(0xFFFFFFFFu, base, (int)leader);
       if (mode == kIdle) {
-        const uint32_t id = base + (uint32_t)__popc(idle & lt_mask);
+        const uint32_t id = a.id_begin + base + (uint32_t)__popc(idle & lt_mask);
         if (id >= n_ids) {
           mode = kDone;
         } else {

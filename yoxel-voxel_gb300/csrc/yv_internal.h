@@ -14,7 +14,7 @@
 // The reference pool is an array of 40-byte VoxNode records read through a
 // 1D texture (reaction/report/main.tex:36-67).  On the device each node is
 // re-laid as one 32-byte, 32-byte-aligned record of 8 child words, so a node
-// fetch is exactly one L2 sector read with two 128-bit loads.  The leaf /
+// is exactly one L2 sector (a traversal step reads the word it tests).  The leaf /
 // null information of `flags` is folded into the words:
 //   word & YV_DW_LEAF  -> leaf, low 31 bits = VoxData (leaf attribute index)
 //   word & YV_DW_NULL  -> null child (EmptyNode / FullNode)

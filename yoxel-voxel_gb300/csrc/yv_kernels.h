@@ -42,7 +42,15 @@ struct SvoFrameArgs {
   uint32_t* shadow_fetches;
   float* normal;                 // 3 floats per pixel
   uint32_t* counters;            // device scratch, kSvoCounterWords words
+  // ray ids [id_begin, id_end) of the frame to trace (32 per 8x4-pixel
+  // tile, tiles row-major); the whole frame is [0, 32 * tiles)
+  uint32_t id_begin, id_end;
 };
+
+// Ray ids of a whole width x height frame (8x4-pixel tiles of 32 ids).
+inline uint32_t frame_ray_ids(int width, int height) {
+  return (uint32_t)((width + 7) / 8) * (uint32_t)((height + 3) / 4) * 32u;
+}
 
 // Scratch words a frame uses: [0] tile queue, [1] status bits, [2] hits,
 // [3] shadowed hits.

@@ -152,6 +152,8 @@ _SIGS = {
     "yv_get_launch_config": (S, [P, C.POINTER(LaunchConfig)]),
     "yv_render_frame": (S, [P, P, P, P]),
     "yv_render_frame_async": (S, [P, C.POINTER(FrameOutputs), P]),
+    "yv_render_frame_tiles": (S, [P, U32, U32, C.POINTER(FrameOutputs), P]),
+    "yv_get_tile_count": (S, [P, C.POINTER(U32), C.POINTER(U32)]),
     "yv_renderer_frame_stats": (S, [P, C.POINTER(FrameStats)]),
     "yv_get_ray_basis": (S, [P, F3, F3, F3]),
     "yv_get_device_scene_info": (S, [P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
@@ -183,6 +185,7 @@ _SIGS = {
     "yv_batch_destroy": (None, [P]),
     "yv_batch_clear": (S, [P]),
     "yv_batch_add_svo": (S, [P, P, P]),
+    "yv_batch_add_svo_outputs": (S, [P, P, C.POINTER(FrameOutputs)]),
     "yv_batch_add_volume": (S, [P, C.POINTER(VolumeDevice), C.POINTER(Camera), C.c_int32,
                                 C.c_int32, C.POINTER(MarchParams), P]),
     "yv_batch_set_launch_config": (S, [P, C.POINTER(LaunchConfig)]),
@@ -211,6 +214,7 @@ _SIGS = {
     "yv_svo_dynamic_host_info": (S, [P, C.POINTER(U32), C.POINTER(U32), C.POINTER(U32)]),
     "yv_render_svo_noalloc": (S, [P, U32, U32, P, U32, C.POINTER(Camera), C.POINTER(Light),
                                   C.c_int32, C.c_int32, C.POINTER(FrameOutputs), P]),
+    "yv_render_svo_noalloc_status": (S, [P, C.POINTER(U32)]),
     "yv_ssna_defaults": (S, [P, C.POINTER(SsnaParams)]),
     "yv_render_ssna": (S, [P, C.POINTER(SsnaParams), P, P, P, P]),
     "yv_renderer_trace_dump": (S, [P, P, P, P]),

@@ -33,12 +33,22 @@ class Batch:
         L.check(L.lib.yv_batch_clear(self._h), "yv_batch_clear")
         self._keep = []
 
-    def add_svo(self, renderer, rgba):
+    def add_svo(self, renderer, rgba, hit=None, hit_t=None, fetches=None, shadow_fetches=None):
         """Snapshot of `renderer` (scene, camera, light, resolution) into the
-        (h, w) int32 CUDA tensor `rgba`."""
-        L.check(L.lib.yv_batch_add_svo(self._h, renderer.handle, C.c_void_p(rgba.data_ptr())),
-                "yv_batch_add_svo")
-        self._keep += [renderer, rgba]
+        (h, w) int32 CUDA tensor `rgba`, and optionally the per-pixel hit ids
+        ((node << 3) | child), hit t, fetch and shadow-fetch counts, as a
+        per-scene frame reports them."""
+        if hit is None and hit_t is None and fetches is None and shadow_fetches is None:
+            L.check(L.lib.yv_batch_add_svo(self._h, renderer.handle,
+                                           C.c_void_p(rgba.data_ptr())), "yv_batch_add_svo")
+        else:
+            def ptr(t):
+                return None if t is None else C.c_void_p(t.data_ptr())
+            o = L.FrameOutputs(ptr(rgba), ptr(hit), ptr(hit_t), ptr(fetches),
+                               ptr(shadow_fetches), None)
+            L.check(L.lib.yv_batch_add_svo_outputs(self._h, renderer.handle, C.byref(o)),
+                    "yv_batch_add_svo_outputs")
+        self._keep += [renderer, rgba, hit, hit_t, fetches, shadow_fetches]
 
     def add_volume(self, desc, cam, width, height, rgba, alpha_scale=1.0, step_vox=0.5):
         """One camera (pos, dir, up, fov) of a device volume into the

@@ -94,7 +94,15 @@ class DynamicSVO:
     def render(self, pos, view, up, fov, width, height, light, ambient=0.15, diffuse=0.85,
                shadows=False, stream=None):
         """One frame from the device mirror: dict of CUDA tensors (rgba, hit,
-        hit_t, fetches, shadow_fetches)."""
+        hit_t, fetches, shadow_fetches).
+
+        The frame runs through the allocation-free entry point, whose scratch
+        (ray-queue counter, status word, hit counters) is one static device
+        array shared by every such frame: frames in flight at the same time,
+        on different streams or host threads, race on it and come out wrong.
+        Serialise them, or bind the scene to a Renderer
+        (Renderer.SetSceneDynamic), which has counters of its own.  The
+        frame's device status is read with `status()`."""
         import torch
         n, cnt, root, a, na = self._device()
         cam = L.Camera(L.F3(*[float(v) for v in pos]), L.F3(*[float(v) for v in view]),
@@ -111,3 +119,13 @@ class DynamicSVO:
                                             width, height, C.byref(o), _stream(stream)),
                 "yv_render_svo_noalloc")
         return out
+
+    @staticmethod
+    def status(stream=None):
+        """Device status of the last frame rendered by `render` (waits for
+        `stream`): raises YvError on YV_ERR_BAD_POOL or YV_ERR_ITERATION_CAP,
+        else returns the raw status bits (0)."""
+        bits = C.c_uint32()
+        L.check(L.lib.yv_render_svo_noalloc_status(_stream(stream), C.byref(bits)),
+                "yv_render_svo_noalloc_status")
+        return bits.value

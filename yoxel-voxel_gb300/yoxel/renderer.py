@@ -175,6 +175,25 @@ class Renderer:
         L.check(L.lib.yv_render_frame_async(self._h, C.byref(o), _stream_ptr(stream)),
                 "yv_render_frame_async")
 
+    def tile_count(self):
+        """(tiles_x, tiles_y) of the frame's 8x4-pixel tiles."""
+        tx, ty = C.c_uint32(), C.c_uint32()
+        L.check(L.lib.yv_get_tile_count(self._h, C.byref(tx), C.byref(ty)), "yv_get_tile_count")
+        return tx.value, ty.value
+
+    def render_tiles(self, tile_begin, tile_end, rgba=None, hit=None, hit_t=None, fetches=None,
+                     shadow_fetches=None, normal=None, stream=None):
+        """Enqueues tiles [tile_begin, tile_end) of the frame (8x4-pixel
+        tiles, row-major) into full-frame CUDA tensors; pixels outside the
+        range are left as they are (the work split of the reference's
+        threaded renderer, cell/ppu_renderer.cpp:121-144)."""
+        def ptr(t):
+            return None if t is None else C.c_void_p(t.data_ptr())
+        o = L.FrameOutputs(ptr(rgba), ptr(hit), ptr(hit_t), ptr(fetches), ptr(shadow_fetches),
+                           ptr(normal))
+        L.check(L.lib.yv_render_frame_tiles(self._h, int(tile_begin), int(tile_end), C.byref(o),
+                                            _stream_ptr(stream)), "yv_render_frame_tiles")
+
     def frame_stats(self, check=True):
         s = L.FrameStats()
         st = L.lib.yv_renderer_frame_stats(self._h, C.byref(s))

@@ -47,3 +47,79 @@ def cfg5_specs(seed=1234, n=32):
         specs.append(dict(kind=kind, depth=depth, res=res, seed=int(seed * 1000 + i),
                           cam_dir=tuple(float(v) for v in cam_dir)))
     return specs
+
+
+def cfg5_batch(specs, precision=3, hits=False, keep_scenes=False):
+    """The batch of `specs` (cfg5_specs): one yoxel.Batch with an SVO frame
+    (spheres scene, Lambert, no shadows) or a brick-volume composite per
+    spec, in spec order.  Returns (batch, items); each item is a dict with
+    kind, spec, res, cam (pos, view, up, fov) and out (the batch's output
+    tensor), plus for SVO items the renderer (the host scene too with
+    keep_scenes=True; a depth-11 scene holds about 0.6 GB of host memory) and,
+    with hits=True, the hit / hit_t / fetches tensors the batch also writes;
+    for brick items the host volume and its device pool."""
+    import torch
+
+    from .batch import Batch
+    from .renderer import Renderer
+    from .volume import BrickVolume
+    batch = Batch()
+    items = []
+    for sp in specs:
+        res = sp["res"]
+        pos, view = camera(sp["cam_dir"])
+        cam = (pos, view, (0, 0, 1), 60.0)
+        it = dict(kind=sp["kind"], spec=sp, res=res, cam=cam)
+        if sp["kind"] == "svo":
+            s = spheres(sp["depth"], seed=sp["seed"])
+            r = Renderer()
+            r.SetScene(s)
+            r.SetViewPos(pos)
+            r.SetViewDir(view)
+            r.SetResolution(res, res)
+            r.SetFOV(60.0)
+            r.SetLight(LIGHT, 0.15, 0.85, False)
+            out = torch.empty((res, res), dtype=torch.int32, device="cuda")
+            extra = {}
+            if hits:
+                extra = dict(hit=torch.empty((res, res), dtype=torch.int32, device="cuda"),
+                             hit_t=torch.empty((res, res), dtype=torch.float32, device="cuda"),
+                             fetches=torch.empty((res, res), dtype=torch.int32, device="cuda"))
+            batch.add_svo(r, out, **extra)
+            it.update(renderer=r, out=out, **extra)
+            if keep_scenes:
+                it["scene"] = s
+            del s
+        else:
+            v = BrickVolume.noise(brick_levels_for_depth(sp["depth"]), 0.4, 1.4, sp["seed"])
+            gv = v.upload(precision)
+            out = torch.empty((res, res, 4), dtype=torch.float32, device="cuda")
+            batch.add_volume(gv.desc(), cam, res, res, out)
+            it.update(volume=v, gpu_volume=gv, out=out, precision=precision)
+        items.append(it)
+    return batch, items
+
+
+def cfg4_problem(levels=2, ncams=64, seed=1234):
+    """The differentiable-volume workload: the noise volume as torch tensors
+    (yoxel.BrickVolume.to_torch), the target volume (density and albedo
+    + N(0, 0.1) from a CUDA generator seeded with `seed`, clamped to [0, 1],
+    owners perturbed then aprons synced) and the cameras (Fibonacci sphere,
+    radius 1.5).  Returns (volume, tv, target_density, target_albedo, cams)."""
+    import ctypes as C
+
+    import torch
+
+    from . import _lib as L
+    from .volume import BrickVolume, sphere_cameras, torch_desc
+    vol = BrickVolume.noise(levels, 0.4, 1.4, seed)
+    tv = vol.to_torch()
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    tgt_d = (tv["density"] + 0.1 * torch.randn(tv["density"].shape, generator=g,
+                                               device="cuda")).clamp_(0, 1)
+    tgt_a = (tv["albedo"] + 0.1 * torch.randn(tv["albedo"].shape, generator=g,
+                                              device="cuda")).clamp_(0, 1)
+    L.check(L.lib.yv_volume_sync_aprons(C.byref(torch_desc(tv, tgt_d, tgt_a)),
+                                        C.c_void_p(tgt_d.data_ptr()),
+                                        C.c_void_p(tgt_a.data_ptr()), None), "sync")
+    return vol, tv, tgt_d, tgt_a, sphere_cameras(ncams)
