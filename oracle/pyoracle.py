@@ -54,6 +54,7 @@ def load_library(build_if_missing=True):
         "orc_brick_backward_f64": (I, [P, U, P, P, U, I, P, P, P, P, I, I, D, D, P, P, P]),
         "orc_svo_build_dense": (I, [P, P, I, F, P, U, P, U, P, P, P]),
         "orc_svo_hits_f64_mt": (I, [I, P, U, U, P, P, P, D, I, I, P, P]),
+        "orc_brick_march_rays_f64": (I, [P, U, P, P, U, I, D, D, I, P, P, I, P, P]),
         "orc_svo_hits_f64_f32ray_mt": (I, [I, P, U, U, P, P, P, P, I, I, P, P]),
         "orc_brick_backward_f64_f32ray_mt": (I, [I, P, U, P, P, U, I, P, P, P, P, I, I, D, D,
                                                  P, P, P]),
@@ -373,6 +374,26 @@ def brick_render_f64_f32ray(grids, density, albedo, levels, pos, dir_, up, fov, 
         raise RuntimeError(f"oracle brick render failed: {st}")
     out = (rgba.reshape(height, width, 4), ns.reshape(height, width), nb.reshape(height, width))
     return out + (tf.reshape(height, width).astype(bool),) if ties else out
+
+
+@_keeps
+def brick_march_rays_f64(grids, density, albedo, levels, origins, dirs, alpha_scale=1.0,
+                         step_vox=0.5, transfer=0):
+    """FP64 march of rays (n x 3 origins and directions); transfer 1 is the
+    fixed transfer of reaction/trace/trace.cu.  Returns (rgba (n, 4),
+    samples (n,))."""
+    g, d, a = _vol_arrays(grids, density, albedo)
+    o = np.ascontiguousarray(origins, np.float64).reshape(-1, 3)
+    dv = np.ascontiguousarray(dirs, np.float64).reshape(-1, 3)
+    n = len(o)
+    rgba = np.zeros((n, 4), np.float64)
+    ns = np.zeros(n, np.uint32)
+    st = lib().orc_brick_march_rays_f64(_p(g), len(g) // 64, _p(d), _p(a), len(d) // 729,
+                                        levels, float(alpha_scale), float(step_vox),
+                                        int(transfer), _p(o), _p(dv), n, _p(rgba), _p(ns))
+    if st != 0:
+        raise RuntimeError(f"oracle brick march failed: {st}")
+    return rgba, ns
 
 
 class BrickWindow:

@@ -843,3 +843,24 @@ static int backward_mt(int nthreads, bwd_job* jp, const uint32_t* grids, uint32_
   free(j.ga);
   return st;
 }
+
+/* ---- FP64 march of arbitrary rays (origins and directions given) ---- */
+int orc_brick_march_rays_f64(const uint32_t* grids, uint32_t ngrids, const float* density,
+                             const float* albedo, uint32_t nbricks, int levels,
+                             double alpha_scale, double step_vox, int transfer,
+                             const double* origins, const double* dirs, int n, double* rgba,
+                             uint32_t* samples) {
+  brick_ctx_f64 c;
+  if (brick_ctx_init_f64(&c, grids, ngrids, density, albedo, nbricks, levels, alpha_scale,
+                         step_vox))
+    return 1;
+  c.transfer = transfer;
+  for (int i = 0; i < n; ++i) {
+    uint32_t ns = 0;
+    int st = brick_march_f64(&c, origins + 3 * (size_t)i, dirs + 3 * (size_t)i,
+                             rgba + 4 * (size_t)i, &ns, 0, 0, 0);
+    if (st) return st;
+    if (samples) samples[i] = ns;
+  }
+  return 0;
+}

@@ -13,10 +13,18 @@
  *   AdjustDir / SetupTrace         cell/spu/trace_spu.c_:66-105,
  *                                  reaction/report/voxel.tex:309-326
  *   brick march castRay/walkBrick  reaction/trace/trace.cu:42-139
- * The reference cannot be compiled here (its cpp/ headers, Boost and
- * libspe2 are missing), so parity with it is pinned by this restatement and
- * by the hand-made known-answer cases in tests/ ("parity unpinned" by the
- * reference's own tests, which cover no tracing code).
+ * Pinned against the reference itself: oracle/build_ref.py compiles the
+ * reference's own renderer code on the host (cell/ppu_renderer.cpp with
+ * renderer_base.h and svodata.h, cell/spu/trace_spu.cpp, and
+ * reaction/trace/trace.cu), with stand-ins (oracle/ref_shim/) only for the
+ * headers its snapshot lacks (cpp/, Boost, the Cell SDK, CUDA).  The float
+ * instantiation reproduces that renderer's camera basis, every pixel's hit
+ * leaf, hit t and node-fetch count bit for bit, and the double march under
+ * trace.cu's fixed transfer agrees with its castRay to 1e-5
+ * (tests/test_ref_pin.py, fixtures tests/golden/ref_*.npz).  What the
+ * snapshot does not define - SetupTrace / AdjustDir, the shading, the
+ * configs' transfer and the ntree lattice layout - is restated, as the
+ * comments below say.
  */
 #ifndef YV_ORACLE_H
 #define YV_ORACLE_H
@@ -229,6 +237,18 @@ int orc_brick_render_f64_f32ray_rect(const uint32_t* grids, uint32_t ngrids,
                                      const float dv[3], int width, int height,
                                      double alpha_scale, double step_vox, int x0, int x1,
                                      int y0, int y1, double* rgba, uint32_t* samples);
+
+/* FP64 march of n rays with the given origins and directions (3 doubles
+ * each; directions need not be unit: t is their parameter).  transfer 0:
+ * the configs' (alpha = saturate(alpha_scale * density), albedo colour);
+ * 1: the fixed transfer of reaction/trace/trace.cu:52-56 (s = saturate(2 v
+ * - 0.9), alpha = s / 2, colour s), used to pin the march against the
+ * reference's own castRay.  rgba: 4 doubles per ray. */
+int orc_brick_march_rays_f64(const uint32_t* grids, uint32_t ngrids, const float* density,
+                             const float* albedo, uint32_t nbricks, int levels,
+                             double alpha_scale, double step_vox, int transfer,
+                             const double* origins, const double* dirs, int n, double* rgba,
+                             uint32_t* samples);
 
 /* SVO build from a dense density grid (yv_oracle_build.c): 2^depth grid,
  * solid = density > iso, canonical breadth-first pool (nodes: 10 uint32 per

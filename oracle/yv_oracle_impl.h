@@ -253,6 +253,11 @@ typedef struct {
    * entry cell's coordinate within TIE_T of an integer, or the opacity
    * within TIE_A of the early-exit threshold after a sample */
   int tie;
+  /* 0: the configs' transfer, alpha = saturate(alpha_scale * density) and
+   * the interpolated albedo as colour; 1: the reference's fixed transfer of
+   * reaction/trace/trace.cu:52-56, s = saturate(2 v - 0.9), alpha = s / 2,
+   * colour (s, s, s) */
+  int transfer;
 } FN(brick_ctx);
 
 /* Tree descent for brick cell c (ntree/ntree/nodes.h:56-99 child offsets
@@ -406,9 +411,18 @@ static int FN(brick_march)(FN(brick_ctx) * c, const REAL* o, const REAL* d,
           for (int ch = 0; ch < 3; ++ch)
             col[ch] += w[j] * (REAL)c->albedo[(size_t)idx[j] * 3u + (uint32_t)ch];
         }
-        REAL alpha = sigma * c->alpha_scale;
-        if (alpha < 0) alpha = 0;
-        if (alpha > 1) alpha = 1;
+        REAL alpha;
+        if (c->transfer == 1) {
+          REAL sv = (REAL)2 * sigma - (REAL)0.9;
+          if (sv < 0) sv = 0;
+          if (sv > 1) sv = 1;
+          alpha = (REAL)0.5 * sv;
+          col[0] = col[1] = col[2] = sv;
+        } else {
+          alpha = sigma * c->alpha_scale;
+          if (alpha < 0) alpha = 0;
+          if (alpha > 1) alpha = 1;
+        }
         if (fn) fn(user, idx, w, sigma, col, alpha, acc_a, acc_c);
         REAL wgt = ((REAL)1 - acc_a) * alpha;
         for (int ch = 0; ch < 3; ++ch) acc_c[ch] += wgt * col[ch];
@@ -454,6 +468,8 @@ static int FN(brick_ctx_init)(FN(brick_ctx) * c, const uint32_t* grids,
   c->dt = step_vox / c->S;
   c->inv_dt = c->S / step_vox;
   c->err = 0;
+  c->tie = 0;
+  c->transfer = 0;
   return 0;
 }
 

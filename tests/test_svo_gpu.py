@@ -254,3 +254,32 @@ def test_deepest_tree_16_levels(yoxel_mod, oracle):
                               [0, 0, 1], 70.0, 128, 96, LIGHT, shadows=True)
         assert_bit_exact(g, o, True)
         assert o["fetches"].max() >= 16
+
+
+@pytest.mark.parametrize("name", ["ref_svo_spheres_d6", "ref_svo_terrain_d6",
+                                  "ref_svo_inside_d5", "ref_svo_axis_d5", "ref_svo_deep16"])
+def test_reference_renderer_fixtures(yoxel_mod, name):
+    """The CUDA path against outputs of the reference's own CPU renderer
+    (cell/ppu_renderer.cpp compiled on the host, tests/golden/
+    make_ref_golden.py): every pixel's hit leaf (its VoxData), t and node
+    fetches bit-exact."""
+    gf = np.load(os.path.join(ROOT, "tests", "golden", name + ".npz"))
+    nodes = gf["nodes"].view(yoxel_mod.NODE_DTYPE)
+    attrs = gf["attrs"].reshape(-1).view(yoxel_mod.ATTR_DTYPE)
+    r = yoxel_mod.Renderer()
+    r.SetSceneArrays(nodes, int(gf["root"]), attrs)
+    r.SetViewPos(gf["pos"])
+    r.SetViewDir(gf["view"])
+    r.SetViewUp(gf["up"])
+    r.SetResolution(int(gf["width"]), int(gf["height"]))
+    r.SetFOV(float(gf["fov"]))
+    r.SetLight(LIGHT, 0.15, 0.85, False)
+    o = r.render_outputs()
+    hit = o["hit"].cpu().numpy().view(np.uint32)
+    pool = gf["nodes"].reshape(-1, 10)
+    data = np.full(hit.shape, 0xFFFFFFFF, np.uint32)
+    m = hit != 0xFFFFFFFF
+    data[m] = pool[hit[m] >> 3, 2 + (hit[m] & 7)]
+    assert np.array_equal(data, gf["data"])
+    assert np.array_equal(o["hit_t"].cpu().numpy().view(np.uint32), gf["t"].view(np.uint32))
+    assert np.array_equal(o["fetches"].cpu().numpy().view(np.uint32), gf["fetches"])
