@@ -177,19 +177,33 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+ARM_PARTS = {0xd0c: "Neoverse-N1", 0xd40: "Neoverse-V1", 0xd49: "Neoverse-N2",
+             0xd4f: "Neoverse-V2", 0xd84: "Neoverse-V3", 0xd8e: "Neoverse-N3"}
+
+
 def cpu_model():
-    """Host CPU name from /proc/cpuinfo (x86 "model name", Arm "CPU part"),
-    or the platform string."""
+    """Host CPU name and core count: x86 "model name", or the Arm part
+    number of /proc/cpuinfo named (0xd4f = Neoverse-V2)."""
+    name = None
     try:
         with open("/proc/cpuinfo") as f:
             for line in f:
                 k, _, v = line.partition(":")
-                if k.strip() in ("model name", "CPU part"):
-                    return v.strip()
+                k, v = k.strip(), v.strip()
+                if k == "model name" and name is None:
+                    name = v
+                elif k == "CPU part" and name is None:
+                    try:
+                        part = int(v, 16)
+                        name = ARM_PARTS.get(part, f"Arm part {v}")
+                    except ValueError:
+                        name = v
     except OSError:
         pass
-    import platform
-    return platform.processor() or platform.machine()
+    if name is None:
+        import platform
+        name = platform.processor() or platform.machine()
+    return f"{name} x {os.cpu_count() or 1} cores"
 
 
 def profile_traffic(name):
@@ -200,6 +214,29 @@ def profile_traffic(name):
         return None
     m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(p).read())
     return float(m.group(1)) if m else None
+
+
+def profile_issue(name):
+    """Issue-side figures of the kernel from profiles/<name>.md (lines
+    `issue_active_pct: X`, `thread_inst_per_unit: Y (unit)`,
+    `simd_efficiency_pct: Z`), or None: the traversal kernels are bound by
+    instruction issue, so these say more than the bandwidth fraction."""
+    p = os.path.join(ROOT, "profiles", name + ".md")
+    if not os.path.exists(p):
+        return None
+    txt = open(p).read()
+    out = {}
+    for key in ("issue_active_pct", "simd_efficiency_pct"):
+        m = re.search(key + r":\s*([0-9.]+)", txt)
+        if m:
+            out[key] = float(m.group(1))
+    m = re.search(r"thread_inst_per_unit:\s*([0-9.]+)\s*\(([^)]*)\)", txt)
+    if m:
+        out["thread_instructions_per_unit"] = float(m.group(1))
+        out["unit"] = m.group(2)
+    if out:
+        out["source"] = f"ncu --set full capture, profiles/{name}.md"
+    return out or None
 
 
 def cfg_seed(cfg):
@@ -262,8 +299,9 @@ def run_reference(args, cfg):
         print(json.dumps({"impl": "reference", "unavailable":
                           f"{args.config}: the reference has no CPU form of this workload"}))
         return
-    # each step: the same view at half the resolution per axis (1/4 of rays)
-    w, h = cfg["width"] // 2, cfg["height"] // 2
+    # each step: the same frame as the GPU arm (all its primary and shadow
+    # rays)
+    w, h = cfg["width"], cfg["height"]
     if cfg["kind"] == "svo":
         scene = make_scene(cfg)
         # the cut-off of the full-size frame (detail * radians(fov / 2) / width)
@@ -294,8 +332,8 @@ def run_reference(args, cfg):
         vals.append(v)
         secs.append(s)
     value = rays * len(secs) / sum(secs) / 1e6
-    sample = (f"{w}x{h} frame of the same scene and camera per step ({rays} rays incl. "
-              f"shadow rays)")
+    sample = (f"the {w}x{h} frame of the same scene and camera per step ({rays} rays incl. "
+              f"shadow rays), as the GPU arm traces it")
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT,
         "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
@@ -306,15 +344,26 @@ def run_reference(args, cfg):
                          "kind": "port", "sample": sample},
         "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
-        "note": "reference CPU renderer (cell/ppu_renderer.cpp) cannot be compiled here "
-                "(missing cpp/ headers, Boost, libspe2); the FP32 C restatement of it is timed",
+        "note": "the FP32 C restatement of the reference CPU renderer (cell/ppu_renderer.cpp) "
+                "on all host cores in row-interleaved threads; the reference renderer itself, "
+                "compiled from its sources with stand-ins for its missing headers "
+                "(oracle/build_ref.py), returns the same hits, t and fetch counts bit for bit "
+                "(tests/test_ref_pin.py) but its sources are not on this machine",
+        "cpu_model": cpu_model(),
     }
     print(json.dumps(line), flush=True)
 
 
 def run_svo(args, cfg):
+    """SVO frame (cfg1 / cfg2 / lod).  With N > 1 ranks the one frame is
+    sharded: rank r traces its contiguous range of 8x4-pixel tiles (ranges of
+    equal node-fetch cost, yoxel.parallel.partition_tiles over the per-tile
+    fetches of a first frame), the tile split of the reference's threaded
+    renderer (cell/ppu_renderer.cpp:121-144); no collective on the data path.
+    `value` = the frame's rays / the slowest rank's time (strong scaling)."""
     import torch
     import yoxel
+    from yoxel import parallel as P
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
     pg = None
@@ -353,17 +402,42 @@ def run_svo(args, cfg):
     F = int(o["fetches"].to(torch.int64).sum())
     Fs = int(o["shadow_fetches"].to(torch.int64).sum())
     hits = int(o["stats"]["hits"])
-    del o
     shadow_rays = hits if cfg["shadows"] else 0
     rays = npix + shadow_rays
     alg_bytes = 40 * F + 40 * Fs + 8 * npix + 8 * hits
+    # this rank's tiles (all of them on one GPU) and its share of the bytes
+    tx, ty = r.tile_count()
+    if ws > 1:
+        fcost = (o["fetches"].to(torch.int64) + o["shadow_fetches"].to(torch.int64)).cpu()
+        ranges = P.partition_tiles(P.tile_costs(fcost.numpy(), w, h), ws)
+        tb, te = ranges[rank]
+        y0, y1 = P.tile_rows((tb, te), w, h)
+        mask = torch.zeros((ty * 4, tx * 8), dtype=torch.bool)
+        for t in range(tb, te):
+            mask[(t // tx) * 4:(t // tx) * 4 + 4, (t % tx) * 8:(t % tx) * 8 + 8] = True
+        mask = mask[:h, :w].cuda()
+        hitm = (o["hit"] != -1) & mask
+        my_bytes = (40 * int(o["fetches"].to(torch.int64)[mask].sum()) +
+                    40 * int(o["shadow_fetches"].to(torch.int64)[mask].sum()) +
+                    8 * int(mask.sum()) + 8 * int(hitm.sum()))
+    else:
+        tb, te, y0, y1 = 0, tx * ty, 0, h
+        my_bytes = alg_bytes
+    del o
 
     rgba = torch.empty((h, w), dtype=torch.int32, device="cuda")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
+
+    def frame():
+        if ws > 1:
+            r.render_tiles(tb, te, rgba=rgba, stream=stream)
+        else:
+            r.render_async(rgba=rgba, stream=stream)
+
     for _ in range(args.warmup):
         flush.fill_(1)
-        r.render_async(rgba=rgba, stream=stream)
+        frame()
     r.frame_stats()
     barrier()
 
@@ -377,7 +451,7 @@ def run_svo(args, cfg):
     for i in range(args.steps):
         flush.fill_(1)
         evs[i][0].record(stream)
-        r.render_async(rgba=rgba, stream=stream)
+        frame()
         evs[i][1].record(stream)
     barrier()
     wall = time.perf_counter() - t0
@@ -389,26 +463,39 @@ def run_svo(args, cfg):
     ew = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
     ew[0].record(stream)
     for _ in range(args.steps):
-        r.render_async(rgba=rgba, stream=stream)
+        frame()
     ew[1].record(stream)
     torch.cuda.synchronize()
     warm_ms = ew[0].elapsed_time(ew[1]) / args.steps
     clocks = sampler.stop()
 
-    # end to end through the C ABI with a pinned host frame buffer
+    # end to end through the C ABI with a pinned host frame buffer: one
+    # GPU renders the whole frame with yv_render_frame (synchronous, frame
+    # read back); sharded, each rank renders its tiles and reads back the
+    # rows that hold them
     host = torch.empty((h, w), dtype=torch.int32, pin_memory=True)
     import ctypes as C
     from yoxel import _lib as L
+
+    def e2e_frame():
+        if ws > 1:
+            r.render_tiles(tb, te, rgba=rgba, stream=stream)
+            if y1 > y0:
+                host[y0:y1].copy_(rgba[y0:y1], non_blocking=True)
+            r.frame_stats()
+        else:
+            L.check(L.lib.yv_render_frame(r.handle, C.c_void_p(host.data_ptr()), None,
+                                          C.c_void_p(stream.cuda_stream)), "render_frame")
+
     for _ in range(2):
-        L.check(L.lib.yv_render_frame(r.handle, C.c_void_p(host.data_ptr()), None,
-                                      C.c_void_p(stream.cuda_stream)), "render_frame")
+        e2e_frame()
     barrier()
-    te = time.perf_counter()
+    te_ = time.perf_counter()
     for _ in range(args.steps):
-        L.check(L.lib.yv_render_frame(r.handle, C.c_void_p(host.data_ptr()), None,
-                                      C.c_void_p(stream.cuda_stream)), "render_frame")
+        e2e_frame()
     barrier()
-    e2e_s = (time.perf_counter() - te) / args.steps
+    e2e_s = (time.perf_counter() - te_) / args.steps
+    d2h = (y1 - y0) * w * 4 + 32
 
     # max over ranks
     tot = torch.tensor([dev_s, e2e_s], dtype=torch.float64, device="cuda")
@@ -421,49 +508,64 @@ def run_svo(args, cfg):
         return
 
     mean_step_s = dev_s / args.steps
-    value = rays * args.steps * ws / dev_s / 1e6
+    value = rays * args.steps / dev_s / 1e6
     peaks, peak_kind = measured_peaks()
-    achieved = alg_bytes / mean_step_s / 1e9
-    traffic = profile_traffic(f"svo_frame_{args.config}")
+    achieved = my_bytes / mean_step_s / 1e9
+    traffic = profile_traffic(f"svo_frame_{args.config}") if ws == 1 else None
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(mean_step_s * 1000, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "scaling": "strong" if ws > 1 else "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
         "config": {"workload": cfg["workload"], "config": args.config, "seed": cfg_seed(cfg),
                    "primary_rays_per_step": npix, "shadow_rays_per_step": shadow_rays,
                    "scene_nodes": dev_nodes, "scene_device_bytes": dev_bytes,
                    "l2": "flushed between steps (256 MiB write); scene > L2",
-                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
-        "primary_mrays_s": round(npix * args.steps * ws / dev_s / 1e6, 3),
-        "warm_l2_mrays_s": round(rays * ws / (warm_ms / 1000) / 1e6, 3),
+                   "parallelism": (f"one frame sharded into {ws} tile ranges of equal node-fetch "
+                                   f"cost (rank 0: tiles {tb}-{te} of {tx * ty})" if ws > 1
+                                   else "single GPU")},
+        "primary_mrays_s": round(npix * args.steps / dev_s / 1e6, 3),
+        "warm_l2_mrays_s": round(rays / (warm_ms / 1000) / 1e6, 3),
         "wall_s_timed_region": round(wall, 4),
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2),
                      "peak": peaks["hbm_gbs"], "unit": "GB/s",
                      "frac": round(achieved / peaks["hbm_gbs"], 4),
                      "traffic": traffic, "peak_source": peak_kind,
-                     "algorithmic_bytes_per_step": alg_bytes,
+                     "traffic_source": (f"ncu capture of one launch (dram__bytes_read.sum + "
+                                        f"dram__bytes_write.sum), profiles/svo_frame_"
+                                        f"{args.config}.md" if traffic else None),
+                     "kernel": "svo_frame_kernel",
+                     "algorithmic_bytes_per_step": my_bytes,
                      "bytes_per_ray": round(alg_bytes / rays, 2),
                      "mean_node_fetches_primary": round(F / npix, 3),
                      "mean_node_fetches_shadow": round(Fs / max(1, shadow_rays), 3)},
         "e2e": {"value": round(rays / e2e_s / 1e6, 3), "unit": UNIT,
-                "h2d_bytes_per_step": 40, "d2h_bytes_per_step": npix * 4 + 32,
-                "path": "yv_render_frame (C ABI) into pinned host memory, synchronous"},
+                "h2d_bytes_per_step": 40, "d2h_bytes_per_step": d2h,
+                "path": ("yv_render_frame (C ABI) into pinned host memory, synchronous"
+                         if ws == 1 else "yv_render_frame_tiles (C ABI) per rank, its rows "
+                         "read back into pinned host memory, synchronous")},
         "gpu_launches": int(st["launches"]) * args.steps,
         "clocks": clocks,
         "scene_build_s": round(t_scene, 2),
     }
+    issue = profile_issue(f"svo_frame_{args.config}")
+    if issue and ws == 1:
+        line["roofline"]["issue"] = issue
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         sw, sh = w // 4, h // 4
-        v, s, rr = cpu_svo(cfg, scene, sw, sh, threads, min_seconds=10.0, max_runs=50,
-                           lod_coef=lod_coef)
+        v, s_, rr = cpu_svo(cfg, scene, sw, sh, threads, min_seconds=10.0, max_runs=100000,
+                            lod_coef=lod_coef)
         v1, s1, rr1 = cpu_svo(cfg, scene, w // 16, h // 16, 1, lod_coef=lod_coef)
         v4, s4, rr4 = cpu_svo(cfg, scene, w // 8, h // 8, 4, lod_coef=lod_coef)
+        runs = max(1, int(round(10.0 / s_))) if s_ > 0 else 1
         line["cpu_baseline"] = {
             "value": round(v, 4), "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{sw}x{sh} frame of the same scene and camera ({rr} rays incl. shadow "
-                      f"rays), repeated for >=10 s; FP32 C restatement of cell/ppu_renderer.cpp",
+                      f"rays), repeated for >= 10 s (~{runs} frames); the FP32 C "
+                      f"restatement of cell/ppu_renderer.cpp, which reproduces the reference "
+                      f"renderer compiled from its sources bit for bit (tests/test_ref_pin.py)",
             "single_thread_value": round(v1, 4),
             "four_thread_value": round(v4, 4),
             "cpu_model": cpu_model()}

@@ -103,6 +103,15 @@ yv_status yv_svo_from_arrays(yv_svo_host** out, const yv_vox_node* nodes,
                              uint32_t count, uint32_t root,
                              const yv_leaf_attr* attrs, uint32_t nattrs);
 
+/* A host container from a reference pool held in memory as SVOData holds it
+ * (cell/svodata.h:20-55): leaves and every node's `data` carry the packed
+ * VoxData of reaction/report/main.tex:38,65 (16-bit RGB565 colour, 16-bit
+ * octahedral int8x2 normal), decoded into leaf attributes exactly as a .vox
+ * file without an attribute section is (the scene then has level-of-detail
+ * data).  Node ids are kept. */
+yv_status yv_svo_from_packed(yv_svo_host** out, const yv_vox_node* nodes,
+                             uint32_t count, uint32_t root);
+
 /* .vox file (SVOData::Load, cell/svodata.h:31-50): little-endian
  * uint32 root, uint32, uint32, uint32 size, VoxNode[size]; followed by an
  * optional attribute section "YVAT" uint32 count, yv_leaf_attr[count], and
@@ -215,6 +224,11 @@ yv_status yv_set_scene_svo(yv_renderer* r, const yv_vox_node* nodes,
                            uint32_t count, uint32_t root,
                            const yv_leaf_attr* attrs, uint32_t nattrs);
 yv_status yv_set_scene_host(yv_renderer* r, const yv_svo_host* svo);
+/* ISVORenderer::SetScene(SVOData*) for a pool in the reference's own packed
+ * leaf format (yv_svo_from_packed): no separate attribute array needed.
+ * Hit ids are the pool's node ids. */
+yv_status yv_set_scene_svo_packed(yv_renderer* r, const yv_vox_node* nodes,
+                                  uint32_t count, uint32_t root);
 yv_status yv_load_scene_vox(yv_renderer* r, const char* path);
 /* SVORenderer::SetScene(DynamicSVO*) (demo/SVORenderer.cpp:33-53): the
  * renderer keeps a non-owning pointer to an editable scene (declared below)
@@ -409,6 +423,14 @@ yv_status yv_volume_render(const yv_volume_device* vol, const yv_camera* cams,
 /* Adjoint of yv_volume_render (fp32 volumes, plain or packed): re-marches
  * every ray and accumulates dL/ddensity and dL/dalbedo (pool layout, ADDED
  * to the buffers) from dL/drgba, given the forward output rgba. */
+/* RunTrace(const RenderParams&, uchar4* img, float*) (ntree/ntree_trace.cuh:
+ * 22-28): the same march written as RGBA8 pixels, each channel
+ * saturate(v) * 255 truncated, R in the low byte (float2uint,
+ * reaction/trace/utils.h:37-44); rgba8: ncams*height*width uint32 (device). */
+yv_status yv_volume_render_rgba8(const yv_volume_device* vol, const yv_camera* cams,
+                                 int32_t ncams, int32_t width, int32_t height,
+                                 const yv_march_params* mp, uint32_t* rgba8,
+                                 void* stream);
 yv_status yv_volume_backward(const yv_volume_device* vol,
                              const yv_camera* cams, int32_t ncams,
                              int32_t width, int32_t height,

@@ -90,3 +90,59 @@ def test_gloo_gradient_sum_and_frame_gather():
     full = (np.arange(6) * sum(range(1, 9))).tolist()
     assert res[0][0] == full and res[1][0] == full
     assert res[0][1] == [[0.0] * 4, [1.0] * 4] and res[1][1] is None
+
+
+def _shard_worker(rank, world, port, q):
+    """A sharded frame as bench.py runs it: every rank derives the same tile
+    ranges from the same cost map (no communication), paints the pixels of
+    its ranges, and rank 0 gathers the frames."""
+    sys.path[:0] = [ROOT, PKG]
+    import torch
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from yoxel import parallel as P
+    w, h = 37, 23
+    cost = np.random.default_rng(7).integers(1, 60, (h, w))
+    ranges = P.partition_tiles(P.tile_costs(cost, w, h), world)
+    tb, te = ranges[rank]
+    tx = (w + 7) // 8
+    frame = torch.full((h, w), -1.0)
+    for t in range(tb, te):
+        frame[(t // tx) * 4:(t // tx) * 4 + 4, (t % tx) * 8:(t % tx) * 8 + 8] = float(rank)
+    y0, y1 = P.tile_rows((tb, te), w, h)
+    painted_rows = torch.nonzero((frame >= 0).any(dim=1)).flatten().tolist()
+    frames = P.gather_to_root(frame, world, rank)
+    q.put((rank, ranges, (y0, y1), painted_rows,
+           None if frames is None else [f.numpy() for f in frames]))
+    dist.destroy_process_group()
+
+
+def test_gloo_sharded_frame_tiles_cover_the_frame_once():
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    world = 3
+    procs = [ctx.Process(target=_shard_worker, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    res = {}
+    for _ in range(world):
+        rank, ranges, rows, painted, frames = q.get(timeout=120)
+        res[rank] = (ranges, rows, painted, frames)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert all(res[r][0] == res[0][0] for r in range(world))
+    frames = res[0][3]
+    merged = np.full(frames[0].shape, -1.0)
+    for r, f in enumerate(frames):
+        mine = f >= 0
+        assert (merged[mine] < 0).all()  # no pixel painted twice
+        merged[mine] = f[mine]
+        painted = res[r][2]
+        y0, y1 = res[r][1]
+        assert all(y0 <= y < y1 for y in painted)  # the rows read back hold the tiles
+    assert (merged >= 0).all()  # every pixel painted once

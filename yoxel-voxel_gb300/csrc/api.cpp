@@ -296,6 +296,17 @@ yv_status yv_set_scene_svo(yv_renderer* r, const yv_vox_node* nodes,
   return set_scene_impl(r, nodes, count, root, attrs, nattrs, false);
 }
 
+yv_status yv_set_scene_svo_packed(yv_renderer* r, const yv_vox_node* nodes, uint32_t count,
+                                  uint32_t root) {
+  if (!r) return YV_ERR_INVALID_ARG;
+  yv_svo_host* h = nullptr;
+  yv_status st = yv_svo_from_packed(&h, nodes, count, root);
+  if (st != YV_OK) return st;
+  st = yv_set_scene_host(r, h);
+  yv_svo_free(h);
+  return st;
+}
+
 yv_status yv_set_scene_host(yv_renderer* r, const yv_svo_host* svo) {
   if (!r || !svo) return YV_ERR_INVALID_ARG;
   return set_scene_impl(r, yv_svo_nodes(svo), yv_svo_node_count(svo), yv_svo_root(svo),

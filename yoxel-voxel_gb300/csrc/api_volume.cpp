@@ -275,6 +275,33 @@ yv_status yv_volume_render(const yv_volume_device* vol, const yv_camera* cams, i
   return YV_OK;
 }
 
+yv_status yv_volume_render_rgba8(const yv_volume_device* vol, const yv_camera* cams,
+                                 int32_t ncams, int32_t width, int32_t height,
+                                 const yv_march_params* mp, uint32_t* rgba8, void* stream) {
+  VolumeArgs* a = new (std::nothrow) VolumeArgs;
+  if (!a) return YV_ERR_OUT_OF_MEMORY;
+  if (!fill_args(vol, mp, width, height, a) || !cams_ok(cams, ncams) || !rgba8) {
+    delete a;
+    return YV_ERR_INVALID_ARG;
+  }
+  const size_t px = (size_t)width * (size_t)height;
+  for (int c0 = 0; c0 < ncams; c0 += kMaxVolumeCams) {
+    const int n = ncams - c0 < kMaxVolumeCams ? ncams - c0 : kMaxVolumeCams;
+    set_cams(a, cams + c0, n);
+    a->rgba = nullptr;
+    a->rgba8 = rgba8 + (size_t)c0 * px;
+    a->samples = nullptr;
+    a->bricks_entered = nullptr;
+    cudaError_t e = launch_volume_forward(*a, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) {
+      delete a;
+      return fail(e, "volume forward launch");
+    }
+  }
+  delete a;
+  return YV_OK;
+}
+
 yv_status yv_volume_backward(const yv_volume_device* vol, const yv_camera* cams, int32_t ncams,
                              int32_t width, int32_t height, const yv_march_params* mp,
                              const float* rgba, const float* grad_rgba, float* grad_density,

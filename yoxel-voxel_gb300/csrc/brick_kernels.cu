@@ -43,6 +43,20 @@ __device__ __forceinline__ bool ray_of_thread(const VolumeArgs& a, uint32_t tile
   return cam < a.ncams && x < a.width && y < a.height;
 }
 
+// RGBA8 pixel of a composited colour: each channel saturate(v) * 255
+// truncated, R in the low byte (float2uint of reaction/trace/utils.h:37-44,
+// the uchar4 image of RunTrace, ntree/ntree_trace.cuh:27).
+__device__ __forceinline__ uint32_t rgba8_of(float r, float g, float b, float al) {
+  const float v[4] = {r, g, b, al};
+  uint32_t out = 0;
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    const float x = v[c] < 0.f ? 0.f : (v[c] > 1.f ? 1.f : v[c]);
+    out |= __float2uint_rz(__fmul_rn(x, 255.f)) << (8 * c);
+  }
+  return out;
+}
+
 // kMinBlocks: resident blocks of 256 per SM the register allocation is
 // sized for.
 template <int P, int kMinBlocks>
@@ -65,6 +79,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) volume_forward_kernel(VolumeA
     bad |= r.bad;
     const size_t off = ((size_t)cam * a.height + (size_t)y) * a.width + (size_t)x;
     if (a.rgba) reinterpret_cast<float4*>(a.rgba)[off] = make_float4(r.c[0], r.c[1], r.c[2], r.a);
+    if (a.rgba8) a.rgba8[off] = rgba8_of(r.c[0], r.c[1], r.c[2], r.a);
     if (a.samples) a.samples[off] = r.samples;
     if (a.bricks_entered) a.bricks_entered[off] = r.bricks;
   }

@@ -707,6 +707,53 @@ static yv_leaf_attr decode_packed_voxdata(uint32_t v) {
   return a;
 }
 
+// The reference's packed VoxData of a host pool - in leaves and in every
+// node's data (the subtree at a coarser level, reaction/report/main.tex:61)
+// - decoded into attributes; leaves and node data then index them.
+static void decode_packed_pool(yv_svo_host* h) {
+  std::unordered_map<uint32_t, uint32_t> remap;
+  auto attr_of = [&](uint32_t v) {
+    auto it = remap.find(v);
+    if (it != remap.end()) return it->second;
+    const uint32_t idx = (uint32_t)h->attrs.size();
+    remap.emplace(v, idx);
+    h->attrs.push_back(decode_packed_voxdata(v));
+    return idx;
+  };
+  for (auto& n : h->nodes)
+    for (int ch = 0; ch < 8; ++ch)
+      if ((n.flags >> ch) & 1u) n.child[ch] = attr_of(n.child[ch]);
+  for (auto& n : h->nodes) n.data = attr_of(n.data);
+  h->lod = !h->nodes.empty();
+}
+
+static void set_depth(yv_svo_host* h) {
+  DeviceLayout dl;
+  std::string why;
+  if (build_device_layout(h->nodes.data(), (uint32_t)h->nodes.size(), h->root,
+                          (uint32_t)h->attrs.size(), &dl, &why) == YV_OK)
+    h->depth = dl.depth;
+}
+
+yv_status yv_svo_from_packed(yv_svo_host** out, const yv_vox_node* nodes, uint32_t count,
+                             uint32_t root) {
+  if (!out || (count && !nodes)) return YV_ERR_INVALID_ARG;
+  *out = nullptr;
+  yv_svo_host* h = nullptr;
+  try {
+    h = new yv_svo_host();
+    h->root = root;
+    h->nodes.assign(nodes, nodes + count);
+    decode_packed_pool(h);
+    set_depth(h);
+    *out = h;
+    return YV_OK;
+  } catch (const std::bad_alloc&) {
+    delete h;
+    return YV_ERR_OUT_OF_MEMORY;
+  }
+}
+
 yv_status yv_svo_load_vox(yv_svo_host** out, const char* path) {
   if (!out || !path) return YV_ERR_INVALID_ARG;
   *out = nullptr;
@@ -741,29 +788,10 @@ yv_status yv_svo_load_vox(yv_svo_host** out, const char* path) {
       char lod_magic[4];
       h->lod = std::fread(lod_magic, 1, 4, f) == 4 && std::memcmp(lod_magic, "YVLD", 4) == 0;
     } else {
-      // the reference's packed VoxData, in leaves and in every node's data
-      // (the subtree at a coarser level, reaction/report/main.tex:61)
-      std::unordered_map<uint32_t, uint32_t> remap;
-      auto attr_of = [&](uint32_t v) {
-        auto it = remap.find(v);
-        if (it != remap.end()) return it->second;
-        const uint32_t idx = (uint32_t)h->attrs.size();
-        remap.emplace(v, idx);
-        h->attrs.push_back(decode_packed_voxdata(v));
-        return idx;
-      };
-      for (auto& n : h->nodes)
-        for (int ch = 0; ch < 8; ++ch)
-          if ((n.flags >> ch) & 1u) n.child[ch] = attr_of(n.child[ch]);
-      for (auto& n : h->nodes) n.data = attr_of(n.data);
-      h->lod = !h->nodes.empty();
+      decode_packed_pool(h);
     }
     std::fclose(f);
-    DeviceLayout dl;
-    std::string why;
-    if (build_device_layout(h->nodes.data(), (uint32_t)h->nodes.size(), h->root,
-                            (uint32_t)h->attrs.size(), &dl, &why) == YV_OK)
-      h->depth = dl.depth;
+    set_depth(h);
     *out = h;
     return YV_OK;
   } catch (const std::bad_alloc&) {

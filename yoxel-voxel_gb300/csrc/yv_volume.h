@@ -42,7 +42,8 @@ struct VolumeArgs {
   int ncams, width, height;
   CamBasis cam[kMaxVolumeCams];
   // outputs / adjoint inputs
-  float* rgba;            // ncams*h*w float4
+  float* rgba;            // ncams*h*w float4 (optional if rgba8 is set)
+  uint32_t* rgba8;        // optional ncams*h*w RGBA8 (float2uint of trace.cu)
   uint32_t* samples;      // optional per-ray counters
   uint32_t* bricks_entered;
   const float* rgba_fwd;  // backward: forward output

@@ -138,6 +138,8 @@ _SIGS = {
     "yv_load_scene_vox": (S, [P, C.c_char_p]),
     "yv_set_scene_dense": (S, [P, P, P, C.c_int32, C.c_float, P]),
     "yv_set_scene_dynamic": (S, [P, P]),
+    "yv_set_scene_svo_packed": (S, [P, P, U32, U32]),
+    "yv_svo_from_packed": (S, [C.POINTER(P), P, U32, U32]),
     "yv_set_view_pos": (S, [P, F3]),
     "yv_set_view_dir": (S, [P, F3]),
     "yv_set_view_up": (S, [P, F3]),
@@ -176,6 +178,8 @@ _SIGS = {
     "yv_volume_gpu_desc": (S, [P, C.POINTER(VolumeDevice)]),
     "yv_volume_render": (S, [C.POINTER(VolumeDevice), C.POINTER(Camera), C.c_int32, C.c_int32,
                              C.c_int32, C.POINTER(MarchParams), P, P, P, P]),
+    "yv_volume_render_rgba8": (S, [C.POINTER(VolumeDevice), C.POINTER(Camera), C.c_int32,
+                                   C.c_int32, C.c_int32, C.POINTER(MarchParams), P, P]),
     "yv_volume_backward": (S, [C.POINTER(VolumeDevice), C.POINTER(Camera), C.c_int32,
                                C.c_int32, C.c_int32, C.POINTER(MarchParams), P, P, P, P, P]),
     "yv_volume_fold_aprons": (S, [C.POINTER(VolumeDevice), P, P, P]),

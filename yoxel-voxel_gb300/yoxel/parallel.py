@@ -46,6 +46,26 @@ def partition_tiles(tile_costs, world):
     return [(bounds[r], bounds[r + 1]) for r in range(world)]
 
 
+def tile_costs(pixel_cost, width, height):
+    """Cost per 8x4-pixel tile (row-major tiles, the order of
+    yv_render_frame_tiles) from a per-pixel cost map (h, w), e.g. the node
+    fetches of a previous frame; every tile costs at least 1."""
+    c = np.asarray(pixel_cost, np.float64).reshape(height, width)
+    tx, ty = (width + 7) // 8, (height + 3) // 4
+    pad = np.zeros((ty * 4, tx * 8), np.float64)
+    pad[:height, :width] = c
+    return pad.reshape(ty, 4, tx, 8).sum(axis=(1, 3)).reshape(-1) + 1.0
+
+
+def tile_rows(tile_range, width, height):
+    """Pixel rows [y0, y1) covered by a range of 8x4 tiles."""
+    tb, te = tile_range
+    tx = (width + 7) // 8
+    if te <= tb:
+        return 0, 0
+    return (tb // tx) * 4, min(height, ((te - 1) // tx + 1) * 4)
+
+
 def partition_cameras(ncams, world):
     """Contiguous camera ranges per rank (data parallelism over views)."""
     base, extra = divmod(ncams, world)

@@ -87,6 +87,15 @@ class Renderer:
                                        attrs.ctypes.data, len(attrs)), "SetSceneArrays")
         self._scene = (nodes, attrs)
 
+    def SetSceneSVOPacked(self, nodes, root):
+        """ISVORenderer::SetScene for a pool in the reference's packed leaf
+        format (SVOScene.from_packed), without a separate attribute array."""
+        from .svo import NODE_DTYPE
+        nodes = np.ascontiguousarray(nodes, dtype=NODE_DTYPE)
+        L.check(L.lib.yv_set_scene_svo_packed(self._h, nodes.ctypes.data, len(nodes), root),
+                "SetSceneSVOPacked")
+        self._scene = (nodes,)
+
     def SetViewPos(self, pos):
         L.check(L.lib.yv_set_view_pos(self._h, _f3(pos)), "SetViewPos")
 

@@ -54,6 +54,17 @@ class SVOScene:
         return cls(h.value)
 
     @classmethod
+    def from_packed(cls, nodes, root):
+        """A pool as the reference's SVOData holds it in memory: leaves and
+        node data carry the packed 16-bit colour + 16-bit normal VoxData,
+        decoded into leaf attributes (node ids kept)."""
+        nodes = np.ascontiguousarray(nodes, dtype=NODE_DTYPE)
+        h = C.c_void_p()
+        L.check(L.lib.yv_svo_from_packed(C.byref(h), nodes.ctypes.data, len(nodes), root),
+                "yv_svo_from_packed")
+        return cls(h.value)
+
+    @classmethod
     def build_dense(cls, density, depth, iso=0.0, rgb=None, stream=None):
         """GPU build from a dense CUDA float32 grid of (2^depth)^3 values
         (x fastest, e.g. a (G, G, G) tensor indexed [z, y, x]); rgb: CUDA

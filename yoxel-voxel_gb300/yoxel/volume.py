@@ -285,6 +285,22 @@ def render_volume(desc, cams, width, height, alpha_scale=1.0, step_vox=0.5, out=
     return out
 
 
+def render_volume_rgba8(desc, cams, width, height, alpha_scale=1.0, step_vox=0.5, out=None,
+                        stream=None):
+    """RGBA8 frames (ntree RunTrace's uchar4 image): (ncams, h, w) int32 CUDA
+    tensor, R in the low byte, each channel saturate(v) * 255 truncated."""
+    torch = _torch()
+    ca = cams if isinstance(cams, C.Array) else cameras(cams)
+    n = len(ca)
+    if out is None:
+        out = torch.empty((n, height, width), dtype=torch.int32, device="cuda")
+    mp = L.MarchParams(float(alpha_scale), float(step_vox))
+    L.check(L.lib.yv_volume_render_rgba8(C.byref(desc), ca, n, width, height, C.byref(mp),
+                                         C.c_void_p(out.data_ptr()), _stream(stream)),
+            "yv_volume_render_rgba8")
+    return out
+
+
 def volume_backward(desc, cams, width, height, rgba, grad_rgba, grad_density, grad_albedo,
                     alpha_scale=1.0, step_vox=0.5, fold=True, stream=None):
     ca = cams if isinstance(cams, C.Array) else cameras(cams)
