@@ -180,3 +180,24 @@ def test_oracle_march_matches_reference_castray_live_128(oracle, yoxel_mod):
     ours = oracle_march_as_reference(oracle, yoxel_mod, vol, eye, dirs)
     assert (ref[:, 3] > 0.5).mean() > 0.5
     assert np.abs(ours - ref).max() <= 2e-5
+
+
+def test_integration_subclass_compiles_against_the_reference_headers(tmp_path):
+    """The ISVORenderer subclass INTEGRATION.md gives a maintainer compiles
+    against the reference's own cell/svorenderer.h and svodata.h (with the
+    stand-ins for the headers the snapshot lacks) and the C ABI header."""
+    import re
+    import subprocess
+    from oracle import pyref
+    if not pyref.available():
+        pytest.skip("reference checkout not present")
+    txt = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    block = re.search(r"```cpp\n(#include \"svorenderer.h\".*?)```", txt, re.S).group(1)
+    src = tmp_path / "gb300_renderer.cpp"
+    src.write_text('#include "stdafx.h"\n#include <map>\n' + block)
+    ref = pyref._builder().reference_root()
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only",
+                        "-I" + os.path.join(ROOT, "oracle", "ref_shim"),
+                        "-I" + os.path.join(ref, "cell"), "-I" + os.path.join(ROOT, "include"),
+                        str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
