@@ -373,6 +373,14 @@ typedef struct yv_volume_device {
   int32_t precision;
   const int32_t* nbr_up;
   const int32_t* nbr_dn;
+  /* optional (NULL = none): per brick 16 words, bit (y & 3) * 8 + x of word
+   * z * 2 + (y >> 2) set where trilinear cell (x, y, z) has a non-zero
+   * density corner.  The forward march passes over the samples of cells
+   * without one (they add nothing: alpha 0), counting them as taken.  Pools
+   * owned by the library (yv_volume_upload, yv_volume_upload_dense,
+   * yv_volume_rebuild_dense) carry it; a pool whose densities change between
+   * frames (the learnable tensors) leaves it NULL. */
+  const uint32_t* cell_mask;
 } yv_volume_device;
 
 /* Device copy owned by the library (BrickPool<T>, ntree/BrickManager.h). */

@@ -325,3 +325,48 @@ def test_more_cameras_than_one_launch_holds(yoxel_mod):
     assert float((gd - gd2).norm() / gd.norm()) < 1e-5
     assert float((ga - ga2).norm() / ga.norm()) < 1e-5
     assert gd.abs().sum() > 0
+
+
+@pytest.mark.parametrize("precision", [0, 1, 2, 3])
+def test_cell_mask_and_empty_cell_skipping(yoxel_mod, precision):
+    """The occupancy mask of a library-owned pool marks exactly the trilinear
+    cells with a non-zero density corner (as stored: fp16 formats round),
+    and skipping the samples of unmarked cells changes no output bit: the
+    same frame, sample counts included, with the mask removed."""
+    import torch
+    vol = yoxel_mod.BrickVolume.noise(2, 0.4, 1.4, 17)
+    gv = vol.upload(precision)
+    desc = gv.desc()
+    assert desc.cell_mask
+    nb = vol.nbricks
+
+    class _DeviceWords:  # a view of the library's device array
+        __cuda_array_interface__ = {"shape": (nb * 16,), "typestr": "<i4",
+                                    "data": (desc.cell_mask, False), "version": 2}
+
+    got = torch.as_tensor(_DeviceWords(), device="cuda").cpu().numpy().view(np.uint32)
+    den, _ = gpu_inputs(vol, precision)
+    nz = den.reshape(nb, 9, 9, 9) != 0
+    cell = np.zeros((nb, 8, 8, 8), bool)
+    for j in range(8):
+        dx, dy, dz = j & 1, (j >> 1) & 1, j >> 2
+        cell |= nz[:, dz:dz + 8, dy:dy + 8, dx:dx + 8]
+    expect = np.zeros((nb, 16), np.uint32)
+    for z in range(8):
+        for y in range(8):
+            for x in range(8):
+                expect[:, z * 2 + (y >> 2)] |= cell[:, z, y, x].astype(np.uint32) << np.uint32(
+                    ((y & 3) << 3) | x)
+    assert np.array_equal(got.reshape(nb, 16), expect)
+    assert 0 < cell.mean() < 1
+    cams = [cam_at([1.6, 1.3, 1.1]), cam_at([-0.7, 0.4, 0.9], 50.0)]
+    w, h = 96, 80
+    outs = []
+    for use_mask in (True, False):
+        d = gv.desc()
+        if not use_mask:
+            d.cell_mask = None
+        ns = torch.zeros((2, h, w), dtype=torch.int32, device="cuda")
+        rgba = yoxel_mod.render_volume(d, cams, w, h, samples=ns)
+        outs.append((rgba.cpu().numpy().view(np.uint32), ns.cpu().numpy()))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])

@@ -21,6 +21,8 @@ struct yv_volume_gpu {
   yv_volume_device desc;
   void* mem[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   size_t cap[5] = {0, 0, 0, 0, 0};  // bytes allocated per array (reused by rebuilds)
+  uint32_t* mask = nullptr;         // cell occupancy mask (16 words per brick)
+  size_t mask_cap = 0;
 };
 
 namespace {
@@ -77,6 +79,7 @@ bool fill_args(const yv_volume_device* v, const yv_march_params* mp, int width, 
   a->v.albedo = v->albedo;
   a->v.nbricks = v->nbricks;
   a->v.precision = v->precision;
+  a->v.cell_mask = v->cell_mask;
   a->nbr_up = v->nbr_up;
   a->nbr_dn = v->nbr_dn;
   a->v.S = (float)(8 * a->v.nb);
@@ -127,7 +130,39 @@ yv_status volume_gpu_from_device(void* mem[5], const size_t bytes[5], const yv_v
     g->cap[i] = mem[i] ? bytes[i] : 0;
   }
   g->desc = d;
+  g->desc.cell_mask = nullptr;
   *out = g;
+  return YV_OK;
+}
+
+yv_status volume_gpu_refresh_mask(yv_volume_gpu* g, cudaStream_t s) {
+  const size_t bytes = (size_t)g->desc.nbricks * 16u * sizeof(uint32_t);
+  g->desc.cell_mask = nullptr;
+  if (!bytes) return YV_OK;
+  cudaError_t e = cudaSuccess;
+  if (g->mask_cap < bytes) {
+    // the old mask may still be read by queued work on `s`
+    if (g->mask) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess) {
+      cudaFree(g->mask);
+      g->mask = nullptr;
+      g->mask_cap = 0;
+      e = cudaMalloc(&g->mask, bytes);
+    }
+    if (e != cudaSuccess) return fail(e, "cell mask");
+    g->mask_cap = bytes;
+  }
+  yv_march_params mp = {1.0f, 0.5f};
+  VolumeArgs* a = new (std::nothrow) VolumeArgs;
+  if (!a) return YV_ERR_OUT_OF_MEMORY;
+  if (!fill_args(&g->desc, &mp, 1, 1, a)) {
+    delete a;
+    return YV_ERR_INVALID_ARG;
+  }
+  e = launch_cell_mask(a->v, g->mask, s);
+  delete a;
+  if (e != cudaSuccess) return fail(e, "cell mask");
+  g->desc.cell_mask = g->mask;
   return YV_OK;
 }
 
@@ -232,6 +267,13 @@ yv_status yv_volume_upload(const yv_volume_host* v, int32_t precision, yv_volume
   g->desc.precision = precision;
   g->desc.nbr_up = static_cast<const int32_t*>(g->mem[3]);
   g->desc.nbr_dn = static_cast<const int32_t*>(g->mem[4]);
+  g->desc.cell_mask = nullptr;
+  yv_status st = volume_gpu_refresh_mask(g, nullptr);
+  cudaError_t e = st == YV_OK ? cudaStreamSynchronize(nullptr) : cudaSuccess;
+  if (st != YV_OK || e != cudaSuccess) {
+    yv_volume_gpu_free(g);
+    return st != YV_OK ? st : fail(e, "cell mask");
+  }
   *out = g;
   return YV_OK;
 }
@@ -240,6 +282,7 @@ void yv_volume_gpu_free(yv_volume_gpu* g) {
   if (!g) return;
   cudaSetDevice(g->device);
   for (void* p : g->mem) cudaFree(p);
+  cudaFree(g->mask);
   delete g;
 }
 

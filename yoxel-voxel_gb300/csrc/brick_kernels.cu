@@ -189,6 +189,28 @@ __global__ void __launch_bounds__(256, kMinBlocks) volume_backward_kernel(Volume
   if (bad && a.status) atomicOr(a.status, 4u);
 }
 
+// Cell occupancy mask: one warp per mask word - the 32 cells (x, y) of four
+// rows of one z layer of a brick - sets the bit of every cell with a
+// non-zero density corner, as the march reads the corners (format P).
+template <int P>
+__global__ void cell_mask_kernel(VolumeView v, uint32_t* mask) {
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= v.nbricks * 16u) return;  // uniform across the warp
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t b = warp >> 4, word = warp & 15u;
+  const uint32_t z = word >> 1, y = (word & 1u) * 4u + (lane >> 3), x = lane & 7u;
+  const uint32_t base = b * (uint32_t)kL3 + (z * kL + y) * kL + x;
+  bool any = false;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    float d, c[3];
+    Voxel<P>::corner(v, base + corner_offset(j), d, c);
+    any |= d != 0.f;
+  }
+  const uint32_t bits = __ballot_sync(0xFFFFFFFFu, any);
+  if (lane == 0) mask[warp] = bits;
+}
+
 // Apron fold, pass 1: every owned lattice point (x,y,z < 8) adds the
 // gradient its copies received in the aprons of the lower neighbours.
 __global__ void fold_gather_kernel(VolumeArgs a, int channels, float* g) {
@@ -290,6 +312,19 @@ cudaError_t launch_volume_backward(const VolumeArgs& a, cudaStream_t s) {
     volume_backward_kernel<2, kBackwardMinBlocks><<<blocks, 256, 0, s>>>(a);
   else
     return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cell_mask(const VolumeView& v, uint32_t* mask, cudaStream_t s) {
+  if (!v.nbricks) return cudaSuccess;
+  const uint32_t threads = v.nbricks * 16u * 32u;
+  const uint32_t blocks = (threads + 255u) / 256u;
+  switch (v.precision) {
+    case 0: cell_mask_kernel<0><<<blocks, 256, 0, s>>>(v, mask); break;
+    case 1: cell_mask_kernel<1><<<blocks, 256, 0, s>>>(v, mask); break;
+    case 2: cell_mask_kernel<2><<<blocks, 256, 0, s>>>(v, mask); break;
+    default: cell_mask_kernel<3><<<blocks, 256, 0, s>>>(v, mask); break;
+  }
   return cudaGetLastError();
 }
 

@@ -333,10 +333,27 @@ __device__ __forceinline__ void march(const VolumeView& a, const uint32_t* sg, u
       for (int it = 0; it < 1 << 16; ++it, ++k) {
         const float t = fmul((float)k, a.dt);
         if (!(t < t_out)) break;
-        SampleCtx s;
         float lc[3], le[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) sample_coord(t, D[i], Lh[i], Ll[i], lc[i], le[i]);
+        if (kColor && a.cell_mask) {
+          // a cell whose 8 corners are all zero has sigma = 0, alpha = 0:
+          // the sample adds exactly nothing (C, A unchanged), so the
+          // forward passes over it; the replay of the adjoint, whose
+          // density gradient reaches such samples, takes every sample
+          int kc[3];
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            const int kk = __float2int_rd(lc[i]);
+            kc[i] = kk < 0 ? 0 : (kk > 7 ? 7 : kk);
+          }
+          const uint32_t mw = __ldg(a.cell_mask + (size_t)b * 16u + (uint32_t)(kc[2] * 2 + (kc[1] >> 2)));
+          if (!((mw >> (((kc[1] & 3) << 3) | kc[0])) & 1u)) {
+            ++r.samples;
+            continue;
+          }
+        }
+        SampleCtx s;
         eval_sample<P>(a, b, lc, le, s);
         const float T = fsub(1.f, A);
         const float w = fmul(T, s.alpha);

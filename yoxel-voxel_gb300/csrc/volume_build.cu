@@ -528,16 +528,26 @@ yv_status upload_dense(const float* density, const uint8_t* rgb, int32_t levels,
   d.precision = precision;
   d.nbr_up = static_cast<const int32_t*>(mem[3]);
   d.nbr_dn = static_cast<const int32_t*>(mem[4]);
+  d.cell_mask = nullptr;
   if (into) {
     *desc = d;
-    return YV_OK;
+    return volume_gpu_refresh_mask(into, s);
   }
   // a new volume: its buffers are complete once the stream gets here
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) {
     for (void* p : fresh) cudaFree(p);
     return vbuild_fail(e, "device pool");
   }
-  return volume_gpu_from_device(fresh, bytes, d, out);
+  yv_status mst = volume_gpu_from_device(fresh, bytes, d, out);
+  if (mst != YV_OK) return mst;
+  mst = volume_gpu_refresh_mask(*out, s);
+  if (mst == YV_OK && (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    mst = vbuild_fail(e, "cell mask");
+  if (mst != YV_OK) {
+    yv_volume_gpu_free(*out);
+    *out = nullptr;
+  }
+  return mst;
 }
 
 }  // namespace

@@ -2,6 +2,8 @@
 // the scene builders and the kernel launchers.  Not part of the public ABI.
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -103,6 +105,9 @@ yv_status volume_host_from_parts(int levels, std::vector<uint32_t>&& grids,
 // d (api_volume.cpp).
 yv_status volume_gpu_from_device(void* mem[5], const size_t bytes[5], const yv_volume_device& d,
                                  yv_volume_gpu** out);
+// (Re)computes the cell occupancy mask of a library-owned volume on `s`
+// (after its pool changed) and points its descriptor at it.
+yv_status volume_gpu_refresh_mask(yv_volume_gpu* g, cudaStream_t s);
 // The owned buffers, their allocated sizes and the descriptor of a volume
 // (for rebuilds in place).
 yv_status volume_gpu_arrays(yv_volume_gpu* g, void*** mem, size_t** cap, yv_volume_device** d);

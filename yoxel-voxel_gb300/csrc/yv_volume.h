@@ -27,6 +27,9 @@ struct VolumeView {
                          // 3: uint2 {fp16 density | r<<16 | g<<24, b}
   uint32_t nbricks;
   int precision;
+  // per brick 16 words: bit (y & 3) * 8 + x of word z * 2 + (y >> 2) set
+  // where trilinear cell (x, y, z) has a non-zero density corner; null = none
+  const uint32_t* cell_mask;
   // march
   float S;               // lattice cells per axis
   float cell_size;       // world size of a brick cell = 8/S
@@ -67,5 +70,7 @@ cudaError_t launch_unpack_grads(const float4* packed, uint32_t n, float* grad_de
 cudaError_t launch_apron_fold(const VolumeArgs& a, int channels, float* g, bool gather,
                               cudaStream_t s);
 int device_sm_count_vol();
+// mask[b * 16 + w] for the nbricks bricks of v (cell_mask of VolumeView).
+cudaError_t launch_cell_mask(const VolumeView& v, uint32_t* mask, cudaStream_t s);
 
 }  // namespace yv

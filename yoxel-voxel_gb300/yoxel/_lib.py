@@ -88,7 +88,8 @@ class LaunchConfig(C.Structure):
 class VolumeDevice(C.Structure):
     _fields_ = [("grids", C.c_void_p), ("ngrids", C.c_uint32), ("levels", C.c_int32),
                 ("density", C.c_void_p), ("albedo", C.c_void_p), ("nbricks", C.c_uint32),
-                ("precision", C.c_int32), ("nbr_up", C.c_void_p), ("nbr_dn", C.c_void_p)]
+                ("precision", C.c_int32), ("nbr_up", C.c_void_p), ("nbr_dn", C.c_void_p),
+                ("cell_mask", C.c_void_p)]
 
 
 class Camera(C.Structure):
