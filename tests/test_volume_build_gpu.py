@@ -93,3 +93,42 @@ def test_rebuild_in_place_renders_like_fresh_build(yoxel_mod, precision):
         x = yoxel_mod.render_volume(vol.desc(), cams, 40, 32)
         y = yoxel_mod.render_volume(fresh.desc(), cams, 40, 32)
         assert torch.equal(x.view(torch.int32), y.view(torch.int32))
+
+
+def device_mask(desc):
+    """The cell occupancy mask words of a device pool (a view of the
+    library's array)."""
+    import torch
+    n = desc.nbricks * 16
+
+    class _Words:
+        __cuda_array_interface__ = {"shape": (n,), "typestr": "<i4",
+                                    "data": (desc.cell_mask, False), "version": 2}
+
+    return torch.as_tensor(_Words(), device="cuda").cpu().numpy().view(np.uint32)
+
+
+@pytest.mark.parametrize("precision", [0, 1, 2, 3])
+def test_pack_kernel_cell_mask_matches_upload(yoxel_mod, precision):
+    """The occupancy mask the pack kernel builds with a device pool (from a
+    lattice, and rebuilt in place) equals the mask computed from the stored
+    corners of an upload of the host build - lattice values that the fp16
+    formats round to zero included."""
+    import torch
+    levels = 2
+    d = lattice(levels, 6, "blobs")
+    rng = np.random.default_rng(7)
+    tiny = rng.random(d.shape) < 0.002
+    d[tiny] = np.float32(1e-9)  # non-zero in fp32, zero once stored as fp16
+    host = yoxel_mod.BrickVolume.from_dense(levels, d)
+    up = host.upload(precision)
+    gv = yoxel_mod.VolumeGPU.from_dense(torch.from_numpy(d).cuda(), levels, precision)
+    assert gv.desc().cell_mask and gv.desc().nbricks == host.nbricks
+    want = device_mask(up.desc())
+    assert np.array_equal(device_mask(gv.desc()), want)
+    assert 0 < np.unpackbits(want.view(np.uint8)).mean() < 1
+    # in place, over a pool that held other bricks
+    other = yoxel_mod.VolumeGPU.from_dense(torch.from_numpy(lattice(levels, 12, "blobs")).cuda(),
+                                           levels, precision)
+    other.rebuild_dense(torch.from_numpy(d).cuda(), levels)
+    assert np.array_equal(device_mask(other.desc()), want)

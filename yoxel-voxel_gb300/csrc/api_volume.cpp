@@ -118,10 +118,11 @@ bool cams_ok(const yv_camera* c, int n) {
 namespace yv {
 
 yv_status volume_gpu_from_device(void* mem[5], const size_t bytes[5], const yv_volume_device& d,
-                                 yv_volume_gpu** out) {
+                                 yv_volume_gpu** out, uint32_t* mask) {
   yv_volume_gpu* g = new (std::nothrow) yv_volume_gpu();
   if (!g) {
     for (int i = 0; i < 5; ++i) cudaFree(mem[i]);
+    cudaFree(mask);
     return YV_ERR_OUT_OF_MEMORY;
   }
   cudaGetDevice(&g->device);
@@ -130,14 +131,17 @@ yv_status volume_gpu_from_device(void* mem[5], const size_t bytes[5], const yv_v
     g->cap[i] = mem[i] ? bytes[i] : 0;
   }
   g->desc = d;
-  g->desc.cell_mask = nullptr;
+  g->desc.cell_mask = mask;
+  g->mask = mask;
+  g->mask_cap = mask ? (size_t)d.nbricks * 16u * sizeof(uint32_t) : 0;
   *out = g;
   return YV_OK;
 }
 
-yv_status volume_gpu_refresh_mask(yv_volume_gpu* g, cudaStream_t s) {
-  const size_t bytes = (size_t)g->desc.nbricks * 16u * sizeof(uint32_t);
-  g->desc.cell_mask = nullptr;
+yv_status volume_gpu_mask_buffer(yv_volume_gpu* g, uint32_t nbricks, cudaStream_t s,
+                                 uint32_t** mask) {
+  const size_t bytes = (size_t)nbricks * 16u * sizeof(uint32_t);
+  *mask = nullptr;
   if (!bytes) return YV_OK;
   cudaError_t e = cudaSuccess;
   if (g->mask_cap < bytes) {
@@ -147,11 +151,22 @@ yv_status volume_gpu_refresh_mask(yv_volume_gpu* g, cudaStream_t s) {
       cudaFree(g->mask);
       g->mask = nullptr;
       g->mask_cap = 0;
+      g->desc.cell_mask = nullptr;
       e = cudaMalloc(&g->mask, bytes);
     }
     if (e != cudaSuccess) return fail(e, "cell mask");
     g->mask_cap = bytes;
   }
+  *mask = static_cast<uint32_t*>(g->mask);
+  return YV_OK;
+}
+
+yv_status volume_gpu_refresh_mask(yv_volume_gpu* g, cudaStream_t s) {
+  uint32_t* mask = nullptr;
+  yv_status st = volume_gpu_mask_buffer(g, g->desc.nbricks, s, &mask);
+  g->desc.cell_mask = nullptr;
+  if (st != YV_OK || !mask) return st;
+  cudaError_t e;
   yv_march_params mp = {1.0f, 0.5f};
   VolumeArgs* a = new (std::nothrow) VolumeArgs;
   if (!a) return YV_ERR_OUT_OF_MEMORY;
@@ -159,10 +174,10 @@ yv_status volume_gpu_refresh_mask(yv_volume_gpu* g, cudaStream_t s) {
     delete a;
     return YV_ERR_INVALID_ARG;
   }
-  e = launch_cell_mask(a->v, g->mask, s);
+  e = launch_cell_mask(a->v, mask, s);
   delete a;
   if (e != cudaSuccess) return fail(e, "cell mask");
-  g->desc.cell_mask = g->mask;
+  g->desc.cell_mask = mask;
   return YV_OK;
 }
 

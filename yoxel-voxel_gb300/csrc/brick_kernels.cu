@@ -59,7 +59,8 @@ __device__ __forceinline__ uint32_t rgba8_of(float r, float g, float b, float al
 
 // kMinBlocks: resident blocks of 256 per SM the register allocation is
 // sized for.
-template <int P, int kMinBlocks>
+// kSkip: the pool carries a cell occupancy mask (a learnable pool does not).
+template <int P, int kMinBlocks, bool kSkip>
 __global__ void __launch_bounds__(256, kMinBlocks) volume_forward_kernel(VolumeArgs a) {
   // grid nodes are read through L1 (see prefer_l1)
   const uint32_t* sg = nullptr;
@@ -75,7 +76,7 @@ __global__ void __launch_bounds__(256, kMinBlocks) volume_forward_kernel(VolumeA
     pixel_ray(a.cam[cam], x, y, o, d);
     NoVis nv;
     RayOut r;
-    march<P>(a.v, sg, nsg, o, d, nv, r);
+    march<P, NoVis, true, kSkip>(a.v, sg, nsg, o, d, nv, r);
     bad |= r.bad;
     const size_t off = ((size_t)cam * a.height + (size_t)y) * a.width + (size_t)x;
     if (a.rgba) reinterpret_cast<float4*>(a.rgba)[off] = make_float4(r.c[0], r.c[1], r.c[2], r.a);
@@ -266,11 +267,15 @@ void prefer_l1() {
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64 || done[dev]) return;
   const cudaFuncAttribute k = cudaFuncAttributePreferredSharedMemoryCarveout;
-  const cudaError_t e[6] = {
-      cudaFuncSetAttribute(volume_forward_kernel<0, ForwardBlocks<0>::value>, k, 0),
-      cudaFuncSetAttribute(volume_forward_kernel<1, ForwardBlocks<1>::value>, k, 0),
-      cudaFuncSetAttribute(volume_forward_kernel<2, ForwardBlocks<2>::value>, k, 0),
-      cudaFuncSetAttribute(volume_forward_kernel<3, ForwardBlocks<3>::value>, k, 0),
+  const cudaError_t e[10] = {
+      cudaFuncSetAttribute(volume_forward_kernel<0, ForwardBlocks<0>::value, false>, k, 0),
+      cudaFuncSetAttribute(volume_forward_kernel<0, ForwardBlocks<0>::value, true>, k, 0),
+      cudaFuncSetAttribute(volume_forward_kernel<1, ForwardBlocks<1>::value, false>, k, 0),
+      cudaFuncSetAttribute(volume_forward_kernel<1, ForwardBlocks<1>::value, true>, k, 0),
+      cudaFuncSetAttribute(volume_forward_kernel<2, ForwardBlocks<2>::value, false>, k, 0),
+      cudaFuncSetAttribute(volume_forward_kernel<2, ForwardBlocks<2>::value, true>, k, 0),
+      cudaFuncSetAttribute(volume_forward_kernel<3, ForwardBlocks<3>::value, false>, k, 0),
+      cudaFuncSetAttribute(volume_forward_kernel<3, ForwardBlocks<3>::value, true>, k, 0),
       cudaFuncSetAttribute(volume_backward_kernel<1, kBackwardMinBlocks>, k, 0),
       cudaFuncSetAttribute(volume_backward_kernel<2, kBackwardMinBlocks>, k, 0)};
   // a hint: a refusal keeps the default configuration and is not reported
@@ -290,11 +295,32 @@ cudaError_t launch_volume_forward(const VolumeArgs& a, cudaStream_t s) {
   const uint32_t blocks = (tiles + 7) / 8;
   if (blocks == 0) return cudaSuccess;
   prefer_l1();
+  const bool skip = a.v.cell_mask != nullptr;
   switch (a.v.precision) {
-    case 0: volume_forward_kernel<0, ForwardBlocks<0>::value><<<blocks, 256, 0, s>>>(a); break;
-    case 1: volume_forward_kernel<1, ForwardBlocks<1>::value><<<blocks, 256, 0, s>>>(a); break;
-    case 2: volume_forward_kernel<2, ForwardBlocks<2>::value><<<blocks, 256, 0, s>>>(a); break;
-    case 3: volume_forward_kernel<3, ForwardBlocks<3>::value><<<blocks, 256, 0, s>>>(a); break;
+    case 0:
+      if (skip)
+        volume_forward_kernel<0, ForwardBlocks<0>::value, true><<<blocks, 256, 0, s>>>(a);
+      else
+        volume_forward_kernel<0, ForwardBlocks<0>::value, false><<<blocks, 256, 0, s>>>(a);
+      break;
+    case 1:
+      if (skip)
+        volume_forward_kernel<1, ForwardBlocks<1>::value, true><<<blocks, 256, 0, s>>>(a);
+      else
+        volume_forward_kernel<1, ForwardBlocks<1>::value, false><<<blocks, 256, 0, s>>>(a);
+      break;
+    case 2:
+      if (skip)
+        volume_forward_kernel<2, ForwardBlocks<2>::value, true><<<blocks, 256, 0, s>>>(a);
+      else
+        volume_forward_kernel<2, ForwardBlocks<2>::value, false><<<blocks, 256, 0, s>>>(a);
+      break;
+    case 3:
+      if (skip)
+        volume_forward_kernel<3, ForwardBlocks<3>::value, true><<<blocks, 256, 0, s>>>(a);
+      else
+        volume_forward_kernel<3, ForwardBlocks<3>::value, false><<<blocks, 256, 0, s>>>(a);
+      break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

@@ -261,7 +261,9 @@ struct RayOut {
 // before the sample).
 // kColor = false (the adjoint's replay): the composited colour is not
 // accumulated (the visitor tracks what it needs; r.c stays 0).
-template <int P, class Vis, bool kColor = true>
+// kSkip: the forward passes over the samples of cells the pool's
+// cell_mask marks empty (compiled out for pools without one).
+template <int P, class Vis, bool kColor = true, bool kSkip = kColor>
 __device__ __forceinline__ void march(const VolumeView& a, const uint32_t* sg, uint32_t nsg,
                                       const float* o, const float* d, Vis& vis, RayOut& r) {
   r.c[0] = r.c[1] = r.c[2] = 0.f;
@@ -336,7 +338,7 @@ __device__ __forceinline__ void march(const VolumeView& a, const uint32_t* sg, u
         float lc[3], le[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) sample_coord(t, D[i], Lh[i], Ll[i], lc[i], le[i]);
-        if (kColor && a.cell_mask) {
+        if (kColor && kSkip && a.cell_mask) {
           // a cell whose 8 corners are all zero has sigma = 0, alpha = 0:
           // the sample adds exactly nothing (C, A unchanged), so the
           // forward passes over it; the replay of the adjoint, whose

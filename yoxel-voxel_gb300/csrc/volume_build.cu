@@ -206,12 +206,27 @@ __device__ __forceinline__ uint16_t f16_saturating(float f) {
 // Pack: one warp per brick, its 729 lattice values (and RGB).  format < 0:
 // fp32 density + uint8 RGB (host container layout); else a device pool
 // format (YV_PRECISION_*), written to d_out / a_out.
+// mask (device pools, optional): the cell occupancy mask of the march (16
+// words per brick, bit (y & 3) * 8 + x of word z * 2 + (y >> 2) set where
+// trilinear cell (x, y, z) has a non-zero stored density corner), from a
+// 729-bit non-zero map of the brick's lattice the warp gathers by ballots
+// while it packs (blocks of 256 threads).
+__device__ __forceinline__ uint32_t lattice_row9(const uint32_t* bits, int off) {
+  const int w = off >> 5, sh = off & 31;
+  uint32_t v = bits[w] >> sh;
+  if (sh > 23) v |= bits[w + 1] << (32 - sh);
+  return v & 0x1FFu;
+}
+
 __global__ void pack_bricks_kernel(Lattice g, const uint64_t* cells, uint32_t nbricks, int format,
                                    float* dens, uint8_t* rgb, void* d_out, void* a_out,
-                                   int32_t* cell_xyz, int32_t* map) {
+                                   int32_t* cell_xyz, int32_t* map, uint32_t* mask) {
+  __shared__ uint32_t nzbits[8][24];
   const uint32_t lane = threadIdx.x & 31u;
+  uint32_t* nz = nzbits[(threadIdx.x >> 5) & 7u];
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nbs = __ffs(g.nb) - 1;
+  const bool half = format == YV_PRECISION_F16 || format == YV_PRECISION_F16_PACKED;
   for (uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < nbricks; b += nwarps) {
     const uint64_t c = cells[b];
     const int cx = (int)(c & (uint64_t)(g.nb - 1)), cy = (int)((c >> nbs) & (uint64_t)(g.nb - 1)),
@@ -226,12 +241,23 @@ __global__ void pack_bricks_kernel(Lattice g, const uint64_t* cells, uint32_t nb
     // any is used
     for (int q0 = 0; q0 < (kVL3 + 31) / 32; q0 += 8) {
       float pv[8];
+      uint32_t nzf = 0;
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int k = (int)lane + 32 * (q0 + u);
         pv[u] = k < kVL3 ? __ldg(g.d + lat(g, cx * kVB + k % kVL, cy * kVB + (k / kVL) % kVL,
                                             cz * kVB + k / (kVL * kVL)))
                          : 0.f;
+        // non-zero as stored (the fp16 formats round small values to 0)
+        const bool nzv = half ? (f16_saturating(pv[u]) & 0x7FFFu) != 0 : pv[u] != 0.f;
+        nzf |= (k < kVL3 && nzv ? 1u : 0u) << u;
+      }
+      if (mask) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const uint32_t bits = __ballot_sync(0xFFFFFFFFu, (nzf >> u) & 1u);
+          if (lane == 0 && q0 + u < 24) nz[q0 + u] = bits;
+        }
       }
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
@@ -271,6 +297,25 @@ __global__ void pack_bricks_kernel(Lattice g, const uint64_t* cells, uint32_t nb
                          (uint32_t)bb);
         }
       }
+    }
+    if (mask) {
+      if (lane == 0) nz[23] = 0u;  // beyond the 729 points
+      __syncwarp();
+      if (lane < 16u) {
+        const int z = (int)(lane >> 1), y0 = (int)(lane & 1u) * 4;
+        uint32_t word = 0;
+        for (int yy = 0; yy < 4; ++yy) {
+          uint32_t rows = 0;
+          for (int dz = 0; dz < 2; ++dz)
+            for (int dy = 0; dy < 2; ++dy) {
+              const uint32_t r9 = lattice_row9(nz, (z + dz) * 81 + (y0 + yy + dy) * 9);
+              rows |= r9 | (r9 >> 1);  // cell x holds point x or x + 1
+            }
+          word |= (rows & 0xFFu) << (8 * yy);
+        }
+        mask[(size_t)b * 16u + lane] = word;
+      }
+      __syncwarp();
     }
   }
 }
@@ -429,7 +474,7 @@ yv_status yv_volume_build_dense(const float* density, const uint8_t* rgb, int32_
   if (t.nbricks)
     pack_bricks_kernel<<<grid_for((uint64_t)t.nbricks * 32), 256, 0, s>>>(
         g, t.cells.as<uint64_t>(), t.nbricks, -1, dens.as<float>(), col.as<uint8_t>(), nullptr,
-        nullptr, cxyz.as<int32_t>(), map.as<int32_t>());
+        nullptr, cxyz.as<int32_t>(), map.as<int32_t>(), nullptr);
   if ((e = cudaGetLastError()) != cudaSuccess) return vbuild_fail(e, "pack");
   std::vector<uint32_t> grids((size_t)t.ngrids * 64);
   std::vector<float> hd(n);
@@ -498,6 +543,16 @@ yv_status upload_dense(const float* density, const uint8_t* rgb, int32_t levels,
     e = cudaMalloc(&mem[i], bytes[i]);
     if (e == cudaSuccess && cap) cap[i] = bytes[i];
   }
+  // the cell occupancy mask, computed by the pack kernel
+  uint32_t* mask = nullptr;
+  if (e == cudaSuccess && t.nbricks) {
+    if (into) {
+      const yv_status mst = volume_gpu_mask_buffer(into, t.nbricks, s, &mask);
+      if (mst != YV_OK) return mst;
+    } else {
+      e = cudaMalloc(&mask, (size_t)t.nbricks * 16u * sizeof(uint32_t));
+    }
+  }
   DevBuf cxyz, map;
   if (e == cudaSuccess) e = cxyz.alloc((size_t)t.nbricks * 12, s);
   if (e == cudaSuccess) e = map.alloc(cells * 4, s);
@@ -507,15 +562,17 @@ yv_status upload_dense(const float* density, const uint8_t* rgb, int32_t levels,
   if (e == cudaSuccess && t.nbricks) {
     pack_bricks_kernel<<<grid_for((uint64_t)t.nbricks * 32), 256, 0, s>>>(
         g, t.cells.as<uint64_t>(), t.nbricks, precision, nullptr, nullptr, mem[1], mem[2],
-        cxyz.as<int32_t>(), map.as<int32_t>());
+        cxyz.as<int32_t>(), map.as<int32_t>(), mask);
     neighbors_kernel<<<grid_for(t.nbricks), 256, 0, s>>>(
         cxyz.as<int32_t>(), map.as<int32_t>(), t.nbricks, g.nb, static_cast<int32_t*>(mem[3]),
         static_cast<int32_t*>(mem[4]));
     e = cudaGetLastError();
   }
   if (e != cudaSuccess) {
-    if (!into)
+    if (!into) {
       for (void* p : fresh) cudaFree(p);
+      cudaFree(mask);
+    }
     return vbuild_fail(e, "device pool");
   }
   yv_volume_device d;
@@ -528,26 +585,18 @@ yv_status upload_dense(const float* density, const uint8_t* rgb, int32_t levels,
   d.precision = precision;
   d.nbr_up = static_cast<const int32_t*>(mem[3]);
   d.nbr_dn = static_cast<const int32_t*>(mem[4]);
-  d.cell_mask = nullptr;
+  d.cell_mask = mask;
   if (into) {
     *desc = d;
-    return volume_gpu_refresh_mask(into, s);
+    return YV_OK;
   }
   // a new volume: its buffers are complete once the stream gets here
   if ((e = cudaStreamSynchronize(s)) != cudaSuccess) {
     for (void* p : fresh) cudaFree(p);
+    cudaFree(mask);
     return vbuild_fail(e, "device pool");
   }
-  yv_status mst = volume_gpu_from_device(fresh, bytes, d, out);
-  if (mst != YV_OK) return mst;
-  mst = volume_gpu_refresh_mask(*out, s);
-  if (mst == YV_OK && (e = cudaStreamSynchronize(s)) != cudaSuccess)
-    mst = vbuild_fail(e, "cell mask");
-  if (mst != YV_OK) {
-    yv_volume_gpu_free(*out);
-    *out = nullptr;
-  }
-  return mst;
+  return volume_gpu_from_device(fresh, bytes, d, out, mask);
 }
 
 }  // namespace

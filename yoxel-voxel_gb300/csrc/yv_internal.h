@@ -102,9 +102,14 @@ yv_status volume_host_from_parts(int levels, std::vector<uint32_t>&& grids,
                                  std::vector<int32_t>&& cells, yv_volume_host** out);
 // A yv_volume_gpu that owns device buffers mem[0..4] (grids, density,
 // albedo, neighbours up, neighbours down) of bytes[0..4] bytes, described by
-// d (api_volume.cpp).
+// d (api_volume.cpp), and, when `mask` is given, the cell occupancy mask
+// already computed in it (d.nbricks x 16 words).
 yv_status volume_gpu_from_device(void* mem[5], const size_t bytes[5], const yv_volume_device& d,
-                                 yv_volume_gpu** out);
+                                 yv_volume_gpu** out, uint32_t* mask = nullptr);
+// The volume's cell-mask buffer, grown to hold nbricks x 16 words (the old
+// one is released after `s` drains).
+yv_status volume_gpu_mask_buffer(yv_volume_gpu* g, uint32_t nbricks, cudaStream_t s,
+                                 uint32_t** mask);
 // (Re)computes the cell occupancy mask of a library-owned volume on `s`
 // (after its pool changed) and points its descriptor at it.
 yv_status volume_gpu_refresh_mask(yv_volume_gpu* g, cudaStream_t s);
