@@ -659,7 +659,10 @@ def run_brick(args, cfg):
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
                      "traffic": profile_traffic("volume_forward_cfg3"), "peak_source": kind,
-                     "algorithmic_bytes_per_step": alg},
+                     "traffic_source": "ncu capture of one launch (dram__bytes_read.sum + "
+                                       "dram__bytes_write.sum), profiles/volume_forward_cfg3.md",
+                     "algorithmic_bytes_per_step": alg,
+                     "issue": profile_issue("volume_forward_cfg3")},
         "e2e": {"value": round(rays / e2e_s / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": 40,
                 "d2h_bytes_per_step": rays * 16,
                 "path": "yoxel.render_volume + copy into pinned host memory"},
@@ -758,7 +761,15 @@ def run_train(args, cfg):
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
                      "traffic": profile_traffic("volume_backward_cfg4"), "peak_source": kind,
-                     "kernel": "volume_backward_kernel", "algorithmic_bytes_per_launch": alg_b},
+                     "traffic_source": "ncu capture of one launch (dram__bytes_read.sum + "
+                                       "dram__bytes_write.sum), profiles/volume_backward_cfg4.md",
+                     "kernel": "volume_backward_kernel", "algorithmic_bytes_per_launch": alg_b,
+                     "note": "the replay reads and the gradient atomics are served by L1/L2 "
+                             "(the 29 MB gradient scratch stays in L2), so the algorithmic "
+                             "bytes exceed what HBM could move in the time (frac > 1) while "
+                             "DRAM moves only `traffic`: the kernel is bound by load latency "
+                             "and L2 atomic requests, not HBM",
+                     "issue": profile_issue("volume_backward_cfg4")},
         "gradient_check": "GPU adjoint vs FP64 adjoint / naive PyTorch marcher / FP64 central "
                           "differences: rel. error <= 1e-4 (tests/test_volume_gpu.py)",
         # per fwd+bwd step: pack, forward, adjoint, unpack, 2 x (fold gather +
