@@ -37,7 +37,7 @@ typedef int32_t yv_status;
                                     cell/ppu_renderer.cpp:78-79)              */
 #define YV_ERR_BAD_POOL       3  /* node/brick pool failed validation         */
 #define YV_ERR_ITERATION_CAP  4  /* a ray hit the per-ray iteration cap       */
-#define YV_ERR_TIMEOUT        5  /* a bounded device wait gave up             */
+#define YV_ERR_TIMEOUT        5  /* the frame time budget ran out             */
 #define YV_ERR_CUDA           6  /* a CUDA runtime call failed                */
 #define YV_ERR_OUT_OF_MEMORY  7
 #define YV_ERR_IO             8  /* file could not be read / written          */
@@ -265,6 +265,16 @@ yv_status yv_set_light(yv_renderer* r, const yv_light* light);
  * for a leaf in that slot.  0 (the default): exact leaves. */
 yv_status yv_set_detail_coef(yv_renderer* r, float coef);
 yv_status yv_get_detail_coef(const yv_renderer* r, float* coef);
+/* Frame time budget of the persistent ray queue (no reference counterpart:
+ * the reference renders a frame to completion).  With microseconds > 0, a
+ * warp of the frame kernel takes no new rays once that long has passed
+ * since its block started (the GPU global timer); rays in flight finish,
+ * pixels of rays never taken are left unwritten, and the frame's status
+ * (yv_renderer_frame_stats, yv_render_frame) is YV_ERR_TIMEOUT.  Applies
+ * to yv_render_frame, yv_render_frame_async and yv_render_frame_tiles.
+ * 0 (the default): no budget. */
+yv_status yv_set_frame_budget(yv_renderer* r, uint32_t microseconds);
+yv_status yv_get_frame_budget(const yv_renderer* r, uint32_t* microseconds);
 yv_status yv_set_launch_config(yv_renderer* r, const yv_launch_config* cfg);
 yv_status yv_get_launch_config(const yv_renderer* r, yv_launch_config* cfg);
 

@@ -138,3 +138,48 @@ def test_dynamic_scene_malformed_pool_reports_status(yoxel_mod, oracle, mode, ex
     st = r.frame_stats(check=False)
     assert st["status"] == expect
     _check_frame({k: v.cpu().numpy().view(np.uint32) for k, v in out.items()}, ref)
+
+
+def test_frame_budget_times_out_and_frame_recovers(yoxel_mod):
+    """The persistent queue's time budget: with a 1 us budget the frame
+    kernel stops taking rays after the first ones its warps took, the frame
+    reports YV_ERR_TIMEOUT, every pixel it wrote equals the unbudgeted
+    frame's, the others keep their contents; with the budget removed the
+    next frame is complete and the status clean."""
+    import torch
+    from yoxel import _lib as L
+    scene = yoxel_mod.SVOScene.spheres(8, 200, 4.0, 24.0, 1234)
+    pos, view = camera_for()
+    w, h = 1024, 1024
+    r = yoxel_mod.Renderer()
+    r.SetScene(scene)
+    r.SetViewPos(pos)
+    r.SetViewDir(view)
+    r.SetResolution(w, h)
+    r.SetFOV(60.0)
+    r.SetLight(LIGHT, 0.15, 0.85, True)
+    assert r.GetFrameBudget() == 0
+    full = r.render_outputs()
+    assert full.pop("stats")["status"] == L.YV_OK
+    r.SetFrameBudget(1)
+    assert r.GetFrameBudget() == 1
+    out = {k: torch.full((h, w), -7, dtype=torch.float32 if k == "hit_t" else torch.int32,
+                         device="cuda") for k in full}
+    r.render_async(**out)
+    st = r.frame_stats(check=False)
+    assert st["status"] == L.YV_ERR_TIMEOUT
+    with pytest.raises(L.YvError) as e:
+        r.frame_stats()
+    assert e.value.status == L.YV_ERR_TIMEOUT
+    got = {k: v.cpu().numpy() for k, v in out.items()}
+    ref = {k: v.cpu().numpy().view(np.uint32) for k, v in full.items()}
+    written = got["fetches"] != -7
+    assert 0 < written.sum() < w * h
+    for k in got:
+        assert np.array_equal(got[k].view(np.uint32)[written], ref[k][written]), k
+        assert (got[k][~written] == -7).all(), k
+    r.SetFrameBudget(0)
+    again = r.render_outputs()
+    assert again.pop("stats")["status"] == L.YV_OK
+    for k in again:
+        assert torch.equal(again[k].view(torch.int32), full[k].view(torch.int32)), k

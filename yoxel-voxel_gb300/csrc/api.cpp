@@ -35,6 +35,7 @@ struct yv_renderer {
   uint32_t* d_node_data = nullptr;  // level-of-detail attribute per node, or null
   size_t cap_nodes = 0, cap_attrs = 0;  // allocated records of the three
   float detail = 0.f;  // SVORenderer::m_detailCoef; 0 = exact leaves
+  uint32_t budget_us = 0;  // frame time budget of the plain frames; 0 = none
   // SVORenderer::SetScene(DynamicSVO*): a non-owned editable scene whose
   // device mirror (as of its last sync) is traced in place
   const yv_svo_dynamic* dyn = nullptr;
@@ -159,7 +160,7 @@ const char* yv_status_string(yv_status s) {
     case YV_ERR_NO_SCENE: return "no scene set";
     case YV_ERR_BAD_POOL: return "malformed node or brick pool";
     case YV_ERR_ITERATION_CAP: return "ray iteration cap reached";
-    case YV_ERR_TIMEOUT: return "bounded device wait timed out";
+    case YV_ERR_TIMEOUT: return "frame time budget ran out";
     case YV_ERR_CUDA: return "CUDA runtime error";
     case YV_ERR_OUT_OF_MEMORY: return "out of memory";
     case YV_ERR_IO: return "file I/O error";
@@ -316,6 +317,18 @@ yv_status yv_set_scene_host(yv_renderer* r, const yv_svo_host* svo) {
 yv_status yv_set_detail_coef(yv_renderer* r, float coef) {
   if (!r || !std::isfinite(coef) || coef < 0.f) return YV_ERR_INVALID_ARG;
   r->detail = coef;
+  return YV_OK;
+}
+
+yv_status yv_set_frame_budget(yv_renderer* r, uint32_t microseconds) {
+  if (!r) return YV_ERR_INVALID_ARG;
+  r->budget_us = microseconds;
+  return YV_OK;
+}
+
+yv_status yv_get_frame_budget(const yv_renderer* r, uint32_t* microseconds) {
+  if (!r || !microseconds) return YV_ERR_INVALID_ARG;
+  *microseconds = r->budget_us;
   return YV_OK;
 }
 
@@ -501,6 +514,7 @@ static yv_status enqueue_frame(yv_renderer* r, const yv_frame_outputs* out, cuda
   a.shadow_fetches = static_cast<uint32_t*>(out->shadow_fetches);
   a.normal = static_cast<float*>(out->normal);
   a.counters = r->d_counters;
+  if (!unlit) a.budget_us = r->budget_us;
   int launches = 0;
   YV_CUDA(launch_svo_frame(scene_of(r), a, r->cfg, s, &launches), "svo frame launch");
   r->last_stream = s;

@@ -27,7 +27,10 @@
 //    (no FMA contraction), which keeps hit ids bit-identical to the FP32
 //    restatement of the reference;
 //  * every loop is bounded: a ray that exceeds the step cap or the stack
-//    depth stops, is reported as a miss and sets a status bit.
+//    depth stops, is reported as a miss and sets a status bit;
+//  * an optional frame time budget bounds the queue itself: a warp about to
+//    take new rays after the budget has elapsed (the global timer against
+//    its block's start) takes none, and the frame reports a timeout.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -113,6 +116,13 @@ __device__ __forceinline__ uint32_t child_word(const SvoDeviceScene& sc, const u
   }
   if (kStaged && id < nsm) return sm[8 * id + c];
   return __ldg(reinterpret_cast<const uint32_t*>(sc.nodes) + 8 * (size_t)id + c);
+}
+
+// Nanoseconds of the GPU's global timer.
+__device__ __forceinline__ unsigned long long global_timer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
 }
 
 // One stack frame: a level whose current child still has a next sibling
@@ -395,8 +405,13 @@ template <int kMinBlocks, bool kRef, int kRing, bool kStaged, bool kLod = false>
 __global__ void __launch_bounds__(256, kMinBlocks)
     svo_frame_kernel(SvoDeviceScene sc, SvoFrameArgs a, uint32_t nsm, uint32_t refill_min) {
   extern __shared__ uint4 smem[];
+  // the block's deadline under a frame budget (held in shared memory, not
+  // in a register of the traversal)
+  __shared__ unsigned long long deadline;
   if (!kStaged) nsm = 0;
   for (uint32_t i = threadIdx.x; i < 2 * nsm; i += blockDim.x) smem[i] = __ldg(sc.nodes + i);
+  if (threadIdx.x == 0 && a.budget_us)
+    deadline = global_timer_ns() + 1000ull * (unsigned long long)a.budget_us;
   __syncthreads();
   const uint32_t* smw = reinterpret_cast<const uint32_t*>(smem);
   uint4* ring = smem + 2 * nsm + (threadIdx.x >> 5) * (2 * kRing * 32) + (threadIdx.x & 31u);
@@ -418,7 +433,13 @@ __global__ void __launch_bounds__(256, kMinBlocks)
   for (;;) {
     // ---- refill idle lanes from the global ray counter ----
     const uint32_t idle = __ballot_sync(0xFFFFFFFFu, mode == kIdle);
-    if (idle) {
+    // past the frame budget: the idle lanes take no new rays (lane 0's
+    // reading of the timer decides for the warp)
+    if (idle && a.budget_us &&
+        __shfl_sync(0xFFFFFFFFu, global_timer_ns() > deadline ? 1 : 0, 0)) {
+      if (mode == kIdle) mode = kDone;
+      if (lane == 0) err |= YV_DEV_ERR_TIMEOUT;
+    } else if (idle) {
       const uint32_t leader = (uint32_t)__ffs(idle) - 1u;
       uint32_t base = 0;
       if (lane == leader) base = atomicAdd(&a.counters[0], (uint32_t)__popc(idle));

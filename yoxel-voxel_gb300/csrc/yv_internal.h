@@ -34,7 +34,7 @@ constexpr uint32_t YV_MAX_DEVICE_NODES = 0x1FFFFFFFu;  // hit word = id<<3|c
 constexpr uint32_t YV_DEV_ERR_ITER = 1u;    // per-ray iteration cap reached
 constexpr uint32_t YV_DEV_ERR_DEPTH = 2u;   // stack depth exceeded
 constexpr uint32_t YV_DEV_ERR_POOL = 4u;    // index outside the pool
-constexpr uint32_t YV_DEV_ERR_TIMEOUT = 8u; // bounded wait gave up
+constexpr uint32_t YV_DEV_ERR_TIMEOUT = 8u; // frame time budget elapsed
 
 struct yv_svo_host {
   std::vector<yv_vox_node> nodes;

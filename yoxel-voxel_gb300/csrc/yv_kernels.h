@@ -45,6 +45,10 @@ struct SvoFrameArgs {
   // ray ids [id_begin, id_end) of the frame to trace (32 per 8x4-pixel
   // tile, tiles row-major); the whole frame is [0, 32 * tiles)
   uint32_t id_begin, id_end;
+  // frame time budget of the persistent queue in microseconds (0: none):
+  // once it has elapsed since a block started, the block's warps take no
+  // new rays and the frame reports YV_DEV_ERR_TIMEOUT
+  uint32_t budget_us;
 };
 
 // Ray ids of a whole width x height frame (8x4-pixel tiles of 32 ids).

@@ -150,6 +150,8 @@ _SIGS = {
     "yv_get_fov": (S, [P, C.POINTER(C.c_float)]),
     "yv_set_detail_coef": (S, [P, C.c_float]),
     "yv_get_detail_coef": (S, [P, C.POINTER(C.c_float)]),
+    "yv_set_frame_budget": (S, [P, C.c_uint32]),
+    "yv_get_frame_budget": (S, [P, C.POINTER(C.c_uint32)]),
     "yv_set_light": (S, [P, C.POINTER(Light)]),
     "yv_set_launch_config": (S, [P, C.POINTER(LaunchConfig)]),
     "yv_get_launch_config": (S, [P, C.POINTER(LaunchConfig)]),

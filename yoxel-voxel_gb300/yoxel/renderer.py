@@ -132,6 +132,17 @@ class Renderer:
         L.check(L.lib.yv_get_detail_coef(self._h, C.byref(c)), "GetDetailCoef")
         return c.value
 
+    def SetFrameBudget(self, microseconds):
+        """Frame time budget of the persistent ray queue (0 = none): past it
+        the kernel takes no new rays, unwritten pixels keep their contents
+        and the frame status is YV_ERR_TIMEOUT."""
+        L.check(L.lib.yv_set_frame_budget(self._h, int(microseconds)), "SetFrameBudget")
+
+    def GetFrameBudget(self):
+        v = C.c_uint32()
+        L.check(L.lib.yv_get_frame_budget(self._h, C.byref(v)), "GetFrameBudget")
+        return v.value
+
     def lod_coef(self):
         """The per-frame cut-off coefficient detail * radians(fov / 2) /
         width, as the frame uses it (float32)."""
