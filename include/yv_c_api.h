@@ -391,7 +391,26 @@ typedef struct yv_volume_device {
    * yv_volume_rebuild_dense) carry it; a pool whose densities change between
    * frames (the learnable tensors) leaves it NULL. */
   const uint32_t* cell_mask;
+  /* optional (NULL = none): one bit per brick cell of the tree, bit
+   * (ci & 31) of word ci >> 5 for ci = (cz * nb + cy) * nb + cx, nb =
+   * 4^levels, set unless the tree holds no brick there.  The march tests it
+   * before descending the tree for a cell, so the empty cells a ray crosses
+   * cost one load instead of a descent.  It depends on the grids only
+   * (yv_volume_brick_bits computes it); library-owned pools of up to 4
+   * levels carry it. */
+  const uint32_t* brick_bits;
 } yv_volume_device;
+
+/* Words of the brick_bits array of a tree of `levels` levels:
+ * ceil(4^(3 levels) / 32). */
+#define YV_BRICK_BITS_WORDS(levels) \
+  ((((uint64_t)1 << (6 * (levels))) + 31u) / 32u)
+
+/* Computes the brick_bits array of v's tree (v->grids, ngrids, levels,
+ * nbricks) into `bits` (device, YV_BRICK_BITS_WORDS(levels) words), on
+ * `stream`.  v->brick_bits is not read.  No reference counterpart (the
+ * reference descends the tree for every cell). */
+yv_status yv_volume_brick_bits(const yv_volume_device* v, uint32_t* bits, void* stream);
 
 /* Device copy owned by the library (BrickPool<T>, ntree/BrickManager.h). */
 typedef struct yv_volume_gpu yv_volume_gpu;

@@ -132,3 +132,28 @@ def test_pack_kernel_cell_mask_matches_upload(yoxel_mod, precision):
                                            levels, precision)
     other.rebuild_dense(torch.from_numpy(d).cuda(), levels)
     assert np.array_equal(device_mask(other.desc()), want)
+
+
+def test_device_build_brick_bits_match_upload(yoxel_mod):
+    """The brick bitmap of a pool built from a lattice on the device (fresh
+    and rebuilt in place) equals that of an upload of the host build."""
+    import torch
+    levels = 2
+    d = lattice(levels, 8, "blobs")
+    host = yoxel_mod.BrickVolume.from_dense(levels, d)
+    up = host.upload(3)
+    n = (4 ** (3 * levels) + 31) // 32
+
+    def bits(desc):
+        class _Words:
+            __cuda_array_interface__ = {"shape": (n,), "typestr": "<i4",
+                                        "data": (desc.brick_bits, False), "version": 2}
+        return torch.as_tensor(_Words(), device="cuda").cpu().numpy()
+
+    want = bits(up.desc())
+    gv = yoxel_mod.VolumeGPU.from_dense(torch.from_numpy(d).cuda(), levels, 3)
+    assert np.array_equal(bits(gv.desc()), want)
+    other = yoxel_mod.VolumeGPU.from_dense(torch.from_numpy(lattice(levels, 3, "specks")).cuda(),
+                                           levels, 3)
+    other.rebuild_dense(torch.from_numpy(d).cuda(), levels)
+    assert np.array_equal(bits(other.desc()), want)

@@ -370,3 +370,54 @@ def test_cell_mask_and_empty_cell_skipping(yoxel_mod, precision):
         rgba = yoxel_mod.render_volume(d, cams, w, h, samples=ns)
         outs.append((rgba.cpu().numpy().view(np.uint32), ns.cpu().numpy()))
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+def _device_words(ptr, n):
+    import torch
+
+    class _Words:  # a view of the library's device array
+        __cuda_array_interface__ = {"shape": (n,), "typestr": "<i4", "data": (ptr, False),
+                                    "version": 2}
+
+    return torch.as_tensor(_Words(), device="cuda").cpu().numpy().view(np.uint32)
+
+
+def expected_brick_bits(vol):
+    nb = 4 ** vol.levels
+    bits = np.zeros(((nb ** 3 + 31) // 32,), np.uint32)
+    c = np.asarray(vol.cells, np.int64).reshape(-1, 3)
+    ci = (c[:, 2] * nb + c[:, 1]) * nb + c[:, 0]
+    np.bitwise_or.at(bits, ci >> 5, (np.uint32(1) << (ci & 31).astype(np.uint32)))
+    return bits
+
+
+@pytest.mark.parametrize("precision", [0, 1, 2, 3])
+def test_brick_bits_and_cheap_empty_cells(yoxel_mod, precision):
+    """The brick bitmap of a library-owned pool has exactly the cells of its
+    bricks set (uploads, device builds and the learnable copy alike), and
+    rendering without it gives the same frame bit for bit, sample and brick
+    counters included."""
+    import torch
+    vol = yoxel_mod.BrickVolume.noise(2, 0.4, 1.4, 23)
+    want = expected_brick_bits(vol)
+    assert 0 < np.unpackbits(want.view(np.uint8)).sum() < 4 ** 6
+    gv = vol.upload(precision)
+    desc = gv.desc()
+    assert desc.brick_bits
+    assert np.array_equal(_device_words(desc.brick_bits, len(want)), want)
+    tv = vol.to_torch()
+    assert np.array_equal(tv["brick_bits"].cpu().numpy().view(np.uint32), want)
+    cams = [cam_at([1.6, 1.3, 1.1]), cam_at([-0.7, 0.4, 0.9], 50.0), cam_at([0.5, 0.5, 0.5])]
+    w, h = 96, 80
+    outs = []
+    for use_bits in (True, False):
+        d = gv.desc()
+        if not use_bits:
+            d.brick_bits = None
+        ns = torch.zeros((len(cams), h, w), dtype=torch.int32, device="cuda")
+        nbk = torch.zeros((len(cams), h, w), dtype=torch.int32, device="cuda")
+        rgba = yoxel_mod.render_volume(d, cams, w, h, samples=ns, bricks=nbk)
+        outs.append([rgba.cpu().numpy().view(np.uint32), ns.cpu().numpy(), nbk.cpu().numpy()])
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+    assert outs[0][2].sum() > 0

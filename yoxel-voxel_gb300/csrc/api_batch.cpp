@@ -224,6 +224,7 @@ yv_status yv_batch_add_volume(yv_batch* b, const yv_volume_device* vol, const yv
   v.nbricks = vol->nbricks;
   v.precision = vol->precision;
   v.cell_mask = vol->cell_mask;
+  v.brick_bits = vol->brick_bits;
   v.S = (float)(8 * v.nb);
   v.cell_size = 8.0f / v.S;
   v.alpha_scale = mp->alpha_scale;

@@ -21,7 +21,9 @@ struct yv_volume_gpu {
   yv_volume_device desc;
   void* mem[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   size_t cap[5] = {0, 0, 0, 0, 0};  // bytes allocated per array (reused by rebuilds)
-  uint32_t* mask = nullptr;         // cell occupancy mask (16 words per brick)
+  // acceleration arrays in one allocation: the cell occupancy mask (16
+  // words per brick), then the brick bitmap (trees of up to 4 levels)
+  uint32_t* mask = nullptr;
   size_t mask_cap = 0;
 };
 
@@ -80,6 +82,7 @@ bool fill_args(const yv_volume_device* v, const yv_march_params* mp, int width, 
   a->v.nbricks = v->nbricks;
   a->v.precision = v->precision;
   a->v.cell_mask = v->cell_mask;
+  a->v.brick_bits = v->brick_bits;
   a->nbr_up = v->nbr_up;
   a->nbr_dn = v->nbr_dn;
   a->v.S = (float)(8 * a->v.nb);
@@ -118,11 +121,11 @@ bool cams_ok(const yv_camera* c, int n) {
 namespace yv {
 
 yv_status volume_gpu_from_device(void* mem[5], const size_t bytes[5], const yv_volume_device& d,
-                                 yv_volume_gpu** out, uint32_t* mask) {
+                                 yv_volume_gpu** out, uint32_t* accel) {
   yv_volume_gpu* g = new (std::nothrow) yv_volume_gpu();
   if (!g) {
     for (int i = 0; i < 5; ++i) cudaFree(mem[i]);
-    cudaFree(mask);
+    cudaFree(accel);
     return YV_ERR_OUT_OF_MEMORY;
   }
   cudaGetDevice(&g->device);
@@ -131,42 +134,67 @@ yv_status volume_gpu_from_device(void* mem[5], const size_t bytes[5], const yv_v
     g->cap[i] = mem[i] ? bytes[i] : 0;
   }
   g->desc = d;
-  g->desc.cell_mask = mask;
-  g->mask = mask;
-  g->mask_cap = mask ? (size_t)d.nbricks * 16u * sizeof(uint32_t) : 0;
+  g->mask = accel;
+  g->mask_cap = accel ? volume_accel_bytes(d.nbricks, d.levels) : 0;
+  if (!accel) {
+    g->desc.cell_mask = nullptr;
+    g->desc.brick_bits = nullptr;
+  }
   *out = g;
   return YV_OK;
 }
 
-yv_status volume_gpu_mask_buffer(yv_volume_gpu* g, uint32_t nbricks, cudaStream_t s,
-                                 uint32_t** mask) {
-  const size_t bytes = (size_t)nbricks * 16u * sizeof(uint32_t);
+size_t volume_accel_bytes(uint32_t nbricks, int levels) {
+  if (!nbricks) return 0;
+  const size_t bits = levels <= 4 ? (size_t)YV_BRICK_BITS_WORDS(levels) * 4u : 0u;
+  return (size_t)nbricks * 16u * sizeof(uint32_t) + bits;
+}
+
+yv_status volume_gpu_accel_buffer(yv_volume_gpu* g, uint32_t nbricks, int levels, cudaStream_t s,
+                                  uint32_t** mask, uint32_t** bits) {
+  const size_t bytes = volume_accel_bytes(nbricks, levels);
   *mask = nullptr;
+  *bits = nullptr;
   if (!bytes) return YV_OK;
   cudaError_t e = cudaSuccess;
   if (g->mask_cap < bytes) {
-    // the old mask may still be read by queued work on `s`
+    // the old arrays may still be read by queued work on `s`
     if (g->mask) e = cudaStreamSynchronize(s);
     if (e == cudaSuccess) {
       cudaFree(g->mask);
       g->mask = nullptr;
       g->mask_cap = 0;
       g->desc.cell_mask = nullptr;
+      g->desc.brick_bits = nullptr;
       e = cudaMalloc(&g->mask, bytes);
     }
-    if (e != cudaSuccess) return fail(e, "cell mask");
+    if (e != cudaSuccess) return fail(e, "acceleration arrays");
     g->mask_cap = bytes;
   }
-  *mask = static_cast<uint32_t*>(g->mask);
+  *mask = g->mask;
+  if (levels <= 4) *bits = g->mask + (size_t)nbricks * 16u;
   return YV_OK;
 }
 
+yv_status volume_brick_bits(const yv_volume_device& d, uint32_t* bits, cudaStream_t s) {
+  yv_march_params mp = {1.0f, 0.5f};
+  VolumeArgs* a = new (std::nothrow) VolumeArgs;
+  if (!a) return YV_ERR_OUT_OF_MEMORY;
+  if (!fill_args(&d, &mp, 1, 1, a)) {
+    delete a;
+    return YV_ERR_INVALID_ARG;
+  }
+  const cudaError_t e = launch_brick_bits(a->v, bits, s);
+  delete a;
+  return e == cudaSuccess ? YV_OK : fail(e, "brick bits");
+}
+
 yv_status volume_gpu_refresh_mask(yv_volume_gpu* g, cudaStream_t s) {
-  uint32_t* mask = nullptr;
-  yv_status st = volume_gpu_mask_buffer(g, g->desc.nbricks, s, &mask);
+  uint32_t *mask = nullptr, *bits = nullptr;
+  yv_status st = volume_gpu_accel_buffer(g, g->desc.nbricks, g->desc.levels, s, &mask, &bits);
   g->desc.cell_mask = nullptr;
+  g->desc.brick_bits = nullptr;
   if (st != YV_OK || !mask) return st;
-  cudaError_t e;
   yv_march_params mp = {1.0f, 0.5f};
   VolumeArgs* a = new (std::nothrow) VolumeArgs;
   if (!a) return YV_ERR_OUT_OF_MEMORY;
@@ -174,10 +202,12 @@ yv_status volume_gpu_refresh_mask(yv_volume_gpu* g, cudaStream_t s) {
     delete a;
     return YV_ERR_INVALID_ARG;
   }
-  e = launch_cell_mask(a->v, mask, s);
+  cudaError_t e = launch_cell_mask(a->v, mask, s);
+  if (e == cudaSuccess && bits) e = launch_brick_bits(a->v, bits, s);
   delete a;
-  if (e != cudaSuccess) return fail(e, "cell mask");
+  if (e != cudaSuccess) return fail(e, "acceleration arrays");
   g->desc.cell_mask = mask;
+  g->desc.brick_bits = bits;
   return YV_OK;
 }
 
@@ -283,6 +313,7 @@ yv_status yv_volume_upload(const yv_volume_host* v, int32_t precision, yv_volume
   g->desc.nbr_up = static_cast<const int32_t*>(g->mem[3]);
   g->desc.nbr_dn = static_cast<const int32_t*>(g->mem[4]);
   g->desc.cell_mask = nullptr;
+  g->desc.brick_bits = nullptr;
   yv_status st = volume_gpu_refresh_mask(g, nullptr);
   cudaError_t e = st == YV_OK ? cudaStreamSynchronize(nullptr) : cudaSuccess;
   if (st != YV_OK || e != cudaSuccess) {
@@ -299,6 +330,11 @@ void yv_volume_gpu_free(yv_volume_gpu* g) {
   for (void* p : g->mem) cudaFree(p);
   cudaFree(g->mask);
   delete g;
+}
+
+yv_status yv_volume_brick_bits(const yv_volume_device* v, uint32_t* bits, void* stream) {
+  if (!v || !bits) return YV_ERR_INVALID_ARG;
+  return volume_brick_bits(*v, bits, static_cast<cudaStream_t>(stream));
 }
 
 yv_status yv_volume_gpu_desc(const yv_volume_gpu* g, yv_volume_device* out) {

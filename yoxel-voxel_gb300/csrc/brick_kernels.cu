@@ -212,6 +212,23 @@ __global__ void cell_mask_kernel(VolumeView v, uint32_t* mask) {
   if (lane == 0) mask[warp] = bits;
 }
 
+// Brick bitmap: one warp per word of 32 brick cells, a lane per cell, its
+// bit set unless the tree descent finds the cell empty (a malformed ref
+// keeps its bit, so the march's own descent still reports it).
+__global__ void brick_bits_kernel(VolumeView v, uint32_t* bits, uint32_t nwords) {
+  const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= nwords) return;  // uniform across the warp
+  const uint32_t nb = (uint32_t)v.nb, n = nb * nb * nb;
+  const uint32_t ci = w * 32u + (threadIdx.x & 31u);
+  bool set = false;
+  if (ci < n) {
+    const int cell[3] = {(int)(ci % nb), (int)((ci / nb) % nb), (int)(ci / (nb * nb))};
+    set = lookup(v, nullptr, 0u, cell) != -1;
+  }
+  const uint32_t word = __ballot_sync(0xFFFFFFFFu, set);
+  if ((threadIdx.x & 31u) == 0) bits[w] = word;
+}
+
 // Apron fold, pass 1: every owned lattice point (x,y,z < 8) adds the
 // gradient its copies received in the aprons of the lower neighbours.
 __global__ void fold_gather_kernel(VolumeArgs a, int channels, float* g) {
@@ -351,6 +368,14 @@ cudaError_t launch_cell_mask(const VolumeView& v, uint32_t* mask, cudaStream_t s
     case 2: cell_mask_kernel<2><<<blocks, 256, 0, s>>>(v, mask); break;
     default: cell_mask_kernel<3><<<blocks, 256, 0, s>>>(v, mask); break;
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_brick_bits(const VolumeView& v, uint32_t* bits, cudaStream_t s) {
+  const uint64_t n = (uint64_t)v.nb * v.nb * v.nb;
+  const uint32_t nwords = (uint32_t)((n + 31) / 32);
+  brick_bits_kernel<<<(uint32_t)(((uint64_t)nwords * 32 + 255) / 256), 256, 0, s>>>(v, bits,
+                                                                                   nwords);
   return cudaGetLastError();
 }
 

@@ -317,7 +317,16 @@ __device__ __forceinline__ void march(const VolumeView& a, const uint32_t* sg, u
     float t_out = tx[0];
     if (tx[1] < t_out) { e = 1; t_out = tx[1]; }
     if (tx[2] < t_out) { e = 2; t_out = tx[2]; }
-    const int b = lookup(a, sg, nsg, cell);
+    int b = -1;
+    {
+      // the tree is descended only where the brick bitmap (if any) says a
+      // brick may be
+      const uint32_t ci =
+          ((uint32_t)cell[2] * (uint32_t)a.nb + (uint32_t)cell[1]) * (uint32_t)a.nb +
+          (uint32_t)cell[0];
+      if (!a.brick_bits || ((__ldg(a.brick_bits + (ci >> 5)) >> (ci & 31u)) & 1u))
+        b = lookup(a, sg, nsg, cell);
+    }
     if (b == -2) {
       r.bad = true;
       break;

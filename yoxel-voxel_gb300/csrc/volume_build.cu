@@ -218,9 +218,13 @@ __device__ __forceinline__ uint32_t lattice_row9(const uint32_t* bits, int off) 
   return v & 0x1FFu;
 }
 
+// bits (device pools, optional, zeroed before): the brick bitmap, bit
+// (ci & 31) of word ci >> 5 set for the cell ci = (cz nb + cy) nb + cx of
+// every brick.
 __global__ void pack_bricks_kernel(Lattice g, const uint64_t* cells, uint32_t nbricks, int format,
                                    float* dens, uint8_t* rgb, void* d_out, void* a_out,
-                                   int32_t* cell_xyz, int32_t* map, uint32_t* mask) {
+                                   int32_t* cell_xyz, int32_t* map, uint32_t* mask,
+                                   uint32_t* bits) {
   __shared__ uint32_t nzbits[8][24];
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t* nz = nzbits[(threadIdx.x >> 5) & 7u];
@@ -236,6 +240,11 @@ __global__ void pack_bricks_kernel(Lattice g, const uint64_t* cells, uint32_t nb
       cell_xyz[3 * (size_t)b + 1] = cy;
       cell_xyz[3 * (size_t)b + 2] = cz;
       map[c] = (int32_t)b;
+      if (bits) {
+        const uint64_t ci = ((uint64_t)cz * (uint64_t)g.nb + (uint64_t)cy) * (uint64_t)g.nb +
+                            (uint64_t)cx;
+        atomicOr(bits + (ci >> 5), 1u << (uint32_t)(ci & 31u));
+      }
     }
     // lattice point k = lane + 32 q; the loads of 8 points are issued before
     // any is used
@@ -474,7 +483,7 @@ yv_status yv_volume_build_dense(const float* density, const uint8_t* rgb, int32_
   if (t.nbricks)
     pack_bricks_kernel<<<grid_for((uint64_t)t.nbricks * 32), 256, 0, s>>>(
         g, t.cells.as<uint64_t>(), t.nbricks, -1, dens.as<float>(), col.as<uint8_t>(), nullptr,
-        nullptr, cxyz.as<int32_t>(), map.as<int32_t>(), nullptr);
+        nullptr, cxyz.as<int32_t>(), map.as<int32_t>(), nullptr, nullptr);
   if ((e = cudaGetLastError()) != cudaSuccess) return vbuild_fail(e, "pack");
   std::vector<uint32_t> grids((size_t)t.ngrids * 64);
   std::vector<float> hd(n);
@@ -543,14 +552,16 @@ yv_status upload_dense(const float* density, const uint8_t* rgb, int32_t levels,
     e = cudaMalloc(&mem[i], bytes[i]);
     if (e == cudaSuccess && cap) cap[i] = bytes[i];
   }
-  // the cell occupancy mask, computed by the pack kernel
-  uint32_t* mask = nullptr;
+  // the acceleration arrays: the cell occupancy mask (written by the pack
+  // kernel), then the brick bitmap
+  uint32_t *mask = nullptr, *bits = nullptr;
   if (e == cudaSuccess && t.nbricks) {
     if (into) {
-      const yv_status mst = volume_gpu_mask_buffer(into, t.nbricks, s, &mask);
+      const yv_status mst = volume_gpu_accel_buffer(into, t.nbricks, levels, s, &mask, &bits);
       if (mst != YV_OK) return mst;
     } else {
-      e = cudaMalloc(&mask, (size_t)t.nbricks * 16u * sizeof(uint32_t));
+      e = cudaMalloc(&mask, volume_accel_bytes(t.nbricks, levels));
+      if (e == cudaSuccess && levels <= 4) bits = mask + (size_t)t.nbricks * 16u;
     }
   }
   DevBuf cxyz, map;
@@ -559,10 +570,12 @@ yv_status upload_dense(const float* density, const uint8_t* rgb, int32_t levels,
   if (e == cudaSuccess) e = cudaMemsetAsync(map.p, 0xFF, cells * 4, s);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(mem[0], t.grids.p, bytes[0], cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess && bits)
+    e = cudaMemsetAsync(bits, 0, (size_t)YV_BRICK_BITS_WORDS(levels) * 4u, s);
   if (e == cudaSuccess && t.nbricks) {
     pack_bricks_kernel<<<grid_for((uint64_t)t.nbricks * 32), 256, 0, s>>>(
         g, t.cells.as<uint64_t>(), t.nbricks, precision, nullptr, nullptr, mem[1], mem[2],
-        cxyz.as<int32_t>(), map.as<int32_t>(), mask);
+        cxyz.as<int32_t>(), map.as<int32_t>(), mask, bits);
     neighbors_kernel<<<grid_for(t.nbricks), 256, 0, s>>>(
         cxyz.as<int32_t>(), map.as<int32_t>(), t.nbricks, g.nb, static_cast<int32_t*>(mem[3]),
         static_cast<int32_t*>(mem[4]));
@@ -586,6 +599,7 @@ yv_status upload_dense(const float* density, const uint8_t* rgb, int32_t levels,
   d.nbr_up = static_cast<const int32_t*>(mem[3]);
   d.nbr_dn = static_cast<const int32_t*>(mem[4]);
   d.cell_mask = mask;
+  d.brick_bits = bits;
   if (into) {
     *desc = d;
     return YV_OK;

@@ -102,16 +102,24 @@ yv_status volume_host_from_parts(int levels, std::vector<uint32_t>&& grids,
                                  std::vector<int32_t>&& cells, yv_volume_host** out);
 // A yv_volume_gpu that owns device buffers mem[0..4] (grids, density,
 // albedo, neighbours up, neighbours down) of bytes[0..4] bytes, described by
-// d (api_volume.cpp), and, when `mask` is given, the cell occupancy mask
-// already computed in it (d.nbricks x 16 words).
+// d (api_volume.cpp), and, when `accel` is given, its acceleration arrays
+// already computed there (volume_accel_bytes(d.nbricks, d.levels) bytes:
+// d.cell_mask and d.brick_bits point into it).
 yv_status volume_gpu_from_device(void* mem[5], const size_t bytes[5], const yv_volume_device& d,
-                                 yv_volume_gpu** out, uint32_t* mask = nullptr);
-// The volume's cell-mask buffer, grown to hold nbricks x 16 words (the old
-// one is released after `s` drains).
-yv_status volume_gpu_mask_buffer(yv_volume_gpu* g, uint32_t nbricks, cudaStream_t s,
-                                 uint32_t** mask);
-// (Re)computes the cell occupancy mask of a library-owned volume on `s`
-// (after its pool changed) and points its descriptor at it.
+                                 yv_volume_gpu** out, uint32_t* accel = nullptr);
+// Bytes of a pool's acceleration arrays: the cell occupancy mask (16 words
+// per brick), then the brick bitmap (YV_BRICK_BITS_WORDS(levels) words, for
+// trees of up to 4 levels).  0 without bricks.
+size_t volume_accel_bytes(uint32_t nbricks, int levels);
+// The volume's acceleration arrays, grown to hold those of a pool of
+// nbricks bricks and `levels` levels (the old ones are released after `s`
+// drains): *mask and *bits (null for trees of more than 4 levels).
+yv_status volume_gpu_accel_buffer(yv_volume_gpu* g, uint32_t nbricks, int levels, cudaStream_t s,
+                                  uint32_t** mask, uint32_t** bits);
+// The brick bitmap of d's tree into `bits` on `s`.
+yv_status volume_brick_bits(const yv_volume_device& d, uint32_t* bits, cudaStream_t s);
+// (Re)computes the acceleration arrays of a library-owned volume on `s`
+// (after its pool changed) and points its descriptor at them.
 yv_status volume_gpu_refresh_mask(yv_volume_gpu* g, cudaStream_t s);
 // The owned buffers, their allocated sizes and the descriptor of a volume
 // (for rebuilds in place).

@@ -30,6 +30,10 @@ struct VolumeView {
   // per brick 16 words: bit (y & 3) * 8 + x of word z * 2 + (y >> 2) set
   // where trilinear cell (x, y, z) has a non-zero density corner; null = none
   const uint32_t* cell_mask;
+  // one bit per brick cell ((cz * nb + cy) * nb + cx), clear where the tree
+  // holds no brick: an empty cell costs one load instead of a descent;
+  // null = descend for every cell
+  const uint32_t* brick_bits;
   // march
   float S;               // lattice cells per axis
   float cell_size;       // world size of a brick cell = 8/S
@@ -72,5 +76,7 @@ cudaError_t launch_apron_fold(const VolumeArgs& a, int channels, float* g, bool 
 int device_sm_count_vol();
 // mask[b * 16 + w] for the nbricks bricks of v (cell_mask of VolumeView).
 cudaError_t launch_cell_mask(const VolumeView& v, uint32_t* mask, cudaStream_t s);
+// brick_bits of v's tree (ceil(nb^3 / 32) words).
+cudaError_t launch_brick_bits(const VolumeView& v, uint32_t* bits, cudaStream_t s);
 
 }  // namespace yv

@@ -9,8 +9,8 @@ from ._lib import YvError, LIB_PATH
 from .svo import SVOScene, NODE_DTYPE, ATTR_DTYPE
 from .renderer import Renderer, CudaRenderer
 from .volume import (BrickVolume, VolumeGPU, render_volume, render_volume_rgba8,
-                     volume_backward, volume_march, torch_desc, pack_volume, cameras,
-                     sphere_cameras)
+                     volume_backward, volume_march, torch_desc, pack_volume, brick_bits,
+                     cameras, sphere_cameras)
 
 from .batch import Batch
 from .dynamic import DynamicSVO
@@ -18,5 +18,5 @@ from .dynamic import DynamicSVO
 __all__ = ["SVOScene", "Renderer", "CudaRenderer", "YvError", "LIB_PATH", "Batch",
            "NODE_DTYPE", "ATTR_DTYPE", "DynamicSVO", "BrickVolume", "VolumeGPU", "render_volume",
            "render_volume_rgba8",
-           "volume_backward", "volume_march", "torch_desc", "pack_volume", "cameras",
-           "sphere_cameras"]
+           "volume_backward", "volume_march", "torch_desc", "pack_volume", "brick_bits",
+           "cameras", "sphere_cameras"]

@@ -89,7 +89,7 @@ class VolumeDevice(C.Structure):
     _fields_ = [("grids", C.c_void_p), ("ngrids", C.c_uint32), ("levels", C.c_int32),
                 ("density", C.c_void_p), ("albedo", C.c_void_p), ("nbricks", C.c_uint32),
                 ("precision", C.c_int32), ("nbr_up", C.c_void_p), ("nbr_dn", C.c_void_p),
-                ("cell_mask", C.c_void_p)]
+                ("cell_mask", C.c_void_p), ("brick_bits", C.c_void_p)]
 
 
 class Camera(C.Structure):
@@ -179,6 +179,7 @@ _SIGS = {
     "yv_volume_upload_dense": (S, [P, P, C.c_int32, C.c_int32, P, C.POINTER(P)]),
     "yv_volume_rebuild_dense": (S, [P, P, P, C.c_int32, P]),
     "yv_volume_gpu_desc": (S, [P, C.POINTER(VolumeDevice)]),
+    "yv_volume_brick_bits": (S, [C.POINTER(VolumeDevice), P, P]),
     "yv_volume_render": (S, [C.POINTER(VolumeDevice), C.POINTER(Camera), C.c_int32, C.c_int32,
                              C.c_int32, C.POINTER(MarchParams), P, P, P, P]),
     "yv_volume_render_rgba8": (S, [C.POINTER(VolumeDevice), C.POINTER(Camera), C.c_int32,

@@ -137,7 +137,7 @@ class BrickVolume:
         """Learnable fp32 copy: dict of torch tensors (grids, density (nb,729),
         albedo (nb,729,3) in [0,1], nbr_up, nbr_dn) on `device`."""
         torch = _torch()
-        return dict(
+        tv = dict(
             levels=self.levels,
             grids=torch.from_numpy(self.grids.astype(np.int32)).to(device),
             density=torch.from_numpy(self.density.copy()).to(device),
@@ -146,6 +146,8 @@ class BrickVolume:
             nbr_up=torch.from_numpy(self.neighbors(True).copy()).to(device),
             nbr_dn=torch.from_numpy(self.neighbors(False).copy()).to(device),
         )
+        tv["brick_bits"] = brick_bits(torch_desc(tv)) if self.levels <= 4 else None
+        return tv
 
 
 def _check_lattice(density, levels, rgb):
@@ -225,7 +227,22 @@ def torch_desc(tv, density=None, albedo=None, packed=None):
         d.precision = L.YV_PRECISION_F32
     d.nbr_up = tv["nbr_up"].data_ptr()
     d.nbr_dn = tv["nbr_dn"].data_ptr()
+    bits = tv.get("brick_bits")
+    d.brick_bits = None if bits is None else bits.data_ptr()
     return d
+
+
+def brick_bits(desc, stream=None):
+    """The brick bitmap of a volume's tree (int32 CUDA tensor of
+    ceil(4^(3 levels) / 32) words: bit (ci & 31) of word ci >> 5 set where
+    brick cell ci = (cz nb + cy) nb + cx may hold a brick), from its grids;
+    VolumeDevice.brick_bits takes its pointer."""
+    torch = _torch()
+    words = ((1 << (6 * int(desc.levels))) + 31) // 32
+    out = torch.empty(words, dtype=torch.int32, device="cuda")
+    L.check(L.lib.yv_volume_brick_bits(C.byref(desc), C.c_void_p(out.data_ptr()),
+                                       _stream(stream)), "yv_volume_brick_bits")
+    return out
 
 
 def pack_volume(density, albedo, out=None, stream=None):
