@@ -216,6 +216,25 @@ def profile_traffic(name):
     return float(m.group(1)) if m else None
 
 
+def profile_l2(name):
+    """L2 traffic of the kernel from profiles/<name>.md (lines
+    `l2_bytes_per_launch: N`, `l2_pct_of_peak: P`, from lts__t_sectors of the
+    capture), or None."""
+    p = os.path.join(ROOT, "profiles", name + ".md")
+    if not os.path.exists(p):
+        return None
+    txt = open(p).read()
+    m = re.search(r"l2_bytes_per_launch:\s*([0-9.eE+]+)", txt)
+    if not m:
+        return None
+    out = {"bytes_per_launch": float(m.group(1))}
+    m = re.search(r"l2_pct_of_peak:\s*([0-9.]+)", txt)
+    if m:
+        out["pct_of_peak_sector_rate"] = float(m.group(1))
+    out["source"] = f"ncu --set full capture (lts__t_sectors.sum x 32 B), profiles/{name}.md"
+    return out
+
+
 def profile_issue(name):
     """Issue-side figures of the kernel from profiles/<name>.md (lines
     `issue_active_pct: X`, `thread_inst_per_unit: Y (unit)`,
@@ -552,6 +571,7 @@ def run_svo(args, cfg):
     issue = profile_issue(f"svo_frame_{args.config}")
     if issue and ws == 1:
         line["roofline"]["issue"] = issue
+        line["roofline"]["l2"] = profile_l2(f"svo_frame_{args.config}")
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         sw, sh = w // 4, h // 4
@@ -662,7 +682,8 @@ def run_brick(args, cfg):
                      "traffic_source": "ncu capture of one launch (dram__bytes_read.sum + "
                                        "dram__bytes_write.sum), profiles/volume_forward_cfg3.md",
                      "algorithmic_bytes_per_step": alg,
-                     "issue": profile_issue("volume_forward_cfg3")},
+                     "issue": profile_issue("volume_forward_cfg3"),
+                     "l2": profile_l2("volume_forward_cfg3")},
         "e2e": {"value": round(rays / e2e_s / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": 40,
                 "d2h_bytes_per_step": rays * 16,
                 "path": "yoxel.render_volume + copy into pinned host memory"},
@@ -769,7 +790,8 @@ def run_train(args, cfg):
                              "bytes exceed what HBM could move in the time (frac > 1) while "
                              "DRAM moves only `traffic`: the kernel is bound by load latency "
                              "and L2 atomic requests, not HBM",
-                     "issue": profile_issue("volume_backward_cfg4")},
+                     "issue": profile_issue("volume_backward_cfg4"),
+                     "l2": profile_l2("volume_backward_cfg4")},
         "gradient_check": "GPU adjoint vs FP64 adjoint / naive PyTorch marcher / FP64 central "
                           "differences: rel. error <= 1e-4 (tests/test_volume_gpu.py)",
         # per fwd+bwd step: pack, forward, adjoint, unpack, 2 x (fold gather +
