@@ -56,12 +56,17 @@ def test_noalloc_frame_matches_renderer_on_two_calls(yoxel_mod):
                    fetches=torch.full((h, w), -7, dtype=torch.int32, device="cuda"),
                    shadow_fetches=torch.full((h, w), -7, dtype=torch.int32, device="cuda"))
         fo = _frame_outputs(out)
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         st = L.lib.yv_render_svo_noalloc(C.c_void_p(d_nodes.data_ptr()), scene.node_count,
                                          scene.root, C.c_void_p(d_attrs.data_ptr()),
                                          scene.attr_count, C.byref(cam), C.byref(light), w, h,
                                          C.byref(fo), C.c_void_p(stream.cuda_stream))
         assert st == L.YV_OK, L.status_string(st)
         torch.cuda.synchronize()
+        if call == 1:
+            # the warm call takes no device memory
+            assert torch.cuda.mem_get_info()[0] == free_before
         for k in ("rgba", "hit", "fetches", "shadow_fetches"):
             assert torch.equal(out[k], ref[k]), f"call {call}: {k} differs"
         assert torch.equal(out["hit_t"].view(torch.int32), ref["hit_t"].view(torch.int32))
