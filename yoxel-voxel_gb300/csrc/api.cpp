@@ -46,6 +46,7 @@ struct yv_renderer {
   uint32_t* d_rgba = nullptr;
   size_t rgba_cap = 0;
   uint32_t* d_counters = nullptr;
+  uint32_t* h_counters = nullptr;  // pinned copy of the counters (yv_render_frame)
   cudaStream_t last_stream = nullptr;
   uint64_t last_pixels = 0;
   int last_shadows = 0;
@@ -203,6 +204,7 @@ void yv_renderer_destroy(yv_renderer* r) {
   free_scene(r);
   cudaFree(r->d_rgba);
   cudaFree(r->d_counters);
+  cudaFreeHost(r->h_counters);
   delete r;
 }
 
@@ -561,13 +563,8 @@ yv_status yv_get_tile_count(const yv_renderer* r, uint32_t* tiles_x, uint32_t* t
   return YV_OK;
 }
 
-yv_status yv_renderer_frame_stats(yv_renderer* r, yv_frame_stats* stats) {
-  if (!r || !stats) return YV_ERR_INVALID_ARG;
-  std::memset(stats, 0, sizeof(*stats));
-  YV_CUDA(cudaSetDevice(r->device), "cudaSetDevice");
-  uint32_t c[kSvoCounterWords];
-  YV_CUDA(cudaStreamSynchronize(r->last_stream), "frame sync");
-  YV_CUDA(cudaMemcpy(c, r->d_counters, sizeof(c), cudaMemcpyDeviceToHost), "read counters");
+// Frame statistics from the counter words c of the last frame.
+static yv_status stats_from_counters(yv_renderer* r, const uint32_t* c, yv_frame_stats* stats) {
   r->frame_pending = false;
   stats->primary_rays = r->last_pixels;
   stats->hits = c[2];
@@ -580,6 +577,16 @@ yv_status yv_renderer_frame_stats(yv_renderer* r, yv_frame_stats* stats) {
   else if (c[1] & YV_DEV_ERR_TIMEOUT) st = YV_ERR_TIMEOUT;
   stats->status = (uint32_t)st;
   return st;
+}
+
+yv_status yv_renderer_frame_stats(yv_renderer* r, yv_frame_stats* stats) {
+  if (!r || !stats) return YV_ERR_INVALID_ARG;
+  std::memset(stats, 0, sizeof(*stats));
+  YV_CUDA(cudaSetDevice(r->device), "cudaSetDevice");
+  uint32_t c[kSvoCounterWords];
+  YV_CUDA(cudaStreamSynchronize(r->last_stream), "frame sync");
+  YV_CUDA(cudaMemcpy(c, r->d_counters, sizeof(c), cudaMemcpyDeviceToHost), "read counters");
+  return stats_from_counters(r, c, stats);
 }
 
 yv_status yv_render_frame(yv_renderer* r, uint32_t* host_rgba, void* device_rgba, void* stream) {
@@ -607,8 +614,17 @@ yv_status yv_render_frame(yv_renderer* r, uint32_t* host_rgba, void* device_rgba
   if (st != YV_OK) return st;
   if (host_rgba)
     YV_CUDA(cudaMemcpyAsync(host_rgba, dst, px * 4u, cudaMemcpyDeviceToHost, s), "read frame");
+  // the counters come back in the same stream as the frame: one wait
+  if (!r->h_counters)
+    YV_CUDA(cudaMallocHost(&r->h_counters, kSvoCounterWords * sizeof(uint32_t)),
+            "cudaMallocHost(counters)");
+  YV_CUDA(cudaMemcpyAsync(r->h_counters, r->d_counters, kSvoCounterWords * sizeof(uint32_t),
+                          cudaMemcpyDeviceToHost, s),
+          "read counters");
+  YV_CUDA(cudaStreamSynchronize(s), "frame sync");
   yv_frame_stats stats;
-  return yv_renderer_frame_stats(r, &stats);
+  std::memset(&stats, 0, sizeof(stats));
+  return stats_from_counters(r, r->h_counters, &stats);
 }
 
 }  // extern "C"
