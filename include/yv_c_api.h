@@ -427,7 +427,9 @@ yv_status yv_volume_upload_dense(const float* density, const uint8_t* rgb,
 /* BrickPool::Update in place: rebuilds `vol` (same precision) from a new
  * lattice on `stream`, reusing its device arrays when they are large enough
  * (growing them otherwise).  Work already queued that reads `vol` must be
- * ordered before this call by the caller (same stream, or a sync). */
+ * ordered before this call by the caller (same stream, or a sync), and a
+ * yv_volume_device taken from `vol` before the call is stale after it:
+ * take it again with yv_volume_gpu_desc. */
 yv_status yv_volume_rebuild_dense(yv_volume_gpu* vol, const float* density,
                                   const uint8_t* rgb, int32_t levels,
                                   void* stream);
