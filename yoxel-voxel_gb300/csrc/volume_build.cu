@@ -250,21 +250,20 @@ __global__ void pack_bricks_kernel(Lattice g, const uint64_t* cells, uint32_t nb
     // any is used
     for (int q0 = 0; q0 < (kVL3 + 31) / 32; q0 += 8) {
       float pv[8];
-      uint32_t nzf = 0;
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const int k = (int)lane + 32 * (q0 + u);
         pv[u] = k < kVL3 ? __ldg(g.d + lat(g, cx * kVB + k % kVL, cy * kVB + (k / kVL) % kVL,
                                             cz * kVB + k / (kVL * kVL)))
                          : 0.f;
-        // non-zero as stored (the fp16 formats round small values to 0)
-        const bool nzv = half ? (f16_saturating(pv[u]) & 0x7FFFu) != 0 : pv[u] != 0.f;
-        nzf |= (k < kVL3 && nzv ? 1u : 0u) << u;
       }
       if (mask) {
+        // after all 8 loads are issued: the non-zero points as stored (the
+        // fp16 formats round small values to 0), one ballot per 32
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-          const uint32_t bits = __ballot_sync(0xFFFFFFFFu, (nzf >> u) & 1u);
+          const bool nzv = half ? (f16_saturating(pv[u]) & 0x7FFFu) != 0 : pv[u] != 0.f;
+          const uint32_t bits = __ballot_sync(0xFFFFFFFFu, nzv);
           if (lane == 0 && q0 + u < 24) nz[q0 + u] = bits;
         }
       }
