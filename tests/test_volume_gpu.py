@@ -421,3 +421,25 @@ def test_brick_bits_and_cheap_empty_cells(yoxel_mod, precision):
     for a, b in zip(*outs):
         assert np.array_equal(a, b)
     assert outs[0][2].sum() > 0
+
+
+@pytest.mark.parametrize("levels", [1, 3])
+def test_brick_bits_other_tree_depths(yoxel_mod, levels):
+    """The bitmap at the smallest tree (4^3 brick cells, two words) and at a
+    512^3 volume; an empty tree gives an all-zero bitmap."""
+    import torch
+    from yoxel import _lib as L
+    vol = yoxel_mod.BrickVolume.noise(levels, 0.4, 1.4, 29)
+    want = expected_brick_bits(vol)
+    gv = vol.upload(3)
+    assert np.array_equal(_device_words(gv.desc().brick_bits, len(want)), want)
+    got = yoxel_mod.brick_bits(gv.desc()).cpu().numpy().view(np.uint32)
+    assert np.array_equal(got, want)
+    n = 8 * 4 ** levels + 1
+    empty = yoxel_mod.BrickVolume.from_dense(levels, np.zeros((n, n, n), np.float32))
+    assert empty.nbricks == 0
+    tv = empty.to_torch()
+    assert not tv["brick_bits"].any()
+    d = yoxel_mod.torch_desc(tv)
+    out = yoxel_mod.render_volume(d, [cam_at([1.6, 1.3, 1.1])], 16, 16)
+    assert not out.any()
