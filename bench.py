@@ -973,7 +973,10 @@ def run_build(args, cfg):
                 "h2d_bytes_per_step": 4 * vox, "d2h_bytes_per_step": 40 * nn + 8 * na,
                 "path": "density from pinned host memory, yoxel.SVOScene.build_dense (pool "
                         "copied back into a host container)"},
-        "gpu_launches": None, "clocks": clocks, "wall_s_timed_region": round(wall, 4)})
+        # 67 kernels per 1024^3 build (the ncu launch list of the same command)
+        "gpu_launches": args.steps * 67,
+        "gpu_launches_source": "ncu launch list, profiles/svo_build_dense_1024.md",
+        "clocks": clocks, "wall_s_timed_region": round(wall, 4)})
     if not args.no_cpu_baseline:
         from oracle import pyoracle
         sd = 8
@@ -1064,7 +1067,10 @@ def run_vbuild(args, cfg):
                 "h2d_bytes_per_step": 4 * vox, "d2h_bytes_per_step": 4 * 729 * nb * 4,
                 "path": "lattice from pinned host memory, yoxel.BrickVolume.build_dense (pool "
                         "copied back into a host container)"},
-        "gpu_launches": None, "clocks": clocks, "wall_s_timed_region": round(wall, 4)})
+        # 21 kernels per 513^3 rebuild (the ncu launch list of the same command)
+        "gpu_launches": args.steps * 21,
+        "gpu_launches_source": "ncu launch list, profiles/volume_build_dense_513.md",
+        "clocks": clocks, "wall_s_timed_region": round(wall, 4)})
     if not args.no_cpu_baseline:
         cpu = lat.cpu().numpy()
         t0 = time.perf_counter()
