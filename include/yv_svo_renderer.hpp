@@ -205,6 +205,16 @@ class GPURenderer : public ISVORenderer {
     if (r_) yv_get_detail_coef(r_, &c);
     return c;
   }
+  /* Frame time budget of the ray queue (no reference counterpart; 0 = none):
+   * a frame past it reports YV_ERR_TIMEOUT through Status(). */
+  void SetFrameBudget(uint32_t microseconds) {
+    if (r_) status_ = yv_set_frame_budget(r_, microseconds);
+  }
+  uint32_t GetFrameBudget() const {
+    uint32_t us = 0;
+    if (r_) yv_get_frame_budget(r_, &us);
+    return us;
+  }
   void SetSSNA(bool enable) { Ssna().ssna = enable ? 1 : 0; }
   bool GetSSNA() { return Ssna().ssna != 0; }
   void SetShowNormals(bool enable) { Ssna().show_normals = enable ? 1 : 0; }
