@@ -98,9 +98,20 @@ cudaError_t launch_svo_frame(const SvoDeviceScene& sc, const SvoFrameArgs& a,
   uint32_t refill = (uint32_t)(cfg.tile_rays <= 0 ? 32 : cfg.tile_rays);
   if (refill > 32) refill = 32;
   // register budget: blocks_per_sm 2 (up to 128 regs), 3 (80), 4 (64), 5
-  // (51); 0 = default 5 (fastest on the 2048^3 frame with unstaged node
-  // reads: 0.991 ms against 1.003 at 4; 6 blocks spill)
-  const int mb = cfg.blocks_per_sm <= 0 ? 5 : (cfg.blocks_per_sm > 5 ? 5 : cfg.blocks_per_sm);
+  // (51).  0 = by the frame's size: 5 (fastest on the 2048^3 frame with
+  // unstaged node reads: 0.991 ms against 1.003 at 4 and 1.105 at 3; 6
+  // blocks spill), fewer while the frame holds under two 8x4-pixel tiles
+  // per resident warp, down to 3 (a warp takes a tile at a time, so a small
+  // frame ends on the warps that took two: the 512^2 frame 0.108 ms at 5,
+  // 0.104 at 4, 0.100 at 3)
+  int mb = cfg.blocks_per_sm > 5 ? 5 : cfg.blocks_per_sm;
+  if (mb <= 0) {
+    const uint64_t tiles = (a.id_end - a.id_begin) / 32u;
+    const uint64_t warps_per_block = (uint64_t)(bt / 32);
+    mb = 5;
+    while (mb > 3 && tiles < 2ull * (uint64_t)device_sm_count() * (uint64_t)mb * warps_per_block)
+      --mb;
+  }
   cudaError_t e;
   if (sc.ref_layout) {
     // a caller VoxNode pool (an editable scene's device mirror): checked
