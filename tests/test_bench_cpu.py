@@ -53,3 +53,17 @@ def test_reference_arm_line_on_the_host_cores():
 def test_reference_arm_unavailable_without_a_cpu_form(config):
     d = run_ref("--config", config)
     assert d["impl"] == "reference" and "unavailable" in d
+
+
+@pytest.mark.parametrize("name", ["svo_frame_cfg2", "volume_forward_cfg3", "volume_backward_cfg4"])
+def test_profile_figures_the_bench_line_cites(bench, name):
+    """The committed ncu summaries carry the figures the bench line reports
+    beside its roofline: DRAM and L2 bytes per launch and the issue side."""
+    t = bench.profile_traffic(name)
+    l2 = bench.profile_l2(name)
+    iss = bench.profile_issue(name)
+    assert t and t > 1e6
+    assert l2 and l2["bytes_per_launch"] > t and 0 < l2["pct_of_peak_sector_rate"] < 100
+    assert iss and 0 < iss["issue_active_pct"] <= 100 and 0 < iss["simd_efficiency_pct"] <= 100
+    assert iss["thread_instructions_per_unit"] > 0 and iss["unit"]
+    assert name in iss["source"] and name in l2["source"]
