@@ -1311,6 +1311,12 @@ def main():
         return run_reference(args, cfg)
     if cfg["kind"] == "svo":
         return run_svo(args, cfg)
+    if dist_env()[0] > 1:
+        # the multi-GPU form shards one SVO frame by tile ranges; the other
+        # workloads run on one GPU (their sharding - volume tiles, batch
+        # scenes, training cameras - is host logic in yoxel.parallel)
+        raise SystemExit(f"--gpus > 1 shards the SVO frame workloads (cfg1, cfg2, lod); "
+                         f"run {args.config} on one GPU")
     if cfg["kind"] == "brick":
         return run_brick(args, cfg)
     if cfg["kind"] == "train":
