@@ -178,6 +178,15 @@ def test_status_codes(yoxel_mod):
     with pytest.raises(yoxel_mod.YvError) as e:
         r.SetSceneArrays(node, 0, np.zeros(0, yoxel_mod.ATTR_DTYPE))
     assert e.value.status == 3
+    # frames up to 2^31 rays in 8x4 tiles (the ray ids are 32-bit); a thin
+    # frame counts its padding
+    from yoxel import _lib as L
+    r.SetResolution(8, 4 * ((1 << 26) - 1))
+    assert r.GetResolution() == (8, 4 * ((1 << 26) - 1))
+    for w, h in [(8, 1 << 28), (1, 1 << 28), (46341, 46341)]:
+        with pytest.raises(yoxel_mod.YvError) as e:
+            r.SetResolution(w, h)
+        assert e.value.status == L.YV_ERR_INVALID_ARG
 
 
 def test_vox_roundtrip_renders_identically(yoxel_mod, spheres, tmp_path):

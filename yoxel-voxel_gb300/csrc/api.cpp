@@ -381,8 +381,13 @@ yv_status yv_set_view_up(yv_renderer* r, const float up[3]) {
   return YV_OK;
 }
 yv_status yv_set_resolution(yv_renderer* r, int width, int height) {
-  if (!r || width <= 0 || height <= 0 || (long long)width * height > (1ll << 31))
+  // the frame kernel numbers rays in 8x4-pixel tiles with 32-bit ids: the
+  // padded ray count stays below 2^31
+  if (!r || width <= 0 || height <= 0 ||
+      (uint64_t)((width + 7) / 8) * (uint64_t)((height + 3) / 4) * 32u > 0x7FFFFFFFull) {
+    set_last_error("yv_set_resolution: frame of more than 2^31 rays in 8x4 tiles");
     return YV_ERR_INVALID_ARG;
+  }
   r->width = width;
   r->height = height;
   return YV_OK;

@@ -385,9 +385,10 @@ __device__ __forceinline__ void write_pixel(const SvoFrameArgs& a, uint32_t off,
   if (a.fetches) a.fetches[off] = f;
   if (a.shadow_fetches) a.shadow_fetches[off] = fs;
   if (a.normal) {
-    a.normal[3u * off] = __uint_as_float(at.y);
-    a.normal[3u * off + 1u] = __uint_as_float(at.z);
-    a.normal[3u * off + 2u] = __uint_as_float(at.w);
+    const size_t n = 3u * (size_t)off;  // off < 2^31: 3 off needs 64 bits
+    a.normal[n] = __uint_as_float(at.y);
+    a.normal[n + 1u] = __uint_as_float(at.z);
+    a.normal[n + 2u] = __uint_as_float(at.w);
   }
 }
 
