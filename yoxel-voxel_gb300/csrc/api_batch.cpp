@@ -75,8 +75,10 @@ yv_status prepare(yv_batch* b) {
     base += (uint64_t)it.tiles * 32u;
     table[(size_t)i] = it;
   }
-  if (base > 0xFFFFFF00ull) {
-    set_last_error("batch has more than 2^32 rays");
+  // 32-bit ray ids with room above for the queue counter's overshoot (every
+  // warp adds 32 past the end once), so the counter never wraps
+  if (base > 0x7FFFFFFFull) {
+    set_last_error("batch has more than 2^31 rays");
     return YV_ERR_INVALID_ARG;
   }
   b->total_ids = (uint32_t)base;

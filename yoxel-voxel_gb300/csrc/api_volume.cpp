@@ -69,6 +69,11 @@ bool fill_args(const yv_volume_device* v, const yv_march_params* mp, int width, 
       !(mp->step_vox > 0.f) || !std::isfinite(mp->alpha_scale) ||
       v->precision < YV_PRECISION_F16 || v->precision > YV_PRECISION_F16_PACKED)
     return false;
+  // warp tiles of one launch (up to kMaxVolumeCams cameras, 16x16-pixel
+  // squares of 8 tiles) are numbered with 32-bit ids
+  const uint64_t sq_x = ((uint64_t)(width + 7) / 8 + 1) / 2;
+  const uint64_t sq_y = ((uint64_t)(height + 3) / 4 + 3) / 4;
+  if ((uint64_t)kMaxVolumeCams * sq_x * sq_y * 8u > 0x7FFFFFFFull) return false;
   // packed formats keep the whole lattice point in the albedo buffer
   const bool packed = v->precision >= YV_PRECISION_F32_PACKED;
   if (v->nbricks && (!v->albedo || (!packed && !v->density))) return false;
