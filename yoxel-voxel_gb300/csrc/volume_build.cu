@@ -103,6 +103,106 @@ __global__ void mark_rows_kernel(Lattice g, uint32_t* R) {
   }
 }
 
+// Mark, pass 1, flat form (lattice 16-byte aligned, 16 <= nb <= 256, so a
+// warp's 128 points touch at most two rows): the rows
+// in groups of 4 (4 L floats start on a 16-byte boundary, L = 8 nb + 1 being
+// odd only shifts the rows inside a group), read as float4 by one warp per
+// group, 128 points per warp load.  A lane marks the cells of its 4 points
+// (own cell x >> 3, apron cell x / 8 - 1 for x a non-zero multiple of 8) in
+// a 32-bit window of cells of the warp's row; one warp OR reduction per row
+// the load touches (at most 2), and lane 0 merges it into the group's row
+// words in shared memory.  Same R as mark_rows_kernel.
+constexpr uint32_t kFlatMaxNW = 8;
+
+__global__ void mark_rows_flat_kernel(Lattice g, uint32_t* R) {
+  __shared__ uint32_t acc_all[8][4][kFlatMaxNW];
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t(*acc)[kFlatMaxNW] = acc_all[(threadIdx.x >> 5) & 7u];
+  const uint32_t L = (uint32_t)g.L;
+  const uint32_t nb = (uint32_t)g.nb;
+  const uint32_t NW = nb >= 32 ? nb / 32u : 1u;
+  const uint64_t rows = g.L * g.L;
+  const uint64_t groups = (rows + 3) / 4;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const float4* d4 = reinterpret_cast<const float4*>(g.d);
+  for (uint64_t grp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; grp < groups;
+       grp += nwarps) {
+    const uint64_t left_rows = rows - grp * 4;
+    const uint32_t nrows = left_rows < 4 ? (uint32_t)left_rows : 4u;
+    const uint32_t nfl = nrows * L;             // floats of the group
+    const uint32_t n4 = (nfl + 3) / 4;          // float4 loads (the last may run past)
+    if (lane < 4 * kFlatMaxNW) acc[lane >> 3][lane & 7u] = 0u;
+    __syncwarp();
+    const float4* src = d4 + grp * (uint64_t)L;  // 4 L floats = L float4
+    // row and x of the warp's first point, advanced by 128 points a step
+    // (L > 128: at most one row boundary per step)
+    uint32_t ra = 0, xs = 0;
+    for (uint32_t f0 = 0; f0 < n4; f0 += 32u) {
+      const uint32_t f = f0 + lane;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (4u * f + 3u < nfl) {
+        v = __ldg(src + f);
+      } else if (f < n4) {
+        // the group's (and the lattice's) last points: no read past them
+        const float* s1 = reinterpret_cast<const float*>(src) + 4u * f;
+        const uint32_t left = nfl - 4u * f;
+        v.x = __ldg(s1);
+        if (left > 1u) v.y = __ldg(s1 + 1);
+        if (left > 2u) v.z = __ldg(s1 + 2);
+      }
+      // the warp's 128 points: rows ra (first point) .. ra + 1
+      const int c_lo = (int)(xs >> 3) - 1;  // window: cells c_lo .. c_lo + 31
+      const uint32_t rb = ra + 1;           // cells -1..30 of the next row
+      const uint32_t xl = xs + 4u * lane;   // x of the lane's first point in row ra
+      uint32_t wa = 0, wb = 0;
+      const float e[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const uint32_t i = 4u * f + (uint32_t)k;
+        if (e[k] == 0.f || i >= nfl) continue;
+        uint32_t x = xl + (uint32_t)k;
+        const bool next_row = x >= L;
+        if (next_row) x -= L;
+        const uint32_t own = x >> 3;  // x = 8 nb: no own cell
+        uint32_t bits = 0;
+        if (own < nb) bits |= 2u;                  // cell own
+        if ((x & 7u) == 0u && x > 0u) bits |= 1u;  // apron of cell own - 1
+        if (!next_row) {
+          wa |= bits << (own - (uint32_t)(c_lo + 1));
+        } else {
+          wb |= bits << own;  // window of row rb starts at cell -1
+        }
+      }
+      wa = __reduce_or_sync(0xFFFFFFFFu, wa);
+      wb = __reduce_or_sync(0xFFFFFFFFu, wb);
+      if (lane == 0) {
+        // window bit b = cell base + b: row ra base c_lo, row rb base -1
+        if (wa) {
+          int c0 = c_lo;
+          uint64_t s = wa;
+          if (c0 < 0) { s >>= 1; c0 = 0; }
+          s <<= (c0 & 31);
+          const uint32_t w = (uint32_t)c0 >> 5;
+          if (w < NW) acc[ra][w] |= (uint32_t)s;
+          if (w + 1 < NW) acc[ra][w + 1] |= (uint32_t)(s >> 32);
+        }
+        if (wb && rb < nrows) acc[rb][0] |= wb >> 1;
+      }
+      xs += 128u;
+      if (xs >= L) {
+        xs -= L;
+        ++ra;
+      }
+    }
+    __syncwarp();
+    if (lane < nrows * NW) {
+      const uint32_t r = lane / NW, w = lane % NW;
+      R[(grp * 4 + r) * NW + w] = acc[r][w] & (nb >= 32 ? 0xFFFFFFFFu : ((1u << nb) - 1u));
+    }
+    __syncwarp();
+  }
+}
+
 // Mark, pass 2: a cell is occupied when its bit is set in any of the 9 x 9
 // rows y in [8 cy, 8 cy + 8], z in [8 cz, 8 cz + 8].  One thread per row word
 // and (cy, cz); count = occupied cells, one atomic per warp.
@@ -377,7 +477,11 @@ yv_status build_volume_tree(const Lattice& g, int levels, cudaStream_t s, Volume
     const uint64_t NW = g.nb >= 32 ? (uint64_t)g.nb / 32 : 1;
     DevBuf rows;
     if ((e = rows.alloc(g.L * g.L * NW * 4, s)) != cudaSuccess) return vbuild_fail(e, "alloc");
-    mark_rows_kernel<<<grid_for(g.L * g.L * 32), 256, 0, s>>>(g, rows.as<uint32_t>());
+    if (g.nb >= 16 && NW <= kFlatMaxNW && (reinterpret_cast<uintptr_t>(g.d) & 15u) == 0)
+      mark_rows_flat_kernel<<<grid_for((g.L * g.L + 3) / 4 * 32), 256, 0, s>>>(
+          g, rows.as<uint32_t>());
+    else
+      mark_rows_kernel<<<grid_for(g.L * g.L * 32), 256, 0, s>>>(g, rows.as<uint32_t>());
     mark_cells_from_rows_kernel<<<grid_for(NW * g.nb * g.nb), 256, 0, s>>>(
         g, rows.as<uint32_t>(), any[(size_t)levels].as<uint8_t>(), dc.as<uint32_t>() + levels);
   }
