@@ -21,16 +21,22 @@
 namespace yv {
 namespace {
 
-// Dynamic shared memory: the per-lane frame ring of the SVO traversal,
-// 1 KB x kBatchRing per warp.
+// Dynamic shared memory: the item table (the batch's own items only, so a
+// small batch leaves more of the SM's memory to L1), then the per-lane frame
+// ring of the SVO traversal, 1 KB x kBatchRing per warp.
 constexpr int kBatchRing = 4;
+
+__host__ __device__ __forceinline__ uint32_t item_table_vec4(int nitems) {
+  return (uint32_t)(((size_t)nitems * sizeof(BatchItem) + 15u) / 16u);
+}
 
 // kP: the lattice format of every brick item (its march alone is compiled
 // in), or -1 for a batch mixing formats (all four marches).
 template <int kMinBlocks, int kP>
 __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
-  __shared__ BatchItem items[kMaxBatchItems];
-  extern __shared__ uint4 ring_smem[];
+  extern __shared__ uint4 dyn_smem[];
+  BatchItem* items = reinterpret_cast<BatchItem*>(dyn_smem);
+  uint4* ring_smem = dyn_smem + item_table_vec4(b.nitems);
   {
     const uint32_t words = (uint32_t)(b.nitems * (int)sizeof(BatchItem) / 4);
     const uint32_t* src = reinterpret_cast<const uint32_t*>(b.items);
@@ -156,16 +162,18 @@ __global__ void __launch_bounds__(256, kMinBlocks) batch_kernel(BatchLaunch b) {
 template <int kMinBlocks, int kP>
 cudaError_t launch_batch_with(const BatchLaunch& b, int bt, cudaStream_t s) {
   auto kern = batch_kernel<kMinBlocks, kP>;
-  const size_t smem = (size_t)(bt / 32) * kBatchRing * 1024u;
+  const size_t smem =
+      (size_t)item_table_vec4(b.nitems) * 16u + (size_t)(bt / 32) * kBatchRing * 1024u;
   static bool opted_in[64] = {false};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) dev = 0;
   cudaError_t e = cudaSuccess;
   if (!opted_in[dev]) {
-    // the item table is static shared memory; the ring is dynamic
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             8 * kBatchRing * 1024);
+    // room for the largest table and ring
+    e = cudaFuncSetAttribute(
+        kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        (int)((size_t)item_table_vec4(kMaxBatchItems) * 16u + 8u * kBatchRing * 1024u));
     if (e != cudaSuccess) return e;
     opted_in[dev] = true;
   }
