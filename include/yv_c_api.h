@@ -459,6 +459,24 @@ yv_status yv_volume_render(const yv_volume_device* vol, const yv_camera* cams,
                            const yv_march_params* mp, float* rgba,
                            uint32_t* samples, uint32_t* bricks, void* stream);
 
+/* A frame split into ranges of warp tiles (the multi-GPU shards of one
+ * frame, as the SVO frames' yv_render_frame_tiles; no reference
+ * counterpart).  The march takes 8x4-pixel tiles in 16x16-pixel squares of
+ * 8: tile id = (square row * squares per row + square column) * 8 + (tile
+ * row within the square) * 2 + tile column within the square, camera-major
+ * over the ncams frames.  yv_volume_tile_count gives the tiles of one
+ * camera's frame. */
+yv_status yv_volume_tile_count(int32_t width, int32_t height, uint32_t* tiles_per_camera);
+/* yv_volume_render over tiles [tile_begin, tile_end) of the ncams (<= 64)
+ * frames only: the other pixels of rgba / samples / bricks are left as
+ * they are.  Ranges that start on a multiple of 8 keep each block of the
+ * launch on one 16x16-pixel square. */
+yv_status yv_volume_render_tiles(const yv_volume_device* vol, const yv_camera* cams,
+                                 int32_t ncams, int32_t width, int32_t height,
+                                 const yv_march_params* mp, uint32_t tile_begin,
+                                 uint32_t tile_end, float* rgba, uint32_t* samples,
+                                 uint32_t* bricks, void* stream);
+
 /* Adjoint of yv_volume_render (fp32 volumes, plain or packed): re-marches
  * every ray and accumulates dL/ddensity and dL/dalbedo (pool layout, ADDED
  * to the buffers) from dL/drgba, given the forward output rgba. */

@@ -146,3 +146,30 @@ def test_gloo_sharded_frame_tiles_cover_the_frame_once():
         y0, y1 = res[r][1]
         assert all(y0 <= y < y1 for y in painted)  # the rows read back hold the tiles
     assert (merged >= 0).all()  # every pixel painted once
+
+
+def test_volume_tile_order_covers_the_frame_in_squares():
+    """The march's tile order: every 8x4 tile of the (padded) frame once,
+    8 consecutive ids on one 16x16-pixel square; costs follow the order and
+    ranges split on square boundaries cover every tile once."""
+    from yoxel import parallel as P
+    for w, h in [(64, 32), (33, 17), (1024, 1024), (100, 60)]:
+        ox, oy = P.volume_tile_order(w, h)
+        tx, ty = (w + 7) // 8, (h + 3) // 4
+        assert len(ox) % 8 == 0
+        seen = set(zip(ox.tolist(), oy.tolist()))
+        assert len(seen) == len(ox)
+        assert {(x, y) for x in range(tx) for y in range(ty)} <= seen
+        sq = np.stack([ox // 2, oy // 4], 1).reshape(-1, 8, 2)
+        assert (sq == sq[:, :1]).all()
+        cost = np.random.default_rng(w).random((2, h, w))
+        c = P.volume_tile_costs(cost, w, h)
+        assert len(c) == 2 * len(ox)
+        k = len(ox) // 2 + 3
+        x0, y0 = ox[k] * 8, oy[k] * 4
+        assert np.isclose(c[len(ox) + k] - 1.0, cost[1, y0:y0 + 4, x0:x0 + 8].sum())
+        for world in (1, 2, 3, 5):
+            rs = P.partition_volume_tiles(c, world)
+            assert rs[0][0] == 0 and rs[-1][1] == len(c)
+            assert all(b % 8 == 0 and e % 8 == 0 and b <= e for b, e in rs)
+            assert all(rs[i][1] == rs[i + 1][0] for i in range(world - 1))

@@ -443,3 +443,47 @@ def test_brick_bits_other_tree_depths(yoxel_mod, levels):
     d = yoxel_mod.torch_desc(tv)
     out = yoxel_mod.render_volume(d, [cam_at([1.6, 1.3, 1.1])], 16, 16)
     assert not out.any()
+
+
+@pytest.mark.parametrize("world", [1, 3, 4])
+def test_volume_tile_ranges_merge_to_the_full_frame(yoxel_mod, world):
+    """A volume frame split into warp-tile ranges of equal estimated cost
+    (the multi-GPU shards of one frame) renders the full frame bit for bit
+    once the ranges are merged - radiance, samples and bricks - and a range
+    writes only its own tiles."""
+    import torch
+    from yoxel import _lib as L
+    from yoxel import parallel as P
+    vol = yoxel_mod.BrickVolume.noise(2, 0.4, 1.4, 31)
+    d = vol.upload(3).desc()
+    cams = [cam_at([1.6, 1.3, 1.1]), cam_at([-0.7, 0.4, 0.9], 50.0)]
+    w, h = 100, 60
+    ns = torch.zeros((2, h, w), dtype=torch.int32, device="cuda")
+    nb = torch.zeros((2, h, w), dtype=torch.int32, device="cuda")
+    full = yoxel_mod.render_volume(d, cams, w, h, samples=ns, bricks=nb)
+    per_cam = yoxel_mod.volume_tile_count(w, h)
+    costs = P.volume_tile_costs(ns.cpu().numpy(), w, h)
+    assert len(costs) == 2 * per_cam
+    ranges = P.partition_volume_tiles(costs, world)
+    out = torch.full((2, h, w, 4), -5.0, device="cuda")
+    ns2 = torch.full((2, h, w), -5, dtype=torch.int32, device="cuda")
+    nb2 = torch.full((2, h, w), -5, dtype=torch.int32, device="cuda")
+    ox, oy = P.volume_tile_order(w, h)
+    for k, (tb, te) in enumerate(ranges):
+        yoxel_mod.render_volume_tiles(d, cams, w, h, tb, te, out, samples=ns2, bricks=nb2)
+        if k == 0 and world > 1:
+            written = np.zeros((2, h, w), bool)
+            for t in range(tb, te):
+                c, i = divmod(t, per_cam)
+                written[c, oy[i] * 4:oy[i] * 4 + 4, ox[i] * 8:ox[i] * 8 + 8] = True
+            got = ns2.cpu().numpy()
+            assert (got[~written] == -5).all() and (got[written] != -5).all()
+    assert torch.equal(out.view(torch.int32), full.view(torch.int32))
+    assert torch.equal(ns2, ns) and torch.equal(nb2, nb)
+    # an empty range writes nothing; a range past the frames is refused
+    out.fill_(-5.0)
+    yoxel_mod.render_volume_tiles(d, cams, w, h, 8, 8, out)
+    assert (out == -5.0).all()
+    with pytest.raises(L.YvError) as e:
+        yoxel_mod.render_volume_tiles(d, cams, w, h, 0, 2 * per_cam + 1, out)
+    assert e.value.status == L.YV_ERR_INVALID_ARG

@@ -374,6 +374,45 @@ yv_status yv_volume_render(const yv_volume_device* vol, const yv_camera* cams, i
   return YV_OK;
 }
 
+yv_status yv_volume_tile_count(int32_t width, int32_t height, uint32_t* tiles_per_camera) {
+  if (width <= 0 || height <= 0 || !tiles_per_camera) return YV_ERR_INVALID_ARG;
+  *tiles_per_camera = volume_tiles_per_camera(width, height);
+  return YV_OK;
+}
+
+yv_status yv_volume_render_tiles(const yv_volume_device* vol, const yv_camera* cams,
+                                 int32_t ncams, int32_t width, int32_t height,
+                                 const yv_march_params* mp, uint32_t tile_begin,
+                                 uint32_t tile_end, float* rgba, uint32_t* samples,
+                                 uint32_t* bricks, void* stream) {
+  if (ncams > kMaxVolumeCams) return YV_ERR_INVALID_ARG;
+  VolumeArgs* a = new (std::nothrow) VolumeArgs;
+  if (!a) return YV_ERR_OUT_OF_MEMORY;
+  if (!fill_args(vol, mp, width, height, a) || !cams_ok(cams, ncams) || !rgba) {
+    delete a;
+    return YV_ERR_INVALID_ARG;
+  }
+  const uint64_t total = (uint64_t)volume_tiles_per_camera(width, height) * (uint64_t)ncams;
+  if (tile_begin > tile_end || tile_end > total) {
+    delete a;
+    set_last_error("yv_volume_render_tiles: tile range outside the frames");
+    return YV_ERR_INVALID_ARG;
+  }
+  if (tile_begin == tile_end) {
+    delete a;
+    return YV_OK;
+  }
+  set_cams(a, cams, ncams);
+  a->rgba = rgba;
+  a->samples = samples;
+  a->bricks_entered = bricks;
+  a->tile_begin = tile_begin;
+  a->tile_end = tile_end;
+  const cudaError_t e = launch_volume_forward(*a, static_cast<cudaStream_t>(stream));
+  delete a;
+  return e == cudaSuccess ? YV_OK : fail(e, "volume forward launch");
+}
+
 yv_status yv_volume_render_rgba8(const yv_volume_device* vol, const yv_camera* cams,
                                  int32_t ncams, int32_t width, int32_t height,
                                  const yv_march_params* mp, uint32_t* rgba8, void* stream) {

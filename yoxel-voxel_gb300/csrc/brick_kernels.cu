@@ -65,11 +65,12 @@ __global__ void __launch_bounds__(256, kMinBlocks) volume_forward_kernel(VolumeA
   // grid nodes are read through L1 (see prefer_l1)
   const uint32_t* sg = nullptr;
   const uint32_t nsg = 0;
-  const uint32_t n_tiles = tile_ids(a);
+  // the launch's tiles (a range of them for a frame split across GPUs)
+  const uint32_t n_tiles = a.tile_end ? a.tile_end : tile_ids(a);
   const uint32_t warps = gridDim.x * (blockDim.x >> 5);
   bool bad = false;
-  for (uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile < n_tiles;
-       tile += warps) {
+  for (uint32_t tile = a.tile_begin + blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+       tile < n_tiles; tile += warps) {
     int cam, x, y;
     if (!ray_of_thread(a, tile, cam, x, y)) continue;
     float o[3], d[3];
@@ -307,8 +308,14 @@ void prefer_l1() {
 
 }  // namespace
 
+uint32_t volume_tiles_per_camera(int width, int height) {
+  const uint32_t tx = (uint32_t)((width + 7) >> 3), ty = (uint32_t)((height + 3) >> 2);
+  return ((tx + 1) >> 1) * ((ty + 3) >> 2) * 8u;
+}
+
 cudaError_t launch_volume_forward(const VolumeArgs& a, cudaStream_t s) {
-  const uint32_t tiles = tile_ids(a);
+  const uint32_t end = a.tile_end ? a.tile_end : tile_ids(a);
+  const uint32_t tiles = end > a.tile_begin ? end - a.tile_begin : 0u;
   const uint32_t blocks = (tiles + 7) / 8;
   if (blocks == 0) return cudaSuccess;
   prefer_l1();

@@ -59,9 +59,15 @@ struct VolumeArgs {
   float* grad_albedo;
   float4* grad_packed;    // backward scratch: (albedo rgb, density) per lattice point
   uint32_t* status;       // optional device status word
+  // forward only: warp tiles [tile_begin, tile_end) of the launch (march
+  // order, see tile_ids); tile_end = 0: all of them
+  uint32_t tile_begin, tile_end;
 };
 
 cudaError_t launch_volume_forward(const VolumeArgs& a, cudaStream_t s);
+// Warp tiles of one camera's width x height frame in the march's order:
+// 16x16-pixel squares (row-major) of 8 tiles of 8x4 pixels.
+uint32_t volume_tiles_per_camera(int width, int height);
 cudaError_t launch_volume_backward(const VolumeArgs& a, cudaStream_t s);
 // packed[i] = (albedo rgb, density) of n lattice points (fp32 layouts).
 cudaError_t launch_pack_f32(const float* density, const float* albedo, uint32_t n,

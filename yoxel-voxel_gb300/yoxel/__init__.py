@@ -10,6 +10,7 @@ from .svo import SVOScene, NODE_DTYPE, ATTR_DTYPE
 from .renderer import Renderer, CudaRenderer
 from .volume import (BrickVolume, VolumeGPU, render_volume, render_volume_rgba8,
                      volume_backward, volume_march, torch_desc, pack_volume, brick_bits,
+                     render_volume_tiles, volume_tile_count,
                      cameras, sphere_cameras)
 
 from .batch import Batch
@@ -17,6 +18,6 @@ from .dynamic import DynamicSVO
 
 __all__ = ["SVOScene", "Renderer", "CudaRenderer", "YvError", "LIB_PATH", "Batch",
            "NODE_DTYPE", "ATTR_DTYPE", "DynamicSVO", "BrickVolume", "VolumeGPU", "render_volume",
-           "render_volume_rgba8",
+           "render_volume_rgba8", "render_volume_tiles", "volume_tile_count",
            "volume_backward", "volume_march", "torch_desc", "pack_volume", "brick_bits",
            "cameras", "sphere_cameras"]

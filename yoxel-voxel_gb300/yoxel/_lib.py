@@ -180,6 +180,10 @@ _SIGS = {
     "yv_volume_rebuild_dense": (S, [P, P, P, C.c_int32, P]),
     "yv_volume_gpu_desc": (S, [P, C.POINTER(VolumeDevice)]),
     "yv_volume_brick_bits": (S, [C.POINTER(VolumeDevice), P, P]),
+    "yv_volume_tile_count": (S, [C.c_int32, C.c_int32, C.POINTER(C.c_uint32)]),
+    "yv_volume_render_tiles": (S, [C.POINTER(VolumeDevice), C.POINTER(Camera), C.c_int32,
+                                   C.c_int32, C.c_int32, C.POINTER(MarchParams), C.c_uint32,
+                                   C.c_uint32, P, P, P, P]),
     "yv_volume_render": (S, [C.POINTER(VolumeDevice), C.POINTER(Camera), C.c_int32, C.c_int32,
                              C.c_int32, C.POINTER(MarchParams), P, P, P, P]),
     "yv_volume_render_rgba8": (S, [C.POINTER(VolumeDevice), C.POINTER(Camera), C.c_int32,

@@ -66,6 +66,45 @@ def tile_rows(tile_range, width, height):
     return (tb // tx) * 4, min(height, ((te - 1) // tx + 1) * 4)
 
 
+def volume_tile_order(width, height):
+    """Tile coordinates (tile column, tile row) of the warp tiles of one
+    camera's volume frame in the march's order (yv_volume_render_tiles):
+    16x16-pixel squares row-major, 8 tiles of 8x4 pixels per square (tile
+    column within the square fastest).  Padding tiles lie outside the
+    frame."""
+    tx, ty = (width + 7) // 8, (height + 3) // 4
+    stx, sty = (tx + 1) // 2, (ty + 3) // 4
+    ids = np.arange(stx * sty * 8)
+    st, w = ids >> 3, ids & 7
+    return (st % stx) * 2 + (w & 1), (st // stx) * 4 + (w >> 1)
+
+
+def volume_tile_costs(pixel_cost, width, height):
+    """Cost per warp tile of volume frames in the march's order, camera-major,
+    from a per-pixel cost map ((ncams,) h, w), e.g. the samples of a previous
+    frame; every tile costs at least 1 (padding tiles too)."""
+    c = np.asarray(pixel_cost, np.float64).reshape(-1, height, width)
+    n = c.shape[0]
+    tx, ty = (width + 7) // 8, (height + 3) // 4
+    stx, sty = (tx + 1) // 2, (ty + 3) // 4
+    pad = np.zeros((n, sty * 16, stx * 16), np.float64)
+    pad[:, :height, :width] = c
+    per_tile = pad.reshape(n, sty * 4, 4, stx * 2, 8).sum(axis=(2, 4))
+    ox, oy = volume_tile_order(width, height)
+    return per_tile[:, oy, ox].reshape(-1) + 1.0
+
+
+def partition_volume_tiles(tile_costs, world):
+    """partition_tiles with every boundary on a multiple of 8 tiles (one
+    16x16-pixel square, the footprint of a block of the march)."""
+    c = np.asarray(tile_costs, np.float64)
+    n = len(c)
+    sq = c.reshape(-1, 8).sum(axis=1) if n % 8 == 0 else c
+    if n % 8:
+        raise ValueError("volume tile counts are multiples of 8")
+    return [(8 * b, 8 * e) for b, e in partition_tiles(sq, world)]
+
+
 def partition_cameras(ncams, world):
     """Contiguous camera ranges per rank (data parallelism over views)."""
     base, extra = divmod(ncams, world)

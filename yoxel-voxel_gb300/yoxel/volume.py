@@ -302,6 +302,32 @@ def render_volume(desc, cams, width, height, alpha_scale=1.0, step_vox=0.5, out=
     return out
 
 
+def volume_tile_count(width, height):
+    """Warp tiles of one camera's frame in the march's order (8x4-pixel
+    tiles in 16x16-pixel squares of 8)."""
+    n = C.c_uint32()
+    L.check(L.lib.yv_volume_tile_count(int(width), int(height), C.byref(n)),
+            "yv_volume_tile_count")
+    return n.value
+
+
+def render_volume_tiles(desc, cams, width, height, tile_begin, tile_end, out,
+                        alpha_scale=1.0, step_vox=0.5, samples=None, bricks=None,
+                        stream=None):
+    """render_volume over warp tiles [tile_begin, tile_end) only (camera-major
+    ids; volume_tile_count per camera) into full-frame tensors: the other
+    pixels are left as they are (one shard of a frame split across GPUs)."""
+    ca = cams if isinstance(cams, C.Array) else cameras(cams)
+    mp = L.MarchParams(float(alpha_scale), float(step_vox))
+    L.check(L.lib.yv_volume_render_tiles(
+        C.byref(desc), ca, len(ca), width, height, C.byref(mp), int(tile_begin), int(tile_end),
+        C.c_void_p(out.data_ptr()),
+        None if samples is None else C.c_void_p(samples.data_ptr()),
+        None if bricks is None else C.c_void_p(bricks.data_ptr()), _stream(stream)),
+        "yv_volume_render_tiles")
+    return out
+
+
 def render_volume_rgba8(desc, cams, width, height, alpha_scale=1.0, step_vox=0.5, out=None,
                         stream=None):
     """RGBA8 frames (ntree RunTrace's uchar4 image): (ncams, h, w) int32 CUDA
