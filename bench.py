@@ -624,11 +624,29 @@ def _base_line(args, cfg, value, ms, dtype):
 
 
 def run_brick(args, cfg):
-    """cfg3: plain brick march, fp16 pool."""
+    """cfg3: plain brick march, fp16 pool.  Under torchrun (N > 1) the frame
+    is split into warp-tile ranges of near-equal sample count (the samples
+    of a first frame; yoxel.parallel.partition_volume_tiles), each rank
+    renders its range (yv_volume_render_tiles), and `value` = the frame's
+    rays / the slowest rank's time (strong scaling); no collective on the
+    data path."""
     import torch
     import yoxel
+    from yoxel import parallel as P
     from yoxel import workloads as W
-    torch.cuda.set_device(dist_env()[2])
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+        torch.cuda.synchronize()
+
     t_scene = time.perf_counter()
     vol = yoxel.BrickVolume.noise(cfg["levels"], 0.4, 1.4, cfg_seed(cfg))
     t_scene = time.perf_counter() - t_scene
@@ -650,31 +668,61 @@ def run_brick(args, cfg):
     per_corner = 5 if prec in (0, 3) else 16
     alg = 8 * per_corner * S + 4 * cfg["levels"] * B + 16 * rays
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    fn = lambda: yoxel.render_volume(desc, cam, w, h, cfg["alpha_scale"], cfg["step_vox"],
-                                     out=out)
+    y0, y1 = 0, h
+    if ws > 1:
+        # this rank's squares of warp tiles and the pixel rows they hold
+        ranges = P.partition_volume_tiles(P.volume_tile_costs(ns.cpu().numpy(), w, h), ws)
+        tb, te_t = ranges[rank]
+        stx = ((w + 7) // 8 + 1) // 2
+        if te_t > tb:
+            y0, y1 = (tb // 8 // stx) * 16, min(h, ((te_t - 1) // 8 // stx + 1) * 16)
+        share = float(ns[:, y0:y1].to(torch.int64).sum()) / max(1, S)
+        alg = int(alg * share)  # this rank's part of the bytes (rows it covers)
+        fn = lambda: yoxel.render_volume_tiles(desc, cam, w, h, tb, te_t, out,
+                                               cfg["alpha_scale"], cfg["step_vox"])
+    else:
+        fn = lambda: yoxel.render_volume(desc, cam, w, h, cfg["alpha_scale"],
+                                         cfg["step_vox"], out=out)
     for _ in range(args.warmup):
         flush.fill_(1)
         fn()
-    sampler = ClockSampler(dist_env()[2])
+    barrier()
+    sampler = ClockSampler(local)
     sampler.start()
     time.sleep(0.4)
+    barrier()
     ms, wall = _timed_steps(torch, args.steps, fn, lambda: flush.fill_(1))
+    barrier()
     clocks = sampler.stop()
     mean_ms = sum(ms) / len(ms)
     host = torch.empty((1, h, w, 4), dtype=torch.float32, pin_memory=True)
     torch.cuda.synchronize()
+    barrier()
     te = time.perf_counter()
     for _ in range(args.steps):
         fn()
-        host.copy_(out)  # synchronous D2H into pinned memory
+        host[:, y0:y1].copy_(out[:, y0:y1])  # synchronous D2H into pinned memory
+    barrier()
     e2e_s = (time.perf_counter() - te) / args.steps
+    my_ms = mean_ms
+    if pg is not None:
+        tot = torch.tensor([mean_ms, e2e_s], dtype=torch.float64, device="cuda")
+        pg.all_reduce(tot, op=pg.ReduceOp.MAX)
+        mean_ms, e2e_s = float(tot[0]), float(tot[1])
+        if rank != 0:
+            pg.destroy_process_group()
+            return
     peaks, kind = measured_peaks()
-    achieved = alg / (mean_ms / 1e3) / 1e9
+    achieved = alg / (my_ms / 1e3) / 1e9
     line = _base_line(args, cfg, rays / (mean_ms / 1e3) / 1e6, mean_ms,
                       "f32 (fp16 storage)" if prec in (0, 3) else "f32")
     line["config"].update(volume_bricks=vol.nbricks, occupancy=round(vol.occupancy, 4),
                           mean_samples_per_ray=round(S / rays, 2),
                           pool_format=POOL_FORMATS[prec])
+    if ws > 1:
+        line["scaling"] = "strong"
+        line["config"]["parallelism"] = (f"one frame split into {ws} warp-tile ranges of "
+                                         f"near-equal samples (rank 0: tiles {tb}..{te_t})")
     line.update({
         "roofline": {"bound": "hbm", "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"],
                      "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 4),
@@ -685,11 +733,13 @@ def run_brick(args, cfg):
                      "issue": profile_issue("volume_forward_cfg3"),
                      "l2": profile_l2("volume_forward_cfg3")},
         "e2e": {"value": round(rays / e2e_s / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": 40,
-                "d2h_bytes_per_step": rays * 16,
-                "path": "yoxel.render_volume + copy into pinned host memory"},
+                "d2h_bytes_per_step": (y1 - y0) * w * 16,
+                "path": ("yoxel.render_volume + copy into pinned host memory" if ws == 1 else
+                         "yoxel.render_volume_tiles per rank, its rows copied into pinned "
+                         "host memory")},
         "gpu_launches": args.steps, "clocks": clocks, "wall_s_timed_region": round(wall, 4),
         "scene_build_s": round(t_scene, 2)})
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and ws == 1:
         from oracle import pyoracle
         den = vol.density.astype(np.float16 if prec in (0, 3) else np.float32)
         den = den.astype(np.float32)
@@ -710,6 +760,8 @@ def run_brick(args, cfg):
                                           "reaction/trace/trace.cu castRay over the ntree pool",
                                 "cpu_model": cpu_model()}
     print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
 
 
 def run_train(args, cfg):
@@ -1311,14 +1363,14 @@ def main():
         return run_reference(args, cfg)
     if cfg["kind"] == "svo":
         return run_svo(args, cfg)
-    if dist_env()[0] > 1:
-        # the multi-GPU form shards one SVO frame by tile ranges; the other
-        # workloads run on one GPU (their sharding - volume tiles, batch
-        # scenes, training cameras - is host logic in yoxel.parallel)
-        raise SystemExit(f"--gpus > 1 shards the SVO frame workloads (cfg1, cfg2, lod); "
-                         f"run {args.config} on one GPU")
     if cfg["kind"] == "brick":
         return run_brick(args, cfg)
+    if dist_env()[0] > 1:
+        # the multi-GPU form shards one frame by tile ranges (SVO and brick
+        # frames); the other workloads run on one GPU (their sharding - batch
+        # scenes, training cameras - is host logic in yoxel.parallel)
+        raise SystemExit(f"--gpus > 1 shards the frame workloads (cfg1, cfg2, cfg3, lod); "
+                         f"run {args.config} on one GPU")
     if cfg["kind"] == "train":
         return run_train(args, cfg)
     if cfg["kind"] == "batch":

@@ -455,7 +455,8 @@ def test_volume_tile_ranges_merge_to_the_full_frame(yoxel_mod, world):
     from yoxel import _lib as L
     from yoxel import parallel as P
     vol = yoxel_mod.BrickVolume.noise(2, 0.4, 1.4, 31)
-    d = vol.upload(3).desc()
+    gv = vol.upload(3)  # the device pool lives as long as this object
+    d = gv.desc()
     cams = [cam_at([1.6, 1.3, 1.1]), cam_at([-0.7, 0.4, 0.9], 50.0)]
     w, h = 100, 60
     ns = torch.zeros((2, h, w), dtype=torch.int32, device="cuda")
