@@ -673,9 +673,8 @@ def run_brick(args, cfg):
         # this rank's squares of warp tiles and the pixel rows they hold
         ranges = P.partition_volume_tiles(P.volume_tile_costs(ns.cpu().numpy(), w, h), ws)
         tb, te_t = ranges[rank]
-        stx = ((w + 7) // 8 + 1) // 2
         if te_t > tb:
-            y0, y1 = (tb // 8 // stx) * 16, min(h, ((te_t - 1) // 8 // stx + 1) * 16)
+            y0, y1 = P.volume_tile_rows((tb, te_t), w, h)
         share = float(ns[:, y0:y1].to(torch.int64).sum()) / max(1, S)
         alg = int(alg * share)  # this rank's part of the bytes (rows it covers)
         fn = lambda: yoxel.render_volume_tiles(desc, cam, w, h, tb, te_t, out,

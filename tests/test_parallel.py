@@ -173,3 +173,19 @@ def test_volume_tile_order_covers_the_frame_in_squares():
             assert rs[0][0] == 0 and rs[-1][1] == len(c)
             assert all(b % 8 == 0 and e % 8 == 0 and b <= e for b, e in rs)
             assert all(rs[i][1] == rs[i + 1][0] for i in range(world - 1))
+
+
+def test_volume_tile_rows_hold_the_range():
+    """The rows a rank of a split brick frame reads back hold every pixel of
+    its tile range (one camera)."""
+    from yoxel import parallel as P
+    for w, h in [(1024, 1024), (100, 60), (33, 17)]:
+        ox, oy = P.volume_tile_order(w, h)
+        n = len(ox)
+        for world in (2, 3, 4):
+            for tb, te in P.partition_volume_tiles(np.ones(n), world):
+                y0, y1 = P.volume_tile_rows((tb, te), w, h)
+                for t in range(tb, te):
+                    if ox[t] * 8 < w and oy[t] * 4 < h:
+                        assert y0 <= oy[t] * 4 and min(h, oy[t] * 4 + 4) <= y1
+

@@ -105,6 +105,16 @@ def partition_volume_tiles(tile_costs, world):
     return [(8 * b, 8 * e) for b, e in partition_tiles(sq, world)]
 
 
+def volume_tile_rows(tile_range, width, height):
+    """Pixel rows [y0, y1) of one camera's frame covered by a range of warp
+    tiles of the march's order (within one camera: ids < volume_tile_count)."""
+    tb, te = tile_range
+    if te <= tb:
+        return 0, 0
+    stx = ((width + 7) // 8 + 1) // 2
+    return (tb // 8 // stx) * 16, min(height, ((te - 1) // 8 // stx + 1) * 16)
+
+
 def partition_cameras(ncams, world):
     """Contiguous camera ranges per rank (data parallelism over views)."""
     base, extra = divmod(ncams, world)
