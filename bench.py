@@ -764,13 +764,27 @@ def run_brick(args, cfg):
 
 
 def run_train(args, cfg):
-    """cfg4: differentiable volume, forward + adjoint."""
+    """cfg4: differentiable volume, forward + adjoint.  Under torchrun
+    (N > 1): data parallel over the cameras (yoxel.parallel.partition_cameras),
+    each step ending in the exchange step - a sum all-reduce of the density
+    and albedo gradients (yoxel.parallel.sum_gradients) - inside the timed
+    region; `value` = all cameras' rays / the slowest rank's step (strong
+    scaling)."""
     import torch
     import yoxel
-    torch.cuda.set_device(dist_env()[2])
+    from yoxel import parallel as P
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
     from yoxel import workloads as W
     vol, tv, tgt_d, tgt_a, cam_list = W.cfg4_problem(cfg["levels"], cfg["cams"], cfg_seed(cfg))
-    cams = yoxel.cameras(cam_list)
+    c0, c1 = P.partition_cameras(len(cam_list), ws)[rank]
+    cams = yoxel.cameras(cam_list[c0:c1])  # this rank's cameras (all of them on one GPU)
+    ncam = c1 - c0
     w, h = cfg["width"], cfg["height"]
     a_s, st = cfg["alpha_scale"], cfg["step_vox"]
     target = yoxel.render_volume(yoxel.torch_desc(tv, tgt_d, tgt_a), cams, w, h, a_s, st)
@@ -784,8 +798,11 @@ def run_train(args, cfg):
         rgba = yoxel.volume_march(density, albedo, tv, cams, w, h, a_s, st)
         loss = ((rgba - target) ** 2).sum()
         loss.backward()
+        if pg is not None:
+            P.sum_gradients([density.grad, albedo.grad])  # the exchange step
+        return loss
 
-    fwd_out = torch.empty((cfg["cams"], h, w, 4), dtype=torch.float32, device="cuda")
+    fwd_out = torch.empty((ncam, h, w, 4), dtype=torch.float32, device="cuda")
     # forward-only and adjoint-only legs read the same packed float4 pool
     # that volume_march builds each step
     packed = yoxel.pack_volume(density.detach(), albedo.detach())
@@ -798,12 +815,14 @@ def run_train(args, cfg):
     for _ in range(args.warmup):
         fwd_bwd()
         fwd()
-    ns = torch.zeros((cfg["cams"], h, w), dtype=torch.int32, device="cuda")
+    ns = torch.zeros((ncam, h, w), dtype=torch.int32, device="cuda")
     yoxel.render_volume(desc, cams, w, h, a_s, st, out=fwd_out, samples=ns)
     S = int(ns.to(torch.int64).sum())
-    sampler = ClockSampler(dist_env()[2])
+    sampler = ClockSampler(local)
     sampler.start()
     time.sleep(0.4)
+    if pg is not None:
+        pg.barrier()
     ms_fb, wall = _timed_steps(torch, args.steps, fwd_bwd, lambda: flush.fill_(1))
     ms_f, _ = _timed_steps(torch, args.steps, fwd, lambda: flush.fill_(1))
     # the adjoint kernel alone (dominant kernel of the step)
@@ -818,12 +837,21 @@ def run_train(args, cfg):
     fb = sum(ms_fb) / len(ms_fb)
     f = sum(ms_f) / len(ms_f)
     b = sum(ms_b) / len(ms_b)
+    b_mine = b
+    if pg is not None:
+        tot = torch.tensor([fb, f, b], dtype=torch.float64, device="cuda")
+        pg.all_reduce(tot, op=pg.ReduceOp.MAX)
+        fb, f, b = (float(x) for x in tot)
     peaks, kind = measured_peaks()
     # adjoint bytes: replay of the fp32 forward reads (8 x (4 + 12) B per
     # sample) + the same again as gradient atomics + 32 B/ray (rgba, dL/drgba)
-    alg_b = 2 * 128 * S + 32 * rays
-    achieved = alg_b / (b / 1e3) / 1e9
+    alg_b = 2 * 128 * S + 32 * ncam * w * h  # this rank's launch
+    achieved = alg_b / (b_mine / 1e3) / 1e9
     line = _base_line(args, cfg, rays / (fb / 1e3) / 1e6, fb, "f32")
+    if ws > 1:
+        line["scaling"] = "strong"
+        line["config"]["parallelism"] = (f"data parallel over the {cfg['cams']} cameras on "
+                                         f"{ws} GPUs, gradient sum all-reduce each step")
     line["config"].update(rays_per_step=rays, mean_samples_per_ray=round(S / rays, 2),
                           bricks=vol.nbricks)
     line.update({
@@ -847,23 +875,31 @@ def run_train(args, cfg):
                           "differences: rel. error <= 1e-4 (tests/test_volume_gpu.py)",
         # per fwd+bwd step: pack, forward, adjoint, unpack, 2 x (fold gather +
         # scatter); the loss and its gradient are torch's own kernels
-        "gpu_launches": args.steps * (6 + 2 * -(-cfg["cams"] // 64)),
+        "gpu_launches": args.steps * (6 + 2 * -(-ncam // 64)),
         "clocks": clocks, "wall_s_timed_region": round(wall, 4)})
     host = torch.empty((), dtype=torch.float32, pin_memory=True)
     torch.cuda.synchronize()
+    if pg is not None:
+        pg.barrier()
     te = time.perf_counter()
     for _ in range(args.steps):
-        density.grad = None
-        albedo.grad = None
-        rgba = yoxel.volume_march(density, albedo, tv, cams, w, h, a_s, st)
-        loss = ((rgba - target) ** 2).sum()
-        loss.backward()
+        loss = fwd_bwd()
         host.copy_(loss.detach())  # D2H of the step's loss
     e2e = (time.perf_counter() - te) / args.steps
+    if pg is not None:
+        t = torch.tensor([e2e], dtype=torch.float64, device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e2e = float(t[0])
+        if rank != 0:
+            pg.destroy_process_group()
+            return
     line["e2e"] = {"value": round(rays / e2e / 1e6, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 4,
-                   "path": "yoxel.volume_march + L2 loss + backward, loss read on the host"}
+                   "path": "yoxel.volume_march + L2 loss + backward, loss read on the host"
+                           + (" (each rank its cameras, gradient all-reduce)" if ws > 1 else "")}
     print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
 
 
 def run_batch(args, cfg):
@@ -1364,14 +1400,14 @@ def main():
         return run_svo(args, cfg)
     if cfg["kind"] == "brick":
         return run_brick(args, cfg)
-    if dist_env()[0] > 1:
-        # the multi-GPU form shards one frame by tile ranges (SVO and brick
-        # frames); the other workloads run on one GPU (their sharding - batch
-        # scenes, training cameras - is host logic in yoxel.parallel)
-        raise SystemExit(f"--gpus > 1 shards the frame workloads (cfg1, cfg2, cfg3, lod); "
-                         f"run {args.config} on one GPU")
     if cfg["kind"] == "train":
         return run_train(args, cfg)
+    if dist_env()[0] > 1:
+        # the multi-GPU forms: one frame split by tile ranges (SVO and brick
+        # frames) and data-parallel training; the other workloads run on one
+        # GPU (splitting a batch by scenes is host logic in yoxel.parallel)
+        raise SystemExit(f"--gpus > 1 runs the frame and training workloads (cfg1, cfg2, "
+                         f"cfg3, cfg4, lod); run {args.config} on one GPU")
     if cfg["kind"] == "batch":
         return run_batch(args, cfg)
     if cfg["kind"] == "build":
