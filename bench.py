@@ -903,13 +903,29 @@ def run_train(args, cfg):
 
 
 def run_batch(args, cfg):
-    """cfg5: batched persistent launch vs per-scene launches."""
+    """cfg5: batched persistent launch vs per-scene launches.  Under torchrun
+    (N > 1) the scenes are split across the ranks (largest-first greedy on
+    pixels, a brick pixel weighing 4; yoxel.parallel.partition_scenes), each
+    rank batches its own, and `value` = all scenes' rays / the slowest rank's
+    batch (strong scaling); no collective on the data path."""
     import torch
     import yoxel
     from yoxel import autotune
+    from yoxel import parallel as P
     from yoxel import workloads as W
-    torch.cuda.set_device(dist_env()[2])
-    specs = W.cfg5_specs(cfg_seed(cfg), cfg["n"])
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    pg = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        pg = dist
+    all_specs = W.cfg5_specs(cfg_seed(cfg), cfg["n"])
+    all_rays = sum(sp["res"] ** 2 for sp in all_specs)
+    specs = all_specs
+    if ws > 1:
+        costs = [sp["res"] ** 2 * (4 if sp["kind"] != "svo" else 1) for sp in all_specs]
+        specs = [all_specs[i] for i in P.partition_scenes(costs, ws)[rank]]
     prec = cfg["precision"] if args.precision is None else args.precision
     t_scene = time.perf_counter()
     batch, items = W.cfg5_batch(specs, prec)
@@ -937,14 +953,16 @@ def run_batch(args, cfg):
         rays += res * res
     t_scene = time.perf_counter() - t_scene
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    best, _ = autotune.tune_batch(batch, f"cfg5-{cfg['n']}", reps=2,
-                                  flush=lambda: flush.fill_(1))
+    best, _ = autotune.tune_batch(batch, f"cfg5-{cfg['n']}" + (f"-r{rank}of{ws}" if ws > 1 else ""),
+                                  reps=2, flush=lambda: flush.fill_(1))
     for _ in range(args.warmup):
         batch.render(graph=True)
         batch.render_separate()
-    sampler = ClockSampler(dist_env()[2])
+    sampler = ClockSampler(local)
     sampler.start()
     time.sleep(0.4)
+    if pg is not None:
+        pg.barrier()
     ms_b, wall = _timed_steps(torch, args.steps, lambda: batch.render(graph=True),
                               lambda: flush.fill_(1))
     ms_s, _ = _timed_steps(torch, args.steps, batch.render_separate, lambda: flush.fill_(1))
@@ -965,8 +983,20 @@ def run_batch(args, cfg):
         torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - te) / args.steps
     peaks, kind = measured_peaks()
-    achieved = alg / (tb / 1e3) / 1e9
+    achieved = alg / (tb / 1e3) / 1e9  # this rank's batch
+    if pg is not None:
+        tot = torch.tensor([tb, ts, tp, e2e_s], dtype=torch.float64, device="cuda")
+        pg.all_reduce(tot, op=pg.ReduceOp.MAX)
+        tb, ts, tp, e2e_s = (float(x) for x in tot)
+        if rank != 0:
+            pg.destroy_process_group()
+            return
+    rays = all_rays
     line = _base_line(args, cfg, rays / (tb / 1e3) / 1e6, tb, "f32")
+    if ws > 1:
+        line["scaling"] = "strong"
+        line["config"]["parallelism"] = (f"the {len(all_specs)} scenes split across {ws} GPUs "
+                                         f"(rank 0: {len(specs)} scenes)")
     line["config"].update(scenes=len(specs), rays_per_step=rays,
                           svo_scenes=sum(1 for s in specs if s["kind"] == "svo"),
                           launch_config=best)
@@ -985,6 +1015,8 @@ def run_batch(args, cfg):
                 "path": "yoxel.Batch.render (CUDA graph replay) + copy of all frames into "
                         "pinned host memory; scenes and cameras resident on the device"}})
     print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
 
 
 def sphere_density(torch, G, n, seed, device):
@@ -1402,14 +1434,14 @@ def main():
         return run_brick(args, cfg)
     if cfg["kind"] == "train":
         return run_train(args, cfg)
-    if dist_env()[0] > 1:
-        # the multi-GPU forms: one frame split by tile ranges (SVO and brick
-        # frames) and data-parallel training; the other workloads run on one
-        # GPU (splitting a batch by scenes is host logic in yoxel.parallel)
-        raise SystemExit(f"--gpus > 1 runs the frame and training workloads (cfg1, cfg2, "
-                         f"cfg3, cfg4, lod); run {args.config} on one GPU")
     if cfg["kind"] == "batch":
         return run_batch(args, cfg)
+    if dist_env()[0] > 1:
+        # the multi-GPU forms: one frame split by tile ranges (SVO and brick
+        # frames), data-parallel training, a batch split by scenes; the
+        # builders and the edit loop run on one GPU
+        raise SystemExit(f"--gpus > 1 runs the frame, training and batch workloads (cfg1-5, "
+                         f"lod); run {args.config} on one GPU")
     if cfg["kind"] == "build":
         return run_build(args, cfg)
     if cfg["kind"] == "vbuild":
